@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the exhaustive epistasis search on GB300.
+
+One step = one complete scan (every combination of the workload, top-N
+selection and FP64 re-score included) over the seeded synthetic data set of
+the named workload; the default is order 3 over 2 000 SNPs x 8 000 samples
+(4 000 cases / 4 000 controls), top-100.
+
+Output: one JSON line (rank 0).  ``value`` is combinations x samples per second
+with the data set resident in HBM; ``e2e`` is the same metric through the
+public host-buffer call (``fiu_search``: pinned host data set -> device ->
+search -> results to host, all inside the timed region).  ``roofline`` is the
+HBM roofline of the dominant kernel and ``int_roofline`` its integer
+(AND+POPC) roofline against a peak measured live on this GPU.
+``cpu_baseline`` times the CPU oracle (a C restatement of the reference's
+scalar search) on a bounded prefix sample of the same workload on the host
+cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload order3_2000x8000]
+
+With --gpus N > 1 (launched by torch.distributed.run), every rank takes the
+Distribution(snps, order-1, N, rank) share of the prefixes (no data-path
+collective), rank 0 gathers the top-N lists; value = all ranks' work / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k=3 combos×samples/s, batched/served vs plain, 1 GB300; scan p50/p99 latency"
+UNIT = "combos*samples/s"
+
+
+# ----------------------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def combos_of(n, k, step=1, offset=0):
+    """Combinations owned by Distribution(n, k-1, step, offset): sum over owned prefixes of (n-1-last)."""
+    if step == 1 and offset == 0:
+        return math.comb(n, k)
+    from oracle.oracle import Oracle  # exact count from the enumeration (small samples only)
+    p = Oracle().prefixes(n, k - 1, step, offset)
+    return int(np.sum(n - 1 - p[:, -1])) if len(p) else 0
+
+
+def cpu_sample(spec, ds, seconds=10.0, threads=None):
+    """The CPU oracle (C restatement of the reference's scalar search) on a
+    uniform sample of the workload's prefixes, sized to about `seconds` of work."""
+    from oracle.oracle import Oracle
+    o = Oracle()
+    threads = threads or os.cpu_count() or 1
+    n_pref = math.comb(spec.snps, spec.order - 1)
+    step = max(1, n_pref // (threads * 4))
+    while True:
+        t0 = time.perf_counter()
+        _, _, _, done = o.search(ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words,
+                                 spec.order, spec.outputs, threads=threads, mi_mode=0, dist=(spec.snps, step, 0))
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 or step == 1:
+            break
+        step = max(1, step // 8)
+    # rescale the sample to ~`seconds`
+    if dt < seconds and step > 1:
+        step = max(1, int(step * dt / seconds))
+        t0 = time.perf_counter()
+        _, _, _, done = o.search(ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words,
+                                 spec.order, spec.outputs, threads=threads, mi_mode=0, dist=(spec.snps, step, 0))
+        dt = time.perf_counter() - t0
+    rate = done * spec.samples / dt
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "every %d-th (order-%d)-prefix of the workload (%d combinations, %.1f s)" %
+                      (step, spec.order - 1, done, dt)}
+
+
+# ----------------------------------------------------------------------------- reference arm
+def run_reference(args, spec):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from fiuncho_gb300 import Dataset, synth
+    from oracle.oracle import Oracle
+    geno, is_case, _ = synth.simulate(spec)
+    ds = Dataset.from_genotypes(geno, is_case)
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    n_pref = math.comb(spec.snps, spec.order - 1)
+    step = max(1, n_pref // (threads * 64))  # ~1/64 of the prefixes per thread-round, a few seconds
+    times, done_all = [], 0
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, _, _, done = o.search(ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words, spec.order,
+                                 spec.outputs, threads=threads, mi_mode=0, dist=(spec.snps, step, it % step))
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+            done_all += done
+    total = sum(times)
+    value = done_all * spec.samples / total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": args.workload, "snps": spec.snps, "cases": spec.cases, "ctrls": spec.ctrls,
+                       "order": spec.order, "outputs": spec.outputs,
+                       "step_sample": "every %d-th prefix (offset rotates per step)" % step},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "every %d-th (order-%d)-prefix per step" % (step, spec.order - 1)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GB300 arm
+def run_gpu(args, spec):
+    ws, rank, local = dist_env()
+    import ctypes as C
+
+    import torch
+
+    from fiuncho_gb300 import Context, Dataset, Distribution, GpuSearch, Resident, synth, _lib
+
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    geno, is_case, planted = synth.simulate(spec)
+    ds = Dataset.from_genotypes(geno, is_case)
+    gs = GpuSearch(local)
+    ctx = gs.ctx
+    lib = ctx.lib
+    res = Resident(ctx, ds)
+    dist_ = Distribution(ds.snps, spec.order - 1, ws, rank)
+    combos = combos_of(ds.snps, spec.order, ws, rank) if ws > 1 else math.comb(ds.snps, spec.order)
+    total_combos = math.comb(ds.snps, spec.order)
+    stream = torch.cuda.ExternalStream(lib.fiu_stream(ctx.h), device=torch.device("cuda", local))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 512 MB > L2 (129 MB)
+
+    peak_rate = C.c_double(0)
+    ctx.check(lib.fiu_probe_popc_rate(ctx.h, C.byref(peak_rate)))
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        out = gs.run(res, spec.order, dist_, spec.outputs)
+    # ---- timed region: resident data set, one event pair per step on the library's stream
+    ctx.check(lib.fiu_set_kernel_timing(ctx.h, 1))
+    launches0 = ctx.launches
+    step_ms = []
+    with ClockSampler(local) as clocks:
+        barrier()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = gs.run(res, spec.order, dist_, spec.outputs)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+        barrier()
+    launches = ctx.launches - launches0
+    kms, klaunch, kcombos = C.c_double(0), C.c_uint64(0), C.c_uint64(0)
+    ctx.check(lib.fiu_kernel_timing(ctx.h, C.byref(kms), C.byref(klaunch), C.byref(kcombos)))
+    ctx.check(lib.fiu_set_kernel_timing(ctx.h, 0))
+    my_time = sum(step_ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([my_time], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        my_time = float(t.item())
+        from fiuncho_gb300 import MPIEngine
+        out = MPIEngine().gather(out, spec.outputs)
+    value = total_combos * spec.samples * args.steps / my_time
+
+    # ---- end to end through the public host-buffer call (pinned host data set)
+    pinned = torch.empty(ds.data.size, dtype=torch.int64, pin_memory=True)
+    pinned.numpy().view(np.uint64)[:] = ds.data
+    hds = _lib.Dataset_t(C.cast(C.c_void_p(pinned.data_ptr()), C.POINTER(C.c_uint64)), ds.snps, ds.cases, ds.ctrls,
+                         ds.cases_words, ds.ctrls_words)
+    comb = np.zeros(spec.outputs * spec.order, np.int32)
+    vals = np.zeros(spec.outputs, np.float32)
+    cnt = C.c_uint(0)
+    dstruct = dist_.c_struct()
+
+    def e2e_call():
+        ctx.check(lib.fiu_search(ctx.h, C.byref(hds), spec.order, C.byref(dstruct), spec.outputs,
+                                 _lib.ptr(comb, C.c_int32), _lib.ptr(vals, C.c_float), C.byref(cnt)))
+
+    e2e_call()
+    e2e_t = []
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_call()
+        e2e_t.append(time.perf_counter() - t0)
+    barrier()
+    e2e_time = sum(e2e_t)
+    if ws > 1:
+        t = torch.tensor([e2e_time], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_time = float(t.item())
+    e2e_value = total_combos * spec.samples * args.steps / e2e_time
+
+    if rank != 0:
+        return
+    # ---- roofline of the dominant (counting) kernel
+    k = spec.order
+    ops_per_combo = 3 ** k * (math.ceil(spec.cases / 32) + math.ceil(spec.ctrls / 32))
+    avg_launch_s = (kms.value / 1e3) / max(1, klaunch.value)
+    ops_per_launch = kcombos.value * ops_per_combo / max(1, klaunch.value)
+    int_achieved = ops_per_launch / avg_launch_s if avg_launch_s > 0 else 0.0
+    ds_bytes = ds.data.size * 8
+    hbm_bytes_per_launch = ds_bytes / max(1, klaunch.value / args.steps)
+    hbm_achieved = hbm_bytes_per_launch / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    try:
+        traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(args.workload)
+    except (OSError, ValueError):
+        pass
+    top = out[0] if out else None
+    cpu = cpu_sample(spec, ds, seconds=args.cpu_seconds) if args.cpu_seconds > 0 and ws == 1 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * my_time / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": args.workload, "snps": spec.snps, "cases": spec.cases, "ctrls": spec.ctrls,
+                   "order": spec.order, "outputs": spec.outputs, "combinations": total_combos,
+                   "parallelism": "prefix-distribution over %d rank(s)" % ws,
+                   "l2": "flushed between steps (512 MB write); data set %.1f MB is L2-resident by design"
+                         % (ds_bytes / 1e6),
+                   "top1": (top.combination if top else None), "planted": [list(p) for p in planted]},
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ds_bytes,
+                "d2h_bytes_per_step": spec.outputs * (4 * spec.order + 4) + 8 * 2},
+        "roofline": {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": hbm_achieved / hbm_peak, "traffic": traffic,
+                     "note": "algorithmic bytes = the data set read once per scan; the kernel is integer-pipe "
+                             "bound (int_roofline)"},
+        "int_roofline": {"bound": "int", "achieved": int_achieved / 1e12, "peak": peak_rate.value / 1e12,
+                         "unit": "T word-ops/s", "frac": int_achieved / peak_rate.value if peak_rate.value else None,
+                         "work": "3^k*(ceil(cases/32)+ceil(ctrls/32)) 32-bit AND+POPC per combination",
+                         "peak_source": "fiu_probe_popc_rate on this GPU (AND+POPC+ADD microbenchmark)"},
+        "kernel": {"count_ms_total": kms.value, "count_launches": klaunch.value, "combinations": kcombos.value},
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="order3_2000x8000")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--snps", type=int, default=0, help="override the SNP count (small profiling cases)")
+    args = ap.parse_args()
+    import dataclasses
+
+    from fiuncho_gb300 import synth
+    spec = synth.WORKLOADS[args.workload]
+    if args.snps:
+        spec = dataclasses.replace(spec, snps=args.snps)
+        args.workload = "%s@%dsnps" % (args.workload, args.snps)
+    if args.impl == "reference":
+        run_reference(args, spec)
+    else:
+        run_gpu(args, spec)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,550 @@
+// C ABI of the library (include/fiuncho_gpu.h): contexts, resident data sets,
+// the search driver and the kernel-level entries.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/fiuncho_gpu.h"
+#include "internal.h"
+
+namespace fiu {
+thread_local unsigned long long* g_launch_counter = nullptr;
+}
+
+using namespace fiu;
+
+struct fiu_ctx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    unsigned long long launches = 0;
+    // growable scratch of the search driver
+    Cand* cand = nullptr;  // candidate buffer
+    size_t cand_cap = 0;
+    Cand* tmp = nullptr;   // select_top working space
+    size_t tmp_cap = 0;
+    unsigned* ctl = nullptr;  // [0] count, [1] overflow, [2..] select scratch (262)
+    double* mi64 = nullptr;
+    size_t mi64_cap = 0;
+    unsigned* pinned = nullptr;  // host mirror of ctl[0..1]
+    // optional timing of the counting kernels (CUDA events on `stream`)
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double count_ms = 0;
+    unsigned long long count_launches = 0;
+    unsigned long long* evaluated = nullptr;  // device counter of combinations evaluated
+};
+
+struct fiu_resident {
+    DevData d{};
+    uint64_t* ref = nullptr;
+    uint64_t* tr = nullptr;
+    long long* ftab = nullptr;
+    long long ftab_max = 0;
+    int one_hot = 0;
+    int device = 0;
+};
+
+namespace {
+
+struct Scope {  // routes launch counting of this thread to the context
+    explicit Scope(fiu_ctx* c) { g_launch_counter = &c->launches; }
+    ~Scope() { g_launch_counter = nullptr; }
+};
+
+int fail(fiu_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_fail(fiu_ctx* ctx, cudaError_t e, const char* what) {
+    const int code = e == cudaErrorMemoryAllocation ? FIU_ERR_NOMEM : FIU_ERR_CUDA;
+    return fail(ctx, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (expr);                         \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+template <typename T>
+int grow(fiu_ctx* ctx, T*& p, size_t& cap, size_t need) {
+    if (need <= cap) return FIU_OK;
+    const size_t n = std::max(need, cap * 2);
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc((void**)&p, n * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "device scratch allocation");
+    cap = n;
+    return FIU_OK;
+}
+
+int bits_for(long long n) {
+    int b = 1;
+    while ((1ll << b) < n) ++b;
+    return b;
+}
+
+// Validates (order, distribution, outputs) against a data set and fills the work description.
+int make_work(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
+              unsigned outputs, ScanWork& w) {
+    if (!res) return fail(ctx, FIU_ERR_INVALID, "null data set");
+    if (order < 2 || order > FIU_MAX_ORDER)
+        return fail(ctx, order < 2 ? FIU_ERR_INVALID : FIU_ERR_UNSUPPORTED, "order must be in [2, 8]");
+    if (outputs > FIU_MAX_OUTPUTS) return fail(ctx, FIU_ERR_UNSUPPORTED, "outputs above FIU_MAX_OUTPUTS");
+    fiu_distribution dd{res->d.snps, (int)order - 1, 1, 0};
+    if (dist) dd = *dist;
+    if (dd.k != (int)order - 1) return fail(ctx, FIU_ERR_INVALID, "distribution.k must be order - 1");
+    if (dd.step < 1 || dd.offset < 0 || dd.n < 0 || dd.n > res->d.snps)
+        return fail(ctx, FIU_ERR_INVALID, "distribution needs step >= 1, offset >= 0, 0 <= n <= snps");
+    const int bits = bits_for(res->d.snps);
+    if ((long long)bits * order > 64)
+        return fail(ctx, FIU_ERR_UNSUPPORTED, "order x index bits exceeds 64 (too many SNPs for this order)");
+    for (int j = 0; j <= dd.k; ++j)
+        if (binom(dd.n, j) >= (1ull << 62)) return fail(ctx, FIU_ERR_UNSUPPORTED, "combination count overflow");
+    const unsigned long long total = binom(dd.n, dd.k);
+    w.d = res->d;
+    w.order = (int)order;
+    w.dist_n = dd.n;
+    w.dist_step = dd.step;
+    w.dist_offset = dd.offset;
+    w.bits = bits;
+    w.n_prefixes = (unsigned long long)dd.offset < total ? (long long)((total - 1 - dd.offset) / dd.step + 1) : 0;
+    const long long N = (long long)res->d.n_cases + res->d.n_ctrls;
+    auto T = [](long long c) -> long long {
+        return c < 2 ? 0 : (long long)llround((double)c * std::log((double)c) * 4294967296.0);
+    };
+    w.base_key = T(N) - T(res->d.n_cases) - T(res->d.n_ctrls);
+    return FIU_OK;
+}
+
+// The search on a resident data set (ThreadedSearch::run semantics).
+int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
+                unsigned outputs, int32_t* out_comb, float* out_vals, double* out_vals64, unsigned* out_count,
+                int kernel) {
+    if (!ctx) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    if (!out_count || (outputs && (!out_comb || !out_vals)))
+        return fail(ctx, FIU_ERR_INVALID, "null output pointer");
+    *out_count = 0;
+    ScanWork w;
+    int rc = make_work(ctx, res, order, dist, outputs, w);
+    if (rc) return rc;
+    if (outputs == 0 || w.n_prefixes == 0) return FIU_OK;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const unsigned keep = outputs + std::max(32u, outputs / 8);
+    const size_t cap = std::max<size_t>({65536, (size_t)16 * keep, (size_t)res->d.snps + keep});
+    if ((rc = grow(ctx, ctx->cand, ctx->cand_cap, cap)) ||
+        (rc = grow(ctx, ctx->tmp, ctx->tmp_cap, cap + 8192)) ||
+        (rc = grow(ctx, ctx->mi64, ctx->mi64_cap, (size_t)keep)))
+        return rc;
+    cudaStream_t s = ctx->stream;
+    unsigned* count = ctx->ctl;
+    unsigned* overflow = ctx->ctl + 1;
+    unsigned* scratch = ctx->ctl + 4;
+    long long thr = (long long)0x8000000000000000ull;
+    unsigned have = 0;
+    const double per_prefix = (double)binom(w.dist_n, order) / std::max<double>(1.0, (double)binom(w.dist_n, order - 1));
+    long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_prefix)));
+    long long m = 0;
+    while (m < w.n_prefixes) {
+        const long long m1 = std::min(w.n_prefixes, m + chunk);
+        ctx->pinned[0] = have;
+        ctx->pinned[1] = 0;
+        CK(cudaMemcpyAsync(count, ctx->pinned, 2 * sizeof(unsigned), cudaMemcpyHostToDevice, s), "reset counters");
+        CandSink sink{ctx->cand, count, overflow, (unsigned)cap, thr, ctx->timing ? ctx->evaluated : nullptr};
+        if (ctx->timing) CK(cudaEventRecord(ctx->ev0, s), "event");
+        CK(launch_count(kernel, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
+        if (ctx->timing) CK(cudaEventRecord(ctx->ev1, s), "event");
+        CK(cudaMemcpyAsync(ctx->pinned, count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read counters");
+        CK(cudaStreamSynchronize(s), "count kernel");
+        if (ctx->timing) {
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
+            ctx->count_ms += ms;
+            ctx->count_launches += 1;
+        }
+        const unsigned M = std::min<unsigned>(ctx->pinned[0], (unsigned)cap);
+        if (ctx->pinned[1]) {  // overflow: drop this chunk's candidates and retry smaller
+            if (m1 - m == 1) return fail(ctx, FIU_ERR_UNSUPPORTED, "candidate buffer overflow on one prefix");
+            chunk = std::max<long long>(1, (m1 - m) / 4);
+            continue;
+        }
+        const unsigned fresh = M - have;
+        if (M > keep) {
+            CK(select_top(ctx->cand, M, keep, ctx->tmp, scratch, s), "top-N selection");
+            Cand last;
+            CK(cudaMemcpyAsync(&last, ctx->cand + keep - 1, sizeof(Cand), cudaMemcpyDeviceToHost, s), "threshold");
+            CK(cudaStreamSynchronize(s), "top-N selection");
+            thr = last.key;
+            have = keep;
+        } else {
+            have = M;
+        }
+        m = m1;
+        if (fresh < cap / 8) chunk *= 4;
+        else if (fresh > cap / 2) chunk = std::max<long long>(1, chunk / 2);
+    }
+    // Final order of the kept set, then FP64 re-score of every kept candidate.
+    CK(select_top(ctx->cand, have, keep, ctx->tmp, scratch, s), "top-N selection");
+    const unsigned n = std::min(have, keep);
+    CK(rescore_sort(w.d, (int)order, w.bits, ctx->cand, n, ctx->mi64, s), "FP64 rescore");
+    const unsigned nout = std::min(n, outputs);
+    std::vector<Cand> hc(nout);
+    std::vector<double> hv(nout);
+    CK(cudaMemcpyAsync(hc.data(), ctx->cand, nout * sizeof(Cand), cudaMemcpyDeviceToHost, s), "results");
+    CK(cudaMemcpyAsync(hv.data(), ctx->mi64, nout * sizeof(double), cudaMemcpyDeviceToHost, s), "results");
+    CK(cudaStreamSynchronize(s), "results");
+    for (unsigned i = 0; i < nout; ++i) {
+        int c[kMaxOrder];
+        unpack_code(hc[i].code, (int)order, w.bits, c);
+        for (unsigned t = 0; t < order; ++t) out_comb[(size_t)i * order + t] = c[t];
+        out_vals[i] = (float)hv[i];
+        if (out_vals64) out_vals64[i] = hv[i];
+    }
+    *out_count = nout;
+    return FIU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fiu_create(int device, fiu_ctx** out) {
+    if (!out) return FIU_ERR_INVALID;
+    *out = nullptr;
+    auto* ctx = new (std::nothrow) fiu_ctx;
+    if (!ctx) return FIU_ERR_NOMEM;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n) {
+        delete ctx;
+        return e != cudaSuccess ? FIU_ERR_CUDA : FIU_ERR_INVALID;
+    }
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc((void**)&ctx->ctl, 512 * sizeof(unsigned)) != cudaSuccess ||
+        cudaMallocHost((void**)&ctx->pinned, 16 * sizeof(unsigned)) != cudaSuccess) {
+        fiu_destroy(ctx);
+        return FIU_ERR_CUDA;
+    }
+    *out = ctx;
+    return FIU_OK;
+}
+
+void fiu_destroy(fiu_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->cand);
+    cudaFree(ctx->tmp);
+    cudaFree(ctx->ctl);
+    cudaFree(ctx->mi64);
+    cudaFree(ctx->evaluated);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* fiu_last_error(const fiu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+uint64_t fiu_launch_count(const fiu_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+void* fiu_stream(const fiu_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int fiu_set_kernel_timing(fiu_ctx* ctx, int enable) {
+    if (!ctx) return FIU_ERR_INVALID;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (enable && !ctx->ev0) {
+        CK(cudaEventCreate(&ctx->ev0), "event");
+        CK(cudaEventCreate(&ctx->ev1), "event");
+        CK(cudaMalloc((void**)&ctx->evaluated, sizeof(unsigned long long)), "counter");
+    }
+    if (enable) CK(cudaMemsetAsync(ctx->evaluated, 0, sizeof(unsigned long long), ctx->stream), "counter");
+    CK(cudaStreamSynchronize(ctx->stream), "counter");
+    ctx->timing = enable != 0;
+    ctx->count_ms = 0;
+    ctx->count_launches = 0;
+    return FIU_OK;
+}
+
+int fiu_kernel_timing(const fiu_ctx* ctx_c, double* count_ms, uint64_t* count_launches, uint64_t* combinations) {
+    fiu_ctx* ctx = const_cast<fiu_ctx*>(ctx_c);
+    if (!ctx) return FIU_ERR_INVALID;
+    if (count_ms) *count_ms = ctx->count_ms;
+    if (count_launches) *count_launches = ctx->count_launches;
+    if (combinations) {
+        unsigned long long v = 0;
+        if (ctx->evaluated) {
+            CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+            CK(cudaMemcpyAsync(&v, ctx->evaluated, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream), "counter");
+            CK(cudaStreamSynchronize(ctx->stream), "counter");
+        }
+        *combinations = v;
+    }
+    return FIU_OK;
+}
+
+int fiu_probe_popc_rate(fiu_ctx* ctx, double* rate) {
+    if (!ctx || !rate) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(probe_popc_rate(ctx->sms, ctx->stream, rate), "popc probe");
+    return FIU_OK;
+}
+
+int fiu_dataset_upload(fiu_ctx* ctx, const fiu_dataset* h, fiu_resident** out) {
+    if (!ctx || !out) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    *out = nullptr;
+    if (!h || !h->data) return fail(ctx, FIU_ERR_INVALID, "null data set");
+    if (h->snps < 1 || h->snps > 0x7fffffffull || h->cases_words > 0x7fffffffull / 8 ||
+        h->ctrls_words > 0x7fffffffull / 8)
+        return fail(ctx, FIU_ERR_INVALID, "data set sizes out of range");
+    if (h->cases > 64 * h->cases_words || h->ctrls > 64 * h->ctrls_words)
+        return fail(ctx, FIU_ERR_INVALID, "more samples than the row words hold");
+    if (h->cases + h->ctrls == 0) return fail(ctx, FIU_ERR_INVALID, "empty data set");
+    if (h->cases_words + h->ctrls_words == 0) return fail(ctx, FIU_ERR_INVALID, "rows without words");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    auto* r = new (std::nothrow) fiu_resident;
+    if (!r) return fail(ctx, FIU_ERR_NOMEM, "host allocation");
+    r->device = ctx->device;
+    const int snps = (int)h->snps, cw = (int)h->cases_words, tw = (int)h->ctrls_words;
+    const size_t rows = 3 * (size_t)(cw + tw);
+    const size_t words = (size_t)snps * rows;
+    const long long tmax = 64ll * (cw + tw);
+    std::vector<long long> ftab(tmax + 1);
+    for (long long c = 0; c <= tmax; ++c)
+        ftab[c] = c < 2 ? 0 : (long long)llround((double)c * std::log((double)c) * 4294967296.0);
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMalloc((void**)&r->ref, words * 8);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&r->tr, words * 8);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&r->ftab, ftab.size() * 8);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r->ref, h->data, words * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r->ftab, ftab.data(), ftab.size() * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_transpose(r->ref, r->tr, snps, (int)rows, s);
+    int* bad = (int*)(ctx->ctl + 300);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = launch_onehot_check(r->ref, snps, cw, tw, (int)h->cases, (int)h->ctrls, bad, s);
+    int hb = 1;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        fiu_dataset_free(ctx, r);
+        return cuda_fail(ctx, e, "data set upload");
+    }
+    r->one_hot = hb == 0;
+    r->ftab_max = tmax;
+    r->d = DevData{r->ref, r->tr, r->ftab, snps, cw, tw, (int)h->cases, (int)h->ctrls};
+    *out = r;
+    return FIU_OK;
+}
+
+void fiu_dataset_free(fiu_ctx* ctx, fiu_resident* r) {
+    if (!r) return;
+    if (ctx) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    cudaFree(r->ref);
+    cudaFree(r->tr);
+    cudaFree(r->ftab);
+    delete r;
+}
+
+int fiu_dataset_is_one_hot(const fiu_resident* r) { return r ? r->one_hot : 0; }
+
+int fiu_search(fiu_ctx* ctx, const fiu_dataset* dataset, unsigned order, const fiu_distribution* distribution,
+               unsigned outputs, int32_t* out_combinations, float* out_vals, unsigned* out_count) {
+    fiu_resident* r = nullptr;
+    int rc = fiu_dataset_upload(ctx, dataset, &r);
+    if (rc) return rc;
+    rc = search_impl(ctx, r, order, distribution, outputs, out_combinations, out_vals, nullptr, out_count, 0);
+    fiu_dataset_free(ctx, r);
+    return rc;
+}
+
+int fiu_search_resident(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* distribution,
+                        unsigned outputs, int32_t* out_combinations, float* out_vals, unsigned* out_count) {
+    return search_impl(ctx, res, order, distribution, outputs, out_combinations, out_vals, nullptr, out_count, 0);
+}
+
+int fiu_search_resident64(fiu_ctx* ctx, const fiu_resident* res, unsigned order,
+                          const fiu_distribution* distribution, unsigned outputs, int32_t* out_combinations,
+                          float* out_vals, double* out_vals64, unsigned* out_count) {
+    return search_impl(ctx, res, order, distribution, outputs, out_combinations, out_vals, out_vals64, out_count, 0);
+}
+
+int fiu_combine(fiu_ctx* ctx, const uint64_t* t1, unsigned size1, const uint64_t* t2, uint64_t cases_words,
+                uint64_t ctrls_words, uint64_t* out) {
+    if (!ctx) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    if (!t1 || !t2 || !out || size1 == 0 || cases_words + ctrls_words == 0 || cases_words > (1u << 28) ||
+        ctrls_words > (1u << 28) || size1 > (1u << 20))
+        return fail(ctx, FIU_ERR_INVALID, "invalid combine arguments");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t n1 = (size_t)size1 * (cases_words + ctrls_words), n2 = 3 * (cases_words + ctrls_words),
+                 no = 3 * n1;
+    uint64_t *d1 = nullptr, *d2 = nullptr, *dout = nullptr;
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMallocAsync((void**)&d1, n1 * 8, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&d2, n2 * 8, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dout, no * 8, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d1, t1, n1 * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d2, t2, n2 * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_combine(d1, (int)size1, d2, (int)cases_words, (int)ctrls_words, dout, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, no * 8, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d1, s);
+    cudaFreeAsync(d2, s);
+    cudaFreeAsync(dout, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "combine");
+    return FIU_OK;
+}
+
+int fiu_combine_and_popcnt(fiu_ctx* ctx, const uint64_t* t1, unsigned size1, const uint64_t* t2,
+                           uint64_t cases_words, uint64_t ctrls_words, uint32_t* cases_out, uint32_t* ctrls_out,
+                           unsigned ct_size) {
+    if (!ctx) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    if (!t1 || !t2 || !cases_out || !ctrls_out || size1 == 0 || ct_size < 3 * size1 ||
+        cases_words + ctrls_words == 0 || cases_words > (1u << 28) || ctrls_words > (1u << 28) || size1 > (1u << 20))
+        return fail(ctx, FIU_ERR_INVALID, "invalid combine_and_popcnt arguments");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t n1 = (size_t)size1 * (cases_words + ctrls_words), n2 = 3 * (cases_words + ctrls_words);
+    uint64_t *d1 = nullptr, *d2 = nullptr;
+    uint32_t* dout = nullptr;
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMallocAsync((void**)&d1, n1 * 8, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&d2, n2 * 8, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dout, 2 * (size_t)ct_size * 4, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d1, t1, n1 * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d2, t2, n2 * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = launch_combine_popcnt(d1, (int)size1, d2, (int)cases_words, (int)ctrls_words, dout, dout + ct_size,
+                                  (int)ct_size, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cases_out, dout, (size_t)ct_size * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctrls_out, dout + ct_size, (size_t)ct_size * 4, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d1, s);
+    cudaFreeAsync(d2, s);
+    cudaFreeAsync(dout, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "combine_and_popcnt");
+    return FIU_OK;
+}
+
+int fiu_mi_compute(fiu_ctx* ctx, const uint32_t* cases, const uint32_t* ctrls, size_t cells, size_t count,
+                   unsigned n_cases, unsigned n_ctrls, int mode, float* out, double* out64) {
+    if (!ctx) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    if (!cases || !ctrls || !out || cells == 0 || (mode != 0 && mode != 1) || n_cases + n_ctrls == 0)
+        return fail(ctx, FIU_ERR_INVALID, "invalid mi_compute arguments");
+    if (count == 0) return FIU_OK;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const long long tmax = (long long)n_cases + n_ctrls;
+    std::vector<long long> ftab(tmax + 1);
+    for (long long c = 0; c <= tmax; ++c)
+        ftab[c] = c < 2 ? 0 : (long long)llround((double)c * std::log((double)c) * 4294967296.0);
+    uint32_t *da = nullptr, *db = nullptr;
+    long long* dt = nullptr;
+    float* dout = nullptr;
+    double* d64 = nullptr;
+    cudaStream_t s = ctx->stream;
+    const size_t n = cells * count;
+    cudaError_t e = cudaMallocAsync((void**)&da, n * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&db, n * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dt, ftab.size() * 8, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dout, count * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&d64, count * 8, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(da, cases, n * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(db, ctrls, n * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dt, ftab.data(), ftab.size() * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = launch_mi(da, db, cells, count, (int)n_cases, (int)n_ctrls, dt, tmax, mode, dout, d64, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, count * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && out64) e = cudaMemcpyAsync(out64, d64, count * 8, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(da, s);
+    cudaFreeAsync(db, s);
+    cudaFreeAsync(dt, s);
+    cudaFreeAsync(dout, s);
+    cudaFreeAsync(d64, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "mi_compute");
+    return FIU_OK;
+}
+
+int fiu_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const int32_t* combos, size_t count,
+               uint32_t* cases_out, uint32_t* ctrls_out) {
+    if (!ctx) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    if (!res || !combos || !cases_out || !ctrls_out || order < 1 || order > FIU_MAX_ORDER)
+        return fail(ctx, FIU_ERR_INVALID, "invalid tables arguments");
+    for (size_t q = 0; q < count * order; ++q)
+        if (combos[q] < 0 || combos[q] >= res->d.snps) return fail(ctx, FIU_ERR_INVALID, "SNP index out of range");
+    if (count == 0) return FIU_OK;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    size_t cells = 1;
+    for (unsigned t = 0; t < order; ++t) cells *= 3;
+    int* dc = nullptr;
+    uint32_t* dout = nullptr;
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMallocAsync((void**)&dc, count * order * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dout, 2 * count * cells * 4, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dc, combos, count * order * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_tables(res->d, (int)order, dc, count, dout, dout + count * cells, nullptr, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cases_out, dout, count * cells * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctrls_out, dout + count * cells, count * cells * 4, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(dc, s);
+    cudaFreeAsync(dout, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "tables");
+    return FIU_OK;
+}
+
+int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* distribution,
+                    int kernel, uint32_t* out, size_t out_words) {
+    if (!ctx) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    ScanWork w;
+    int rc = make_work(ctx, res, order, distribution, 1, w);
+    if (rc) return rc;
+    size_t cells = 1;
+    for (unsigned t = 0; t < order; ++t) cells *= 3;
+    const size_t need = (size_t)w.n_prefixes * res->d.snps * 2 * cells;
+    if (!out || out_words < need) return fail(ctx, FIU_ERR_INVALID, "output buffer too small");
+    if (need == 0) return FIU_OK;
+    if (need > ((size_t)1 << 31)) return fail(ctx, FIU_ERR_UNSUPPORTED, "scan too large to dump");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t s = ctx->stream;
+    uint32_t* d = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d, need * 4, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, out, need * 4, cudaMemcpyHostToDevice, s);
+    CandSink sink{ctx->cand, ctx->ctl, ctx->ctl + 1, 0, (long long)0x7fffffffffffffffll, nullptr};
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ctl, 0, 2 * sizeof(unsigned), s);
+    if (e == cudaSuccess) e = launch_count(kernel, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * 4, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scan tables");
+    return FIU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// Host-side declarations shared by the library's translation units.
+#pragma once
+
+#include "common.cuh"
+
+namespace fiu {
+
+// Where the counting kernels append top-N candidates: every combination whose
+// fixed-point key is >= thr goes to buf[atomicAdd(count, 1)] while below cap;
+// past cap the kernel only raises *overflow.
+struct CandSink {
+    Cand* buf;
+    unsigned* count;
+    unsigned* overflow;
+    unsigned cap;
+    long long thr;
+    unsigned long long* evaluated;  // optional: += combinations evaluated
+};
+
+// Launch-count bookkeeping (kernels of this library only).
+extern thread_local unsigned long long* g_launch_counter;
+inline void count_launch(unsigned n = 1) {
+    if (g_launch_counter) *g_launch_counter += n;
+}
+
+// count.cu -- contingency tables + fused fixed-point MI + candidate filter.
+// kernel 0: generic full 3^k table (any one-hot or not data, orders 2..8).
+cudaError_t launch_count(int kernel, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+                         uint32_t* dump, cudaStream_t s, int sms);
+long long combos_per_prefix_hint(const ScanWork& w);
+
+// layout.cu -- device layouts of a data set.
+cudaError_t launch_transpose(const uint64_t* ref, uint64_t* tr, int snps, int rows, cudaStream_t s);
+cudaError_t launch_onehot_check(const uint64_t* ref, int snps, int cw, int tw, int n_cases, int n_ctrls,
+                                int* bad, cudaStream_t s);
+cudaError_t launch_combine(const uint64_t* t1, int size1, const uint64_t* t2, int cw, int tw, uint64_t* out,
+                           cudaStream_t s);
+// Sustained AND+POPC+ADD word-op rate of this GPU (in-bounds microbenchmark).
+cudaError_t probe_popc_rate(int sms, cudaStream_t s, double* word_ops_per_s);
+cudaError_t launch_combine_popcnt(const uint64_t* t1, int size1, const uint64_t* t2, int cw, int tw,
+                                  uint32_t* cases_out, uint32_t* ctrls_out, int ct_size, cudaStream_t s);
+
+// topn.cu -- top-N selection, FP64 rescoring, tables of given combinations.
+// Keeps the best `keep` of buf[0..M) (key desc, code asc) in buf[0..min(M,keep)),
+// sorted best first.  tmp must hold M + 8192 entries; scratch >= 262 words.
+cudaError_t select_top(Cand* buf, unsigned M, unsigned keep, Cand* tmp, unsigned* scratch, cudaStream_t s);
+// FP64 MI of candidates (recomputing their full tables), then sorts
+// (mi64 desc, code asc) in place; out_mi64[i] matches cands[i] after the sort.
+cudaError_t rescore_sort(const DevData& d, int order, int bits, Cand* cands, unsigned n, double* mi64,
+                         cudaStream_t s);
+cudaError_t launch_tables(const DevData& d, int order, const int* combos, size_t count, uint32_t* cases_out,
+                          uint32_t* ctrls_out, double* mi64, cudaStream_t s);
+cudaError_t launch_mi(const uint32_t* cases, const uint32_t* ctrls, size_t cells, size_t count, int n_cases,
+                      int n_ctrls, const long long* ftab, long long ftab_max, int mode, float* out, double* out64,
+                      cudaStream_t s);
+
+}  // namespace fiu

@@ -50,7 +50,7 @@ def pack_rows(geno: np.ndarray, is_case: np.ndarray, cases_words: int, ctrls_wor
                 # right-align the last, partial word: its last sample lands in bit 0
                 pad = np.zeros((snps, 64 - m), dtype=bool)
                 bits = np.concatenate([bits[:, : nfull * 64], pad, bits[:, nfull * 64:]], axis=1)
-            by = np.packbits(bits, axis=1, bitorder="big")
+            by = np.ascontiguousarray(np.packbits(bits, axis=1, bitorder="big"))
             w = by.reshape(snps, nw, 8).view(">u8").reshape(snps, nw).astype(np.uint64)
             out[:, off + k * words: off + k * words + nw] = w
     return out.reshape(-1)

@@ -1,0 +1,306 @@
+"""The reference-facing search API on the GB300 library.
+
+Mirrors the reference's public surface for the search path:
+
+* ``Distribution`` -- ``Distribution<int>`` (include/fiuncho/Distribution.h:24-203)
+* ``Result``       -- ``Result<int,float>`` (include/fiuncho/utils/Result.h:17-70)
+* ``GpuSearch``    -- a ``Search`` (include/fiuncho/Search.h:19-46) whose
+  ``run(dataset, order, distribution, outputs)`` executes on one GPU
+* ``MPIEngine``    -- ``MPIEngine::run<T>(inputs, order, outputs, args...)``
+  (include/fiuncho/MPIEngine.h:108-182): every rank reads the data set, takes
+  ``Distribution(snps, order-1, size, rank)``, runs the search and rank 0
+  gathers, sorts and truncates.  Ranks come from ``torch.distributed`` when it
+  is initialised, otherwise there is one rank.
+
+Errors are raised as ``FiunchoError`` (the reference throws
+``std::runtime_error``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import functools
+
+import numpy as np
+
+from . import _lib
+from ._lib import FiunchoError
+from .dataset import Dataset
+
+
+@functools.total_ordering
+class Result:
+    """``Result<int, float>``: ordered by ``val`` only (Result.h:22-33)."""
+
+    __slots__ = ("combination", "val")
+
+    def __init__(self, combination=(), val=0.0):
+        self.combination = list(combination)
+        self.val = float(val)
+
+    def __lt__(self, other):
+        return self.val < other.val
+
+    def __eq__(self, other):
+        return self.val == other.val and self.combination == other.combination
+
+    def __hash__(self):
+        return hash((tuple(self.combination), self.val))
+
+    def str(self) -> str:
+        """Text form ``"i j ... val"`` with 6 significant digits (Result.h:37-45)."""
+        return " ".join(str(i) for i in self.combination) + " " + ("%g" % np.float32(self.val))
+
+    __str__ = str
+
+    def __repr__(self):
+        return "Result(%s, %r)" % (self.combination, self.val)
+
+    def serialize(self) -> bytes:
+        """Binary form of Result::serialize (Result.h:47-56): size_t count, int
+        indices, float value, native byte order."""
+        c = np.asarray(self.combination, np.int32)
+        return np.uint64(len(c)).tobytes() + c.tobytes() + np.float32(self.val).tobytes()
+
+    @staticmethod
+    def deserialize(buf: bytes, pos: int = 0):
+        n = int(np.frombuffer(buf, np.uint64, 1, pos)[0])
+        pos += 8
+        comb = np.frombuffer(buf, np.int32, n, pos).tolist()
+        pos += 4 * n
+        val = float(np.frombuffer(buf, np.float32, 1, pos)[0])
+        return Result(comb, val), pos + 4
+
+
+class Distribution:
+    """``Distribution<int>(n, k, step, offset)``; ``layer`` composes splits."""
+
+    def __init__(self, n: int, k: int, step: int = 1, offset: int = 0):
+        if step < 1 or offset < 0 or k < 0 or n < 0:
+            raise ValueError("Distribution requires n, k, offset >= 0 and step >= 1")
+        self.n, self.k, self.step, self.offset = int(n), int(k), int(step), int(offset)
+
+    def layer(self, step: int, offset: int) -> "Distribution":
+        return Distribution(self.n, self.k, self.step * step, self.offset * step + offset)
+
+    def c_struct(self):
+        return _lib.Distribution_t(self.n, self.k, self.step, self.offset)
+
+    def __iter__(self):
+        """Owned k-combinations in the reference's enumeration order."""
+        import itertools
+        for r, c in enumerate(itertools.combinations(range(self.n), self.k)):
+            if r >= self.offset and (r - self.offset) % self.step == 0:
+                yield list(c)
+
+    def __repr__(self):
+        return "Distribution(n=%d, k=%d, step=%d, offset=%d)" % (self.n, self.k, self.step, self.offset)
+
+
+class Context:
+    """One device context of the C library (stream + scratch)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.fiu_create(int(device), C.byref(h))
+        if rc:
+            raise FiunchoError(rc, "cannot create a context on CUDA device %d" % device)
+        self.h = h
+        self.device = device
+
+    def check(self, rc):
+        if rc:
+            raise FiunchoError(rc, self.lib.fiu_last_error(self.h).decode())
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.fiu_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fiu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _c_dataset(ds: Dataset):
+    data = np.ascontiguousarray(ds.data, np.uint64)
+    return _lib.Dataset_t(_lib.ptr(data, C.c_uint64), ds.snps, ds.cases, ds.ctrls, ds.cases_words,
+                          ds.ctrls_words), data
+
+
+class Resident:
+    """A data set held in device memory (uploaded once, searched many times)."""
+
+    def __init__(self, ctx: Context, ds: Dataset):
+        self.ctx = ctx
+        cds, self._keep = _c_dataset(ds)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.fiu_dataset_upload(ctx.h, C.byref(cds), C.byref(h)))
+        self.h = h
+        self.snps, self.cases, self.ctrls = ds.snps, ds.cases, ds.ctrls
+        self._keep = None
+
+    @property
+    def one_hot(self) -> bool:
+        return bool(self.ctx.lib.fiu_dataset_is_one_hot(self.h))
+
+    def free(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.fiu_dataset_free(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _results(order, n, comb, vals):
+    comb = comb[: n * order].reshape(n, order)
+    return [Result(comb[i].tolist(), float(vals[i])) for i in range(n)]
+
+
+class GpuSearch:
+    """``Search`` implementation on one GB300 (the drop-in for ThreadedSearch).
+
+    ``run(dataset, order, distribution, outputs)`` returns at most ``outputs``
+    ``Result``s sorted by MI descending (ties: ascending combination)."""
+
+    def __init__(self, device: int = 0):
+        self.ctx = Context(device)
+
+    def run(self, dataset, order: int, distribution: Distribution, outputs: int, with_fp64: bool = False):
+        lib, ctx = self.ctx.lib, self.ctx
+        outputs = int(outputs)
+        comb = np.zeros(max(outputs, 1) * order, np.int32)
+        vals = np.zeros(max(outputs, 1), np.float32)
+        v64 = np.zeros(max(outputs, 1), np.float64)
+        n = C.c_uint(0)
+        dist = distribution.c_struct()
+        if isinstance(dataset, Resident):
+            ctx.check(lib.fiu_search_resident64(ctx.h, dataset.h, order, C.byref(dist), outputs,
+                                                _lib.ptr(comb, C.c_int32), _lib.ptr(vals, C.c_float),
+                                                _lib.ptr(v64, C.c_double), C.byref(n)))
+        else:
+            if with_fp64:
+                res = Resident(ctx, dataset)
+                try:
+                    return self.run(res, order, distribution, outputs, with_fp64=True)
+                finally:
+                    res.free()
+            cds, keep = _c_dataset(dataset)
+            ctx.check(lib.fiu_search(ctx.h, C.byref(cds), order, C.byref(dist), outputs, _lib.ptr(comb, C.c_int32),
+                                     _lib.ptr(vals, C.c_float), C.byref(n)))
+        out = _results(order, n.value, comb, vals)
+        if with_fp64:
+            return out, v64[: n.value].copy()
+        return out
+
+    # kernel-level entries ----------------------------------------------------
+    def tables(self, resident: Resident, order: int, combos):
+        combos = np.ascontiguousarray(combos, np.int32).reshape(-1, order)
+        q, cells = combos.shape[0], 3 ** order
+        cc = np.zeros((q, cells), np.uint32)
+        tt = np.zeros((q, cells), np.uint32)
+        self.ctx.check(self.ctx.lib.fiu_tables(self.ctx.h, resident.h, order, _lib.ptr(combos, C.c_int32), q,
+                                               _lib.ptr(cc, C.c_uint32), _lib.ptr(tt, C.c_uint32)))
+        return cc, tt
+
+    def scan_tables(self, resident: Resident, order: int, distribution: Distribution, kernel: int = 0):
+        import math
+        total = math.comb(distribution.n, distribution.k)
+        owned = (total - 1 - distribution.offset) // distribution.step + 1 if distribution.offset < total else 0
+        cells = 3 ** order
+        out = np.full(owned * resident.snps * 2 * cells, 0xFFFFFFFF, np.uint32)
+        dist = distribution.c_struct()
+        self.ctx.check(self.ctx.lib.fiu_scan_tables(self.ctx.h, resident.h, order, C.byref(dist), kernel,
+                                                    _lib.ptr(out, C.c_uint32), out.size))
+        return out.reshape(owned, resident.snps, 2, cells)
+
+    def combine(self, t1, size1, t2, cases_words, ctrls_words):
+        t1 = np.ascontiguousarray(t1, np.uint64)
+        t2 = np.ascontiguousarray(t2, np.uint64)
+        out = np.zeros(3 * size1 * (cases_words + ctrls_words), np.uint64)
+        self.ctx.check(self.ctx.lib.fiu_combine(self.ctx.h, _lib.ptr(t1, C.c_uint64), size1,
+                                                _lib.ptr(t2, C.c_uint64), cases_words, ctrls_words,
+                                                _lib.ptr(out, C.c_uint64)))
+        return out
+
+    def combine_and_popcnt(self, t1, size1, t2, cases_words, ctrls_words, ct_size=None):
+        ct_size = ct_size or 3 * size1
+        t1 = np.ascontiguousarray(t1, np.uint64)
+        t2 = np.ascontiguousarray(t2, np.uint64)
+        cc = np.zeros(ct_size, np.uint32)
+        tt = np.zeros(ct_size, np.uint32)
+        self.ctx.check(self.ctx.lib.fiu_combine_and_popcnt(self.ctx.h, _lib.ptr(t1, C.c_uint64), size1,
+                                                           _lib.ptr(t2, C.c_uint64), cases_words, ctrls_words,
+                                                           _lib.ptr(cc, C.c_uint32), _lib.ptr(tt, C.c_uint32),
+                                                           ct_size))
+        return cc, tt
+
+    def mi(self, cases, ctrls, n_cases, n_ctrls, mode=0):
+        cases = np.ascontiguousarray(cases, np.uint32)
+        ctrls = np.ascontiguousarray(ctrls, np.uint32)
+        if cases.ndim == 1:
+            cases, ctrls = cases[None], ctrls[None]
+        count, cells = cases.shape
+        out = np.zeros(count, np.float32)
+        o64 = np.zeros(count, np.float64)
+        self.ctx.check(self.ctx.lib.fiu_mi_compute(self.ctx.h, _lib.ptr(cases, C.c_uint32),
+                                                   _lib.ptr(ctrls, C.c_uint32), cells, count, n_cases, n_ctrls,
+                                                   mode, _lib.ptr(out, C.c_float), _lib.ptr(o64, C.c_double)))
+        return out, o64
+
+
+class MPIEngine:
+    """``MPIEngine`` (include/fiuncho/MPIEngine.h:27-185) over torch.distributed
+    ranks, or one rank when no process group exists."""
+
+    def __init__(self, group=None):
+        self.group = group
+        try:
+            import torch.distributed as dist
+            if dist.is_available() and dist.is_initialized():
+                self.dist = dist
+                self.size = dist.get_world_size(group)
+                self.rank = dist.get_rank(group)
+                return
+        except ImportError:
+            pass
+        self.dist, self.size, self.rank = None, 1, 0
+
+    def run(self, search_cls, inputs, order: int, outputs: int, *args, dataset=None):
+        ds = dataset if dataset is not None else Dataset.read(inputs)
+        if ds.snps > 2 ** 31 - 1:
+            raise FiunchoError(_lib.FIU_ERR_INVALID, "Input data limit exceeded: more than INT_MAX SNPs")
+        distribution = Distribution(ds.snps, order - 1, self.size, self.rank)
+        search = search_cls(*args)
+        local = search.run(ds, order, distribution, outputs)
+        return self.gather(local, outputs)
+
+    def gather(self, local, outputs):
+        """Serialised gather to rank 0, then sort (value desc, combination asc)
+        and truncate (MPIEngine.h:139-174).  Non-zero ranks return []."""
+        blob = b"".join(r.serialize() for r in local)
+        if self.dist is None:
+            blobs = [blob]
+        else:
+            blobs = [None] * self.size if self.rank == 0 else None
+            self.dist.gather_object(blob, blobs, dst=0, group=self.group)
+            if self.rank != 0:
+                return []
+        res = []
+        for b in blobs:
+            pos = 0
+            while pos < len(b):
+                r, pos = Result.deserialize(b, pos)
+                res.append(r)
+        res.sort(key=lambda r: (-r.val, r.combination))
+        return res[:outputs]

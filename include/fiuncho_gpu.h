@@ -1,0 +1,143 @@
+/*
+ * fiuncho_gpu.h -- C ABI of the GB300 (sm_103a) exhaustive epistasis search.
+ *
+ * Plain pointers and sizes only.  A maintainer binds these from the reference
+ * tree's C++ (include/fiuncho/GpuSearch.h in this repository shows the
+ * Search-derived class), from Python (ctypes) or from any FFI.
+ *
+ * Data layout accepted everywhere (identical to the reference's
+ * GenotypeTable<uint64_t>::make_array, include/fiuncho/GenotypeTable.h:77-103):
+ * SNP-major; per SNP 3 case rows of `cases_words` uint64 followed by 3 control
+ * rows of `ctrls_words` uint64; row g holds bit "minor-allele count == g".
+ *
+ * Results follow Search::run (include/fiuncho/Search.h:40-43): at most
+ * `outputs` combinations of `order` ascending 0-based SNP indices, sorted by
+ * mutual information (natural log) in descending order; equal values are
+ * ordered by ascending combination so that the output is deterministic.
+ *
+ * Every function returns FIU_OK (0) or an FIU_ERR_* code; the message of the
+ * last failure of a context is fiu_last_error(ctx).  A context is used from
+ * one host thread at a time.
+ */
+#ifndef FIUNCHO_GPU_H
+#define FIUNCHO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FIU_OK 0
+#define FIU_ERR_INVALID 1     /* invalid argument (sizes, order, distribution, pointers) */
+#define FIU_ERR_NOMEM 2       /* device or host allocation failed / over the memory budget */
+#define FIU_ERR_CUDA 3        /* CUDA runtime error (message in fiu_last_error) */
+#define FIU_ERR_UNSUPPORTED 4 /* valid request outside this build's limits */
+#define FIU_ERR_TIMEOUT 5     /* a device wait ran past its limit */
+#define FIU_ERR_CANCELLED 6   /* request cancelled */
+
+#define FIU_MAX_ORDER 8       /* highest interaction order supported */
+#define FIU_MAX_OUTPUTS 7000  /* largest top-N supported */
+
+typedef struct fiu_ctx fiu_ctx;           /* one per device per host thread */
+typedef struct fiu_resident fiu_resident; /* a data set held in device memory */
+
+/* Host view of Dataset<uint64_t> (include/fiuncho/Dataset.h:26-152). */
+typedef struct {
+    const uint64_t *data;  /* snps * 3 * (cases_words + ctrls_words) words, reference layout */
+    uint64_t snps;         /* Dataset::snps */
+    uint64_t cases;        /* Dataset::cases */
+    uint64_t ctrls;        /* Dataset::ctrls */
+    uint64_t cases_words;  /* GenotypeTable::cases_words */
+    uint64_t ctrls_words;  /* GenotypeTable::ctrls_words */
+} fiu_dataset;
+
+/* Distribution<int>(n, k, step, offset) (include/fiuncho/Distribution.h:147-152):
+ * the (order-1)-SNP prefixes of lexicographic rank offset, offset+step, ...
+ * For one process that is (snps, order-1, 1, 0) (include/fiuncho/MPIEngine.h:133-134). */
+typedef struct {
+    int32_t n;
+    int32_t k;
+    int32_t step;
+    int32_t offset;
+} fiu_distribution;
+
+/* ---- context -------------------------------------------------------------- */
+/* Creates a context on CUDA device `device` (its own stream and scratch). */
+int fiu_create(int device, fiu_ctx **out);
+void fiu_destroy(fiu_ctx *ctx);
+const char *fiu_last_error(const fiu_ctx *ctx);
+/* Sum of the GPU-side launches made by this context since creation (kernels of
+ * this library only); used to report how many launches a timed region made. */
+uint64_t fiu_launch_count(const fiu_ctx *ctx);
+
+/* The context's CUDA stream (a cudaStream_t), on which every kernel of the
+ * context is launched; callers may record events on it. */
+void *fiu_stream(const fiu_ctx *ctx);
+/* Per-context timing of the search's counting kernels with CUDA events on the
+ * context's stream (off by default).  fiu_kernel_timing returns the summed
+ * duration, the number of counting launches and the number of combinations
+ * they evaluated since timing was (re)enabled. */
+int fiu_set_kernel_timing(fiu_ctx *ctx, int enable);
+int fiu_kernel_timing(const fiu_ctx *ctx, double *count_ms, uint64_t *count_launches, uint64_t *combinations);
+/* Measures this GPU's sustained 32-bit AND+POPC+ADD rate (word-ops per second)
+ * with a short in-bounds kernel; the integer-pipe peak for roofline reports. */
+int fiu_probe_popc_rate(fiu_ctx *ctx, double *word_ops_per_s);
+
+/* ---- data sets -------------------------------------------------------------- */
+/* Copies a host data set to the device (Dataset<uint64_t>::read output ->
+ * device buffers) and derives the device layouts the kernels read. */
+int fiu_dataset_upload(fiu_ctx *ctx, const fiu_dataset *host, fiu_resident **out);
+void fiu_dataset_free(fiu_ctx *ctx, fiu_resident *res);
+/* 1 when every SNP's three rows are disjoint, cover each class exactly and
+ * padding words are zero (the reference's own invariant, tests/dataset.cpp:25-44). */
+int fiu_dataset_is_one_hot(const fiu_resident *res);
+
+/* ---- the search (replaces Search::run, include/fiuncho/Search.h:40-43,
+ *      as implemented by ThreadedSearch::run, include/fiuncho/ThreadedSearch.h:207-246) */
+/* Host data set in, results out: upload + search + release, all inside. */
+int fiu_search(fiu_ctx *ctx, const fiu_dataset *dataset, unsigned order, const fiu_distribution *distribution,
+               unsigned outputs, int32_t *out_combinations /* outputs*order */, float *out_vals /* outputs */,
+               unsigned *out_count);
+/* Same on a resident data set. */
+int fiu_search_resident(fiu_ctx *ctx, const fiu_resident *res, unsigned order,
+                        const fiu_distribution *distribution, unsigned outputs, int32_t *out_combinations,
+                        float *out_vals, unsigned *out_count);
+/* As fiu_search_resident and also returns the FP64 MI of each result. */
+int fiu_search_resident64(fiu_ctx *ctx, const fiu_resident *res, unsigned order,
+                          const fiu_distribution *distribution, unsigned outputs, int32_t *out_combinations,
+                          float *out_vals, double *out_vals64, unsigned *out_count);
+
+/* ---- kernel-level entries ------------------------------------------------------- */
+/* GenotypeTable<uint64_t>::combine (include/fiuncho/GenotypeTable.h:123-124,
+ * src/base/gt_combine.cpp:3-27): t1 has size1 rows per class, t2 3 rows per class,
+ * out receives 3*size1 rows per class; each table is [cases rows][ctrls rows]. */
+int fiu_combine(fiu_ctx *ctx, const uint64_t *t1, unsigned size1, const uint64_t *t2, uint64_t cases_words,
+                uint64_t ctrls_words, uint64_t *out);
+/* GenotypeTable<uint64_t>::combine_and_popcnt<uint32_t> (GenotypeTable.h:137-140,
+ * src/base/gt_popcnt.cpp:4-35): cases_out/ctrls_out receive ct_size cells each;
+ * cells from 3*size1 on are zero. */
+int fiu_combine_and_popcnt(fiu_ctx *ctx, const uint64_t *t1, unsigned size1, const uint64_t *t2,
+                           uint64_t cases_words, uint64_t ctrls_words, uint32_t *cases_out, uint32_t *ctrls_out,
+                           unsigned ct_size);
+/* MutualInformation<float>(n_cases, n_ctrls).compute (include/fiuncho/algorithms/
+ * MutualInformation.h:58-84) over `count` tables of `cells` cells per class.
+ * mode 0: the search's fused fixed-point arithmetic; mode 1: FP64. */
+int fiu_mi_compute(fiu_ctx *ctx, const uint32_t *cases, const uint32_t *ctrls, size_t cells, size_t count,
+                   unsigned n_cases, unsigned n_ctrls, int mode, float *out, double *out64);
+/* Contingency tables (3^order cells per class) of given combinations
+ * (count x order ascending indices), computed on the device. */
+int fiu_tables(fiu_ctx *ctx, const fiu_resident *res, unsigned order, const int32_t *combinations, size_t count,
+               uint32_t *cases_out, uint32_t *ctrls_out);
+/* The hot kernel's own tables for every combination of a (small) search:
+ * out[((m * snps) + l) * 2 * 3^order + class * 3^order + cell] for owned
+ * prefix ordinal m and last SNP l (entries with l <= prefix end stay as given). */
+int fiu_scan_tables(fiu_ctx *ctx, const fiu_resident *res, unsigned order, const fiu_distribution *distribution,
+                    int kernel, uint32_t *out, size_t out_words);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,257 @@
+"""Parity of the CUDA path with the oracle and the reference's golden vectors.
+
+Every call goes through the C ABI (libfiuncho_gpu.so via ctypes).  Tolerances:
+contingency counts bit-exact; MI within 1e-5 relative of the FP64 oracle;
+top-N lists identical except for combinations whose exact MI lies within
+1e-5 (relative to the cutoff) of the cutoff.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import as_set, assert_ascending_unique, assert_sorted_desc, assert_topn_equivalent, exact_mi
+
+pytestmark = pytest.mark.gpu
+
+MI_RTOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def gs():
+    from fiuncho_gb300 import GpuSearch
+    return GpuSearch(0)
+
+
+def _ds_from_golden(g):
+    from fiuncho_gb300 import Dataset
+    snps, cases, ctrls, cw, tw = (int(x) for x in g["meta"])
+    return Dataset(cases, ctrls, snps, cw, tw, g["data"])
+
+
+def _check_topn(oracle, ds, order, outputs, res, v64, dist=None, threads=8):
+    c, _, o64, _ = oracle.search(ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words, order,
+                                 outputs, threads=threads, mi_mode=1, dist=dist)
+    got = np.array([r.combination for r in res], np.int32).reshape(-1, order)
+    assert len(res) == len(c)
+    assert_ascending_unique(got)
+    assert_sorted_desc(v64)
+    ex = lambda cs: exact_mi(oracle, ds.data, ds.cases_words, ds.ctrls_words, ds.cases, ds.ctrls, order, cs)
+    if len(c):
+        tol = MI_RTOL * abs(float(o64[-1])) + 1e-12
+        assert_topn_equivalent(got, c, ex, tol)
+        mine = ex(got)
+        assert np.allclose(v64, mine, rtol=MI_RTOL, atol=1e-12)
+        assert np.allclose([r.val for r in res], mine, rtol=MI_RTOL, atol=1e-9)
+    return got
+
+
+# --------------------------------------------------------------- kernel entries
+def test_combine_and_popcnt_bit_exact(gs, oracle, golden_testdata):
+    ds = _ds_from_golden(golden_testdata)
+    cw, tw = ds.cases_words, ds.ctrls_words
+    t1 = ds.data[: 3 * (cw + tw)]
+    t2 = ds.data[3 * (cw + tw): 6 * (cw + tw)]
+    out = gs.combine(t1, 3, t2, cw, tw)
+    exp = np.concatenate([oracle.combine(t1[: 3 * cw], 3, t2[: 3 * cw], cw),
+                          oracle.combine(t1[3 * cw:], 3, t2[3 * cw:], tw)])
+    assert np.array_equal(out, exp)
+    cc, tt = gs.combine_and_popcnt(out, 9, ds.data[6 * (cw + tw): 9 * (cw + tw)], cw, tw, ct_size=32)
+    assert np.array_equal(cc, oracle.popcnt(out[: 9 * cw], 9, ds.data[6 * (cw + tw): 6 * (cw + tw) + 3 * cw], cw, 32))
+    assert np.all(cc[27:] == 0) and np.all(tt[27:] == 0)
+
+
+@pytest.mark.parametrize("order", [2, 3, 4])
+def test_hot_kernel_tables_bit_exact_reference(gs, golden_testdata, order):
+    """The search kernel's own contingency tables for EVERY combination of the
+    reference's test data == the reference's combine_and_popcnt tables."""
+    from fiuncho_gb300 import Distribution, Resident
+    ds = _ds_from_golden(golden_testdata)
+    res = Resident(gs.ctx, ds)
+    out = gs.scan_tables(res, order, Distribution(ds.snps, order - 1))
+    prefixes = list(Distribution(ds.snps, order - 1))
+    ref = {tuple(c): i for i, c in enumerate(golden_testdata["o%d_combos" % order])}
+    n = 0
+    for m, p in enumerate(prefixes):
+        for l in range(p[-1] + 1, ds.snps):
+            i = ref[tuple(p) + (l,)]
+            assert np.array_equal(out[m, l, 0], golden_testdata["o%d_cases" % order][i])
+            assert np.array_equal(out[m, l, 1], golden_testdata["o%d_ctrls" % order][i])
+            n += 1
+    assert n == math.comb(ds.snps, order)
+
+
+def test_tables_entry_bit_exact(gs, oracle, golden_synth):
+    from fiuncho_gb300 import Dataset, Resident
+    ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
+    res = Resident(gs.ctx, ds)
+    cc, tt = gs.tables(res, 3, golden_synth["o3_sample_combos"])
+    assert np.array_equal(cc, golden_synth["o3_cases"]) and np.array_equal(tt, golden_synth["o3_ctrls"])
+
+
+def test_mi_known_answers_and_modes(gs, oracle, golden_testdata):
+    """tests/mi.cpp:7-31 through MutualInformation::compute's replacement, both arithmetics."""
+    for mode in (0, 1):
+        v, v64 = gs.mi(np.full(9, 1, np.uint32), np.full(9, 2, np.uint32), 9, 18, mode=mode)
+        assert abs(v[0]) < 1e-5 and abs(v64[0]) < 1e-9
+        c = np.zeros(9, np.uint32)
+        t = np.zeros(9, np.uint32)
+        c[0], t[1] = 9, 18
+        v, v64 = gs.mi(c, t, 9, 18, mode=mode)
+        assert abs(v[0] - 0.6365141682948129) < 1e-5 and abs(v64[0] - 0.6365141682948129) < 1e-9
+    snps, cases, ctrls, cw, tw = (int(x) for x in golden_testdata["meta"])
+    cc, tt = golden_testdata["o3_cases"], golden_testdata["o3_ctrls"]
+    _, o64 = oracle.mi_batch(cc, tt, cases, ctrls)
+    for mode in (0, 1):
+        v, v64 = gs.mi(cc, tt, cases, ctrls, mode=mode)
+        assert np.allclose(v64, o64, rtol=MI_RTOL, atol=0)
+
+
+# --------------------------------------------------------------- search on the reference's data
+@pytest.mark.parametrize("order", [2, 3, 4])
+def test_search_reference_testdata(gs, oracle, golden_testdata, order):
+    from fiuncho_gb300 import Distribution
+    ds = _ds_from_golden(golden_testdata)
+    res, v64 = gs.run(ds, order, Distribution(ds.snps, order - 1), 90, with_fp64=True)
+    got = _check_topn(oracle, ds, order, 90, res, v64)
+    assert len(res) == min(90, math.comb(10, order))
+    # the reference's own top-90 differs only where its FP32 error cannot order values
+    rc = golden_testdata["o%d_top90_combos" % order]
+    rv = golden_testdata["o%d_top90_vals" % order].astype(np.float64)
+    ex = lambda cs: exact_mi(oracle, ds.data, ds.cases_words, ds.ctrls_words, ds.cases, ds.ctrls, order, cs)
+    ref_err = float(np.max(np.abs(rv - ex(rc))))
+    assert_topn_equivalent(got, rc, ex, 2 * ref_err + 1e-12)
+
+
+def test_search_matches_mpi3snp(gs, golden_testdata):
+    """tests/utils.h:49-101 through the GPU search: normalised order-3 top-90 within 5e-4 of MPI3SNP."""
+    from fiuncho_gb300 import Distribution
+    ds = _ds_from_golden(golden_testdata)
+    res = gs.run(ds, 3, Distribution(ds.snps, 2), 90)
+    norm = {tuple(x): v / golden_testdata["mpi3snp_vals"][0]
+            for x, v in zip(golden_testdata["mpi3snp_combos"], golden_testdata["mpi3snp_vals"])}
+    assert len(res) == 90
+    for r in res:
+        assert abs(r.val / res[0].val - norm.get(tuple(r.combination), 0.0)) <= 5e-4
+
+
+def test_engine_single_rank(gs, golden_testdata):
+    """MPIEngine().run(GpuSearch, ...) at one rank == GpuSearch.run (MPIEngine.h:108-182)."""
+    from fiuncho_gb300 import Distribution, GpuSearch, MPIEngine
+    ds = _ds_from_golden(golden_testdata)
+    a = MPIEngine().run(GpuSearch, None, 3, 90, 0, dataset=ds)
+    b = gs.run(ds, 3, Distribution(ds.snps, 2), 90)
+    assert [r.combination for r in a] == [r.combination for r in b]
+
+
+# --------------------------------------------------------------- synthetic data, distributions
+@pytest.mark.parametrize("order", [2, 3, 4])
+def test_search_synth_vs_reference(gs, oracle, golden_synth, order):
+    from fiuncho_gb300 import Dataset, Distribution
+    ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
+    res, v64 = gs.run(ds, order, Distribution(ds.snps, order - 1), 50, with_fp64=True)
+    got = _check_topn(oracle, ds, order, 50, res, v64)
+    rc = golden_synth["o%d_top50_combos" % order]
+    rv = golden_synth["o%d_top50_vals" % order].astype(np.float64)
+    ex = lambda cs: exact_mi(oracle, ds.data, ds.cases_words, ds.ctrls_words, ds.cases, ds.ctrls, order, cs)
+    assert_topn_equivalent(got, rc, ex, 2 * float(np.max(np.abs(rv - ex(rc)))) + 1e-12)
+
+
+@pytest.mark.parametrize("step,offset", [(2, 1), (3, 0), (5, 4), (1000, 7)])
+def test_search_distribution_layers(gs, oracle, golden_synth, step, offset):
+    """A rank's Distribution(n, k, step, offset) share: same as the oracle's, and
+    for (2, 1) the reference's own step-2/offset-1 run."""
+    from fiuncho_gb300 import Dataset, Distribution
+    ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
+    d = Distribution(ds.snps, 2, step, offset)
+    res, v64 = gs.run(ds, 3, d, 50, with_fp64=True)
+    got = _check_topn(oracle, ds, 3, 50, res, v64, dist=(ds.snps, step, offset))
+    if (step, offset) == (2, 1):
+        rc = golden_synth["o3_step2_off1_combos"]
+        ex = lambda cs: exact_mi(oracle, ds.data, ds.cases_words, ds.ctrls_words, ds.cases, ds.ctrls, 3, cs)
+        rv = golden_synth["o3_step2_off1_vals"].astype(np.float64)
+        assert_topn_equivalent(got, rc, ex, 2 * float(np.max(np.abs(rv - ex(rc)))) + 1e-12)
+
+
+def test_rank_split_merges_to_full_run(gs, golden_synth):
+    """Two ranks' results merged as MPIEngine does == one full run (MPIEngine.h:133-174)."""
+    from fiuncho_gb300 import Dataset, Distribution, MPIEngine
+    ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
+    full = gs.run(ds, 3, Distribution(ds.snps, 2), 40)
+    parts = gs.run(ds, 3, Distribution(ds.snps, 2, 2, 0), 40) + gs.run(ds, 3, Distribution(ds.snps, 2, 2, 1), 40)
+    merged = MPIEngine().gather(parts, 40)
+    assert [r.combination for r in merged] == [r.combination for r in full]
+
+
+# --------------------------------------------------------------- edge cases
+def test_edge_cases(gs, oracle):
+    from fiuncho_gb300 import Dataset, Distribution, FiunchoError
+    rng = np.random.default_rng(5)
+    # ragged class sizes straddling word boundaries, including a single case
+    for n_case, n_ctrl, snps, order in ((1, 130, 9, 2), (65, 63, 12, 3), (127, 1, 7, 4), (300, 301, 6, 5)):
+        geno = rng.integers(0, 3, (snps, n_case + n_ctrl), dtype=np.uint8)
+        is_case = np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)]
+        ds = Dataset.from_genotypes(geno, is_case)
+        out = math.comb(snps, order) + 5  # more outputs than combinations
+        res, v64 = gs.run(ds, order, Distribution(snps, order - 1), out, with_fp64=True)
+        assert len(res) == math.comb(snps, order)
+        _check_topn(oracle, ds, order, out, res, v64)
+    # order larger than the SNP count: no combinations
+    ds = Dataset.from_genotypes(rng.integers(0, 3, (3, 50), dtype=np.uint8), np.r_[np.ones(25), np.zeros(25)])
+    assert gs.run(ds, 4, Distribution(3, 3), 10) == []
+    assert gs.run(ds, 2, Distribution(3, 1), 0) == []
+    # invalid requests are rejected with errors, not results
+    with pytest.raises(FiunchoError):
+        gs.run(ds, 1, Distribution(3, 0), 10)
+    with pytest.raises(FiunchoError):
+        gs.run(ds, 2, Distribution(3, 2), 10)  # k must be order-1
+    with pytest.raises(FiunchoError):
+        gs.run(ds, 2, Distribution(4, 1), 10)  # n beyond the data set
+    with pytest.raises(FiunchoError):
+        gs.run(ds, 2, Distribution(3, 1), 10 ** 6)
+
+
+def test_non_one_hot_data_bit_exact(gs, oracle):
+    """Arbitrary bits (rows overlapping, bits in padding words) are still counted
+    exactly as combine_and_popcnt counts them."""
+    from fiuncho_gb300 import Dataset, Distribution, Resident
+    rng = np.random.default_rng(9)
+    snps, cw, tw = 8, 3, 2
+    data = rng.integers(0, 2 ** 63, snps * 3 * (cw + tw), dtype=np.uint64)
+    ds = Dataset(100, 70, snps, cw, tw, data)
+    res = Resident(gs.ctx, ds)
+    assert not res.one_hot
+    out = gs.scan_tables(res, 3, Distribution(snps, 2))
+    for m, p in enumerate(Distribution(snps, 2)):
+        for l in range(p[-1] + 1, snps):
+            cc, tt = oracle.tables(data, cw, tw, 3, np.array([p + [l]], np.int32))
+            assert np.array_equal(out[m, l, 0], cc[0]) and np.array_equal(out[m, l, 1], tt[0])
+    r, v64 = gs.run(ds, 3, Distribution(snps, 2), 20, with_fp64=True)
+    _check_topn(oracle, ds, 3, 20, r, v64)
+
+
+def test_one_hot_flag(gs, golden_testdata):
+    from fiuncho_gb300 import Resident
+    assert Resident(gs.ctx, _ds_from_golden(golden_testdata)).one_hot
+
+
+# --------------------------------------------------------------- workload shapes
+def test_order2_1000x4000_top10(gs, oracle):
+    """Order-2 scan, 1 000 SNPs x 2 000/2 000 samples, top-10 (full oracle comparison)."""
+    from fiuncho_gb300 import Dataset, Distribution, synth
+    spec = synth.WORKLOADS["order2_1000x4000"]
+    geno, is_case, planted = synth.simulate(spec)
+    ds = Dataset.from_genotypes(geno, is_case)
+    res, v64 = gs.run(ds, 2, Distribution(ds.snps, 1), 10, with_fp64=True)
+    _check_topn(oracle, ds, 2, 10, res, v64, threads=16)
+    assert res[0].combination == list(planted[0])
+
+
+def test_order3_300x8000_top100(gs, oracle):
+    """Order 3 at the 4 000/4 000 row shape on 300 SNPs (4.5e6 combinations), full oracle comparison."""
+    from fiuncho_gb300 import Dataset, Distribution, synth
+    spec = synth.ScanSpec(300, 4000, 4000, 3, 100, seed=21, planted=(3,), penetrance=0.65)
+    geno, is_case, planted = synth.simulate(spec)
+    ds = Dataset.from_genotypes(geno, is_case)
+    res, v64 = gs.run(ds, 3, Distribution(ds.snps, 2), 100, with_fp64=True)
+    _check_topn(oracle, ds, 3, 100, res, v64, threads=16)
