@@ -71,6 +71,35 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     return LIB
 
 
+CPP_INCLUDE = os.path.join(HERE, "cpp", "include")
+BIN = os.path.join(HERE, "bin")
+CPP_TARGETS = {
+    "fiuncho_gpu": os.path.join(HERE, "cpp", "fiuncho_gpu_main.cpp"),
+    "test_gpusearch": os.path.join(os.path.dirname(HERE), "tests", "cpp", "test_gpusearch.cpp"),
+    "dump_dataset": os.path.join(os.path.dirname(HERE), "tests", "cpp", "dump_dataset.cpp"),
+}
+
+
+def build_cpp(force: bool = False) -> dict:
+    """The C++ host side: the CLI and the C++ drop-in test, linked against the library."""
+    lib = build()
+    os.makedirs(BIN, exist_ok=True)
+    headers = glob.glob(os.path.join(CPP_INCLUDE, "fiuncho", "**", "*.h*"), recursive=True) + \
+        glob.glob(os.path.join(INCLUDE, "**", "*.h"), recursive=True)
+    out = {}
+    for name, src in CPP_TARGETS.items():
+        exe = os.path.join(BIN, name)
+        deps = [src, lib] + headers
+        if force or not os.path.exists(exe) or any(os.path.getmtime(d) > os.path.getmtime(exe) for d in deps):
+            cmd = [shutil.which("g++") or "g++", "-std=c++17", "-O2", "-I", CPP_INCLUDE, "-I", INCLUDE, src,
+                   "-o", exe, "-L", HERE, "-lfiuncho_gpu", "-Wl,-rpath," + HERE, "-pthread"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("g++ failed on %s:\n%s%s" % (src, r.stdout, r.stderr))
+        out[name] = exe
+    return out
+
+
 if __name__ == "__main__":
     import sys
     print(build(force="--force" in sys.argv, verbose=True))

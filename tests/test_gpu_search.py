@@ -30,6 +30,10 @@ def _ds_from_golden(g):
 
 
 def _check_topn(oracle, ds, order, outputs, res, v64, dist=None, threads=8):
+    # One worker owns the Distribution's own prefixes (ranks offset, offset+step, ...); the
+    # oracle's threads would re-layer a step > 1 distribution (Distribution::layer), so use one.
+    if dist is not None and dist[1] > 1:
+        threads = 1
     c, _, o64, _ = oracle.search(ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words, order,
                                  outputs, threads=threads, mi_mode=1, dist=dist)
     got = np.array([r.combination for r in res], np.int32).reshape(-1, order)
