@@ -18,6 +18,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "fiuncho_gpu.h")
 FIU_OK, FIU_ERR_INVALID, FIU_ERR_NOMEM, FIU_ERR_CUDA, FIU_ERR_UNSUPPORTED, FIU_ERR_TIMEOUT, FIU_ERR_CANCELLED = \
     range(7)
 FIU_MAX_ORDER = 8
+KERNEL_AUTO, KERNEL_FULL, KERNEL_ELIDED_POPC, KERNEL_ELIDED_HS = 0, 1, 2, 3
 FIU_MAX_OUTPUTS = 7000
 
 ERRORS = {FIU_ERR_INVALID: "invalid argument", FIU_ERR_NOMEM: "out of memory", FIU_ERR_CUDA: "CUDA error",
@@ -52,6 +53,7 @@ _SIGS = {
     "fiu_last_error": (C.c_char_p, [_vp]),
     "fiu_launch_count": (C.c_uint64, [_vp]),
     "fiu_stream": (_vp, [_vp]),
+    "fiu_set_kernel": (C.c_int, [_vp, C.c_int]),
     "fiu_set_kernel_timing": (C.c_int, [_vp, C.c_int]),
     "fiu_kernel_timing": (C.c_int, [_vp, _f64p, _u64p, _u64p]),
     "fiu_probe_popc_rate": (C.c_int, [_vp, _f64p]),

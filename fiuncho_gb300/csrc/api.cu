@@ -38,6 +38,7 @@ struct fiu_ctx {
     double count_ms = 0;
     unsigned long long count_launches = 0;
     unsigned long long* evaluated = nullptr;  // device counter of combinations evaluated
+    int kernel = FIU_KERNEL_AUTO;
 };
 
 struct fiu_resident {
@@ -48,6 +49,8 @@ struct fiu_resident {
     long long ftab_max = 0;
     int one_hot = 0;
     int device = 0;
+    uint32_t* single = nullptr;  // single-SNP cores (elided kernels)
+    uint4* pairs = nullptr;      // pair cores (elided order-3 kernel)
 };
 
 namespace {
@@ -125,6 +128,37 @@ int make_work(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_d
     return FIU_OK;
 }
 
+// Chooses the counting kernel of a request and makes sure its tables exist.
+int choose_kernel(fiu_ctx* ctx, const fiu_resident* res_c, unsigned order, int requested, int& kernel) {
+    fiu_resident* res = const_cast<fiu_resident*>(res_c);
+    const bool elided_ok = res->one_hot && (order == 2 || order == 3) && res->d.n_cases <= 65535 &&
+                           res->d.n_ctrls <= 65535 && elided_smem(order, res->d.cw, res->d.tw) <= 160 * 1024;
+    kernel = requested ? requested : (elided_ok ? FIU_KERNEL_ELIDED_HS : FIU_KERNEL_FULL);
+    if (kernel < FIU_KERNEL_FULL || kernel > FIU_KERNEL_ELIDED_HS)
+        return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
+    if (kernel == FIU_KERNEL_FULL) return FIU_OK;
+    if (!elided_ok)
+        return fail(ctx, FIU_ERR_UNSUPPORTED, "elided kernels need one-hot data, order 2 or 3, classes <= 65535");
+    if (!res->single || (order == 3 && !res->pairs)) {
+        const long long np = (long long)res->d.snps * (res->d.snps - 1) / 2;
+        cudaError_t e = cudaSuccess;
+        if (!res->single) e = cudaMalloc((void**)&res->single, (size_t)res->d.snps * 4 * sizeof(uint32_t));
+        if (e == cudaSuccess && order == 3 && !res->pairs && np > 0)
+            e = cudaMalloc((void**)&res->pairs, (size_t)np * sizeof(uint4));
+        if (e == cudaSuccess)
+            e = build_cores(res->d, res->single, order == 3 ? res->pairs : nullptr, ctx->sms, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "core tables");
+    }
+    return FIU_OK;
+}
+
+cudaError_t launch_kernel(int kernel, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
+                          const CandSink& sink, uint32_t* dump, cudaStream_t s, int sms) {
+    if (kernel == FIU_KERNEL_FULL) return launch_count(0, w, m0, m1, sink, dump, s, sms);
+    return launch_elided(kernel == FIU_KERNEL_ELIDED_HS, w, m0, m1, sink, dump, res->single, res->pairs, s, sms);
+}
+
 // The search on a resident data set (ThreadedSearch::run semantics).
 int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
                 unsigned outputs, int32_t* out_comb, float* out_vals, double* out_vals64, unsigned* out_count,
@@ -139,6 +173,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     if (rc) return rc;
     if (outputs == 0 || w.n_prefixes == 0) return FIU_OK;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((rc = choose_kernel(ctx, res, order, kernel ? kernel : ctx->kernel, kernel))) return rc;
     const unsigned keep = outputs + std::max(32u, outputs / 8);
     const size_t cap = std::max<size_t>({65536, (size_t)16 * keep, (size_t)res->d.snps + keep});
     if ((rc = grow(ctx, ctx->cand, ctx->cand_cap, cap)) ||
@@ -161,7 +196,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
         CK(cudaMemcpyAsync(count, ctx->pinned, 2 * sizeof(unsigned), cudaMemcpyHostToDevice, s), "reset counters");
         CandSink sink{ctx->cand, count, overflow, (unsigned)cap, thr, ctx->timing ? ctx->evaluated : nullptr};
         if (ctx->timing) CK(cudaEventRecord(ctx->ev0, s), "event");
-        CK(launch_count(kernel, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
+        CK(launch_kernel(kernel, res, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
         if (ctx->timing) CK(cudaEventRecord(ctx->ev1, s), "event");
         CK(cudaMemcpyAsync(ctx->pinned, count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read counters");
         CK(cudaStreamSynchronize(s), "count kernel");
@@ -260,6 +295,13 @@ void fiu_destroy(fiu_ctx* ctx) {
 const char* fiu_last_error(const fiu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 uint64_t fiu_launch_count(const fiu_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int fiu_set_kernel(fiu_ctx* ctx, int kernel) {
+    if (!ctx) return FIU_ERR_INVALID;
+    if (kernel < FIU_KERNEL_AUTO || kernel > FIU_KERNEL_ELIDED_HS) return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
+    ctx->kernel = kernel;
+    return FIU_OK;
+}
 
 void* fiu_stream(const fiu_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
@@ -360,6 +402,8 @@ void fiu_dataset_free(fiu_ctx* ctx, fiu_resident* r) {
     cudaFree(r->ref);
     cudaFree(r->tr);
     cudaFree(r->ftab);
+    cudaFree(r->single);
+    cudaFree(r->pairs);
     delete r;
 }
 
@@ -532,13 +576,14 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
     if (need == 0) return FIU_OK;
     if (need > ((size_t)1 << 31)) return fail(ctx, FIU_ERR_UNSUPPORTED, "scan too large to dump");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((rc = choose_kernel(ctx, res, order, kernel, kernel))) return rc;
     cudaStream_t s = ctx->stream;
     uint32_t* d = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&d, need * 4, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d, out, need * 4, cudaMemcpyHostToDevice, s);
     CandSink sink{ctx->cand, ctx->ctl, ctx->ctl + 1, 0, (long long)0x7fffffffffffffffll, nullptr};
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ctl, 0, 2 * sizeof(unsigned), s);
-    if (e == cudaSuccess) e = launch_count(kernel, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
+    if (e == cudaSuccess) e = launch_kernel(kernel, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * 4, cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(d, s);
     cudaError_t e2 = cudaStreamSynchronize(s);

@@ -29,6 +29,12 @@ cudaError_t launch_count(int kernel, const ScanWork& w, long long m0, long long 
                          uint32_t* dump, cudaStream_t s, int sms);
 long long combos_per_prefix_hint(const ScanWork& w);
 
+// elided.cu -- reduced-work kernels for one-hot data, orders 2 and 3.
+cudaError_t build_cores(const DevData& d, uint32_t* single, uint4* pairs, int sms, cudaStream_t s);
+size_t elided_smem(int order, int cw, int tw);
+cudaError_t launch_elided(bool hs, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+                          uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms);
+
 // layout.cu -- device layouts of a data set.
 cudaError_t launch_transpose(const uint64_t* ref, uint64_t* tr, int snps, int rows, cudaStream_t s);
 cudaError_t launch_onehot_check(const uint64_t* ref, int snps, int cw, int tw, int n_cases, int n_ctrls,

@@ -173,8 +173,14 @@ class GpuSearch:
     ``run(dataset, order, distribution, outputs)`` returns at most ``outputs``
     ``Result``s sorted by MI descending (ties: ascending combination)."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, kernel: int = 0):
         self.ctx = Context(device)
+        if kernel:
+            self.set_kernel(kernel)
+
+    def set_kernel(self, kernel: int):
+        """Forces a counting kernel (fiuncho_gb300._lib.KERNEL_*); 0 = automatic."""
+        self.ctx.check(self.ctx.lib.fiu_set_kernel(self.ctx.h, int(kernel)))
 
     def run(self, dataset, order: int, distribution: Distribution, outputs: int, with_fp64: bool = False):
         lib, ctx = self.ctx.lib, self.ctx

@@ -38,6 +38,12 @@ extern "C" {
 #define FIU_ERR_CANCELLED 6   /* request cancelled */
 
 #define FIU_MAX_ORDER 8       /* highest interaction order supported */
+
+/* Counting kernels (fiu_set_kernel, fiu_scan_tables). */
+#define FIU_KERNEL_AUTO 0        /* pick per request (default) */
+#define FIU_KERNEL_FULL 1        /* all 3^order cells, any data, orders 2..8 */
+#define FIU_KERNEL_ELIDED_POPC 2 /* one-hot data, orders 2-3: 2^order cells + exact marginals, POPC */
+#define FIU_KERNEL_ELIDED_HS 3   /* as 2, Harley-Seal carry-save counting on the ALU pipe */
 #define FIU_MAX_OUTPUTS 7000  /* largest top-N supported */
 
 typedef struct fiu_ctx fiu_ctx;           /* one per device per host thread */
@@ -84,6 +90,12 @@ int fiu_kernel_timing(const fiu_ctx *ctx, double *count_ms, uint64_t *count_laun
 /* Measures this GPU's sustained 32-bit AND+POPC+ADD rate (word-ops per second)
  * with a short in-bounds kernel; the integer-pipe peak for roofline reports. */
 int fiu_probe_popc_rate(fiu_ctx *ctx, double *word_ops_per_s);
+
+/* Forces a counting kernel for this context's searches (FIU_KERNEL_*);
+ * FIU_KERNEL_AUTO restores the automatic choice.  A kernel that cannot serve a
+ * request (e.g. an elided kernel on data that is not one-hot) makes the search
+ * fail with FIU_ERR_UNSUPPORTED. */
+int fiu_set_kernel(fiu_ctx *ctx, int kernel);
 
 /* ---- data sets -------------------------------------------------------------- */
 /* Copies a host data set to the device (Dataset<uint64_t>::read output ->

@@ -65,14 +65,15 @@ def test_combine_and_popcnt_bit_exact(gs, oracle, golden_testdata):
     assert np.all(cc[27:] == 0) and np.all(tt[27:] == 0)
 
 
-@pytest.mark.parametrize("order", [2, 3, 4])
-def test_hot_kernel_tables_bit_exact_reference(gs, golden_testdata, order):
-    """The search kernel's own contingency tables for EVERY combination of the
-    reference's test data == the reference's combine_and_popcnt tables."""
+@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 2), (3, 2), (2, 3), (3, 3)])
+def test_hot_kernel_tables_bit_exact_reference(gs, golden_testdata, order, kernel):
+    """Each counting kernel's own contingency tables for EVERY combination of the
+    reference's test data == the reference's combine_and_popcnt tables
+    (kernel 1: full table; 2, 3: core cells + exact marginals, POPC / Harley-Seal)."""
     from fiuncho_gb300 import Distribution, Resident
     ds = _ds_from_golden(golden_testdata)
     res = Resident(gs.ctx, ds)
-    out = gs.scan_tables(res, order, Distribution(ds.snps, order - 1))
+    out = gs.scan_tables(res, order, Distribution(ds.snps, order - 1), kernel=kernel)
     prefixes = list(Distribution(ds.snps, order - 1))
     ref = {tuple(c): i for i, c in enumerate(golden_testdata["o%d_combos" % order])}
     n = 0
@@ -232,6 +233,44 @@ def test_non_one_hot_data_bit_exact(gs, oracle):
             assert np.array_equal(out[m, l, 0], cc[0]) and np.array_equal(out[m, l, 1], tt[0])
     r, v64 = gs.run(ds, 3, Distribution(snps, 2), 20, with_fp64=True)
     _check_topn(oracle, ds, 3, 20, r, v64)
+
+
+@pytest.mark.parametrize("n_case,n_ctrl,snps", [(1000, 777, 60), (65, 63, 40), (1, 513, 30), (4000, 4000, 70)])
+def test_kernels_agree(oracle, n_case, n_ctrl, snps):
+    """Full, elided-POPC and elided-Harley-Seal kernels give identical tables and
+    identical top-N lists (word counts straddling the 8-word Harley-Seal blocks)."""
+    from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident
+    rng = np.random.default_rng(n_case + n_ctrl + snps)
+    maf = rng.uniform(0.05, 0.5, snps)[:, None]
+    u = rng.random((snps, n_case + n_ctrl))
+    geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
+    is_case = np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)]
+    ds = Dataset.from_genotypes(geno, is_case)
+    for order in (2, 3):
+        outs, tabs = [], []
+        for kernel in (1, 2, 3):
+            g = GpuSearch(0, kernel=kernel)
+            res = Resident(g.ctx, ds)
+            assert res.one_hot
+            tabs.append(g.scan_tables(res, order, Distribution(snps, order - 1), kernel=kernel))
+            r, v64 = g.run(res, order, Distribution(snps, order - 1), 40, with_fp64=True)
+            outs.append(([x.combination for x in r], v64))
+        for t in tabs[1:]:
+            mask = tabs[0] != 0xFFFFFFFF
+            assert np.array_equal(t[mask], tabs[0][mask])
+        for o in outs[1:]:
+            assert o[0] == outs[0][0] and np.array_equal(o[1], outs[0][1])
+        r = [type("R", (), {"combination": c, "val": v})() for c, v in zip(outs[0][0], outs[0][1])]
+        _check_topn(oracle, ds, order, 40, r, outs[0][1])
+
+
+def test_elided_rejects_non_one_hot(gs):
+    from fiuncho_gb300 import Dataset, Distribution, FiunchoError, GpuSearch, Resident
+    rng = np.random.default_rng(2)
+    ds = Dataset(100, 70, 6, 2, 2, rng.integers(0, 2 ** 63, 6 * 3 * 4, dtype=np.uint64))
+    g = GpuSearch(0, kernel=3)
+    with pytest.raises(FiunchoError):
+        g.run(ds, 2, Distribution(6, 1), 5)
 
 
 def test_one_hot_flag(gs, golden_testdata):
