@@ -199,7 +199,7 @@ def run_gpu(args, spec):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     geno, is_case, planted = synth.simulate(spec)
     ds = Dataset.from_genotypes(geno, is_case)
-    gs = GpuSearch(local)
+    gs = GpuSearch(local, kernel=args.kernel)
     ctx = gs.ctx
     lib = ctx.lib
     res = Resident(ctx, ds)
@@ -324,7 +324,7 @@ def run_gpu(args, spec):
                          "unit": "T word-ops/s", "frac": int_achieved / peak_rate.value if peak_rate.value else None,
                          "work": "3^k*(ceil(cases/32)+ceil(ctrls/32)) 32-bit AND+POPC per combination",
                          "peak_source": "fiu_probe_popc_rate on this GPU (AND+POPC+ADD microbenchmark)"},
-        "kernel": {"count_ms_total": kms.value, "count_launches": klaunch.value, "combinations": kcombos.value},
+        "kernel": {"id": args.kernel or "auto", "one_hot": res.one_hot, "count_ms_total": kms.value, "count_launches": klaunch.value, "combinations": kcombos.value},
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
     }
@@ -340,6 +340,7 @@ def main():
     ap.add_argument("--workload", default="order3_2000x8000")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--snps", type=int, default=0, help="override the SNP count (small profiling cases)")
+    ap.add_argument("--kernel", type=int, default=0, help="force a counting kernel (0 = automatic choice)")
     args = ap.parse_args()
     import dataclasses
 
