@@ -20,6 +20,7 @@ FIU_OK, FIU_ERR_INVALID, FIU_ERR_NOMEM, FIU_ERR_CUDA, FIU_ERR_UNSUPPORTED, FIU_E
 FIU_MAX_ORDER = 8
 KERNEL_AUTO, KERNEL_FULL, KERNEL_ELIDED_POPC, KERNEL_ELIDED_HS = 0, 1, 2, 3
 FIU_MAX_OUTPUTS = 7000
+FIU_NOALLOC_MAX_SAMPLES = 65536
 
 ERRORS = {FIU_ERR_INVALID: "invalid argument", FIU_ERR_NOMEM: "out of memory", FIU_ERR_CUDA: "CUDA error",
           FIU_ERR_UNSUPPORTED: "unsupported", FIU_ERR_TIMEOUT: "timeout", FIU_ERR_CANCELLED: "cancelled"}
@@ -71,6 +72,7 @@ _SIGS = {
                                          C.c_uint]),
     "fiu_mi_compute": (C.c_int, [_vp, _u32p, _u32p, C.c_size_t, C.c_size_t, C.c_uint, C.c_uint, C.c_int, _f32p,
                                  _f64p]),
+    "fiu_mi_compute_noalloc": (C.c_int, [_vp, _vp, C.c_size_t, C.c_size_t, C.c_uint, C.c_uint, _vp, _vp]),
     "fiu_tables": (C.c_int, [_vp, _vp, C.c_uint, _i32p, C.c_size_t, _u32p, _u32p]),
     "fiu_scan_tables": (C.c_int, [_vp, _vp, C.c_uint, C.POINTER(Distribution_t), C.c_int, _u32p, C.c_size_t]),
 }

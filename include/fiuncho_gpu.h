@@ -138,6 +138,24 @@ int fiu_combine_and_popcnt(fiu_ctx *ctx, const uint64_t *t1, unsigned size1, con
  * mode 0: the search's fused fixed-point arithmetic; mode 1: FP64. */
 int fiu_mi_compute(fiu_ctx *ctx, const uint32_t *cases, const uint32_t *ctrls, size_t cells, size_t count,
                    unsigned n_cases, unsigned n_ctrls, int mode, float *out, double *out64);
+/* No counterpart in the reference.  MutualInformation::compute's fixed-point
+ * arithmetic (mode 0 of fiu_mi_compute) for callers that cannot allocate
+ * device memory at run time (a host that has handed all GPU memory to its own
+ * pool, a pipeline that cannot take cudaMalloc's device-wide synchronisation,
+ * a plugin host owning the memory policy).  Allocates nothing: tables and
+ * outputs are the caller's device buffers (d_cases/d_ctrls: count x cells
+ * uint32 each, d_out: count floats), and the only scratch is a library-owned
+ * static device table sized for n_cases + n_ctrls <= FIU_NOALLOC_MAX_SAMPLES
+ * (512 KiB per GPU that loads the library, kept until exit); larger requests
+ * return FIU_ERR_UNSUPPORTED.  Work is enqueued on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) and not waited for.  The first call on a device
+ * looks up the table's device address with that device current; make that
+ * first call before any stream capture.  All calls share the table and it
+ * keeps the last call's contents, so calls that overlap on the GPU (different
+ * streams, different threads) race and must be serialised by the caller. */
+#define FIU_NOALLOC_MAX_SAMPLES 65536
+int fiu_mi_compute_noalloc(const uint32_t *d_cases, const uint32_t *d_ctrls, size_t cells, size_t count,
+                           unsigned n_cases, unsigned n_ctrls, float *d_out, void *stream);
 /* Contingency tables (3^order cells per class) of given combinations
  * (count x order ascending indices), computed on the device. */
 int fiu_tables(fiu_ctx *ctx, const fiu_resident *res, unsigned order, const int32_t *combinations, size_t count,
