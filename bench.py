@@ -303,6 +303,7 @@ def run_gpu(args, spec):
         pass
     top = out[0] if out else None
     cpu = cpu_sample(spec, ds, seconds=args.cpu_seconds) if args.cpu_seconds > 0 and ws == 1 else None
+    batch = None if (args.no_batch or ws > 1) else run_batch_and_serve(args, gs, ctx)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * my_time / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -327,8 +328,88 @@ def run_gpu(args, spec):
         "kernel": {"id": args.kernel or "auto", "one_hot": res.one_hot, "count_ms_total": kms.value, "count_launches": klaunch.value, "combinations": kcombos.value},
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
+        "batched": batch,
     }
     print(json.dumps(line), flush=True)
+
+
+def run_batch_and_serve(args, gs, ctx):
+    """Batched vs plain on the scaled 64-scan batch, then a served Poisson stream."""
+    import random
+
+    import torch
+
+    from fiuncho_gb300 import Dataset, Distribution, Resident, Server, synth
+    specs = synth.batch_specs(**synth.BATCH_BENCH)
+    t0 = time.perf_counter()
+    data = []
+    for sp in specs:
+        g, c, _ = synth.simulate(sp)
+        data.append(Dataset.from_genotypes(g, c))
+    gen_s = time.perf_counter() - t0
+    work = sum(sp.combos() * sp.samples for sp in specs)
+    res = [Resident(ctx, ds) for ds in data]
+    reqs = [(r, sp.order, Distribution(sp.snps, sp.order - 1), sp.outputs) for r, sp in zip(res, specs)]
+    launches0 = ctx.launches
+
+    def plain():
+        return [gs.run(r, o, d, n, with_fp64=True) for r, o, d, n in reqs]
+
+    def batched():
+        return gs.run_batch(reqs, use_graph=True)
+
+    # warm-up (also builds the core tables), then one timed pass of each
+    a, b = plain(), batched()
+    same = all([x.combination for x in p[0]] == [x.combination for x in q[0]] for p, q in zip(a, b))
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    plain()
+    t_plain = time.perf_counter() - t
+    t = time.perf_counter()
+    batched()
+    t_batch = time.perf_counter() - t
+    for r in res:
+        r.free()
+    out = {"workload": "64 uneven scans: SNPs log-uniform [200, 1200], order-4 capped at 150, samples "
+                       "log-uniform [1000, 32000], case fraction U(0.3, 0.7), order U{2,3,4}, top-50 each",
+           "combos_samples": work, "plain_s": t_plain, "batched_s": t_batch,
+           "plain": work / t_plain, "batched": work / t_batch, "speedup": t_plain / t_batch,
+           "identical_results": same, "graph": True, "data_gen_s": gen_s, "unit": UNIT}
+    # ---- served stream: Poisson arrivals drawn from the same 64 scans
+    rng = random.Random(7)
+    rate, duration = args.serve_rate, args.serve_seconds
+    arrivals, tnow = [], 0.0
+    while True:
+        tnow += rng.expovariate(rate)
+        if tnow >= duration:
+            break
+        arrivals.append((tnow, rng.randrange(len(data))))
+    srv = Server(ctx.device)
+    try:
+        t0 = time.perf_counter()
+        tickets = []
+        for at, i in arrivals:
+            delay = t0 + at - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            tickets.append((srv.submit(data[i], specs[i].order, specs[i].outputs), i))
+        lat = []
+        for tk, i in tickets:
+            lat.append(srv.result(tk)[2])
+        makespan = time.perf_counter() - t0
+        st = srv.stats()
+    finally:
+        srv.close()
+    served_work = sum(specs[i].combos() * specs[i].samples for _, i in arrivals)
+    lat.sort()
+    out["served"] = {"offered_scans_per_s": rate, "duration_s": duration, "requests": len(arrivals),
+                     "completed": int(st["completed"]), "scans_per_s": len(arrivals) / makespan,
+                     "makespan_s": makespan, "combos_samples_per_s": served_work / makespan,
+                     "p50_ms": lat[len(lat) // 2] if lat else None,
+                     "p99_ms": lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))] if lat else None,
+                     "rounds": int(st["rounds"]), "unit": UNIT}
+    out["gpu_launches"] = ctx.launches - launches0
+    return out
 
 
 def main():
@@ -341,6 +422,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--snps", type=int, default=0, help="override the SNP count (small profiling cases)")
     ap.add_argument("--kernel", type=int, default=0, help="force a counting kernel (0 = automatic choice)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched / served measurements")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="served stream: Poisson arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="served stream: arrival window")
     args = ap.parse_args()
     import dataclasses
 

@@ -8,5 +8,5 @@ The compute path is ``libfiuncho_gpu.so`` (hand-written CUDA, C ABI in
 ``MPIEngine``.
 """
 from .dataset import Dataset, GenotypeTable, words_for  # noqa: F401
-from .search import Context, Distribution, GpuSearch, MPIEngine, Resident, Result  # noqa: F401
+from .search import Context, Distribution, GpuSearch, MPIEngine, Resident, Result, Server  # noqa: F401
 from ._lib import FiunchoError  # noqa: F401

@@ -41,6 +41,19 @@ class Distribution_t(C.Structure):
     _fields_ = [("n", C.c_int32), ("k", C.c_int32), ("step", C.c_int32), ("offset", C.c_int32)]
 
 
+class Scan_t(C.Structure):
+    _fields_ = [("res", C.c_void_p), ("order", C.c_uint), ("distribution", Distribution_t), ("outputs", C.c_uint),
+                ("out_combinations", C.POINTER(C.c_int32)), ("out_vals", C.POINTER(C.c_float)),
+                ("out_vals64", C.POINTER(C.c_double)), ("out_count", C.c_uint), ("status", C.c_int)]
+
+
+class ServerStats_t(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64), ("queued", C.c_uint64),
+                ("active", C.c_uint64), ("rounds", C.c_uint64), ("bytes_in_use", C.c_uint64), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
+                ("combos_samples", C.c_double)]
+
+
 _u64p = C.POINTER(C.c_uint64)
 _u32p = C.POINTER(C.c_uint32)
 _i32p = C.POINTER(C.c_int32)
@@ -73,6 +86,13 @@ _SIGS = {
     "fiu_mi_compute": (C.c_int, [_vp, _u32p, _u32p, C.c_size_t, C.c_size_t, C.c_uint, C.c_uint, C.c_int, _f32p,
                                  _f64p]),
     "fiu_mi_compute_noalloc": (C.c_int, [_vp, _vp, C.c_size_t, C.c_size_t, C.c_uint, C.c_uint, _vp, _vp]),
+    "fiu_search_batch": (C.c_int, [_vp, C.POINTER(Scan_t), C.c_uint, C.c_int]),
+    "fiu_server_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_vp)]),
+    "fiu_server_submit": (C.c_int, [_vp, C.POINTER(Dataset_t), C.c_uint, C.c_uint, C.POINTER(C.c_uint64)]),
+    "fiu_server_poll": (C.c_int, [_vp, C.c_uint64, C.c_int, _i32p, _f32p, _f64p, C.POINTER(C.c_uint),
+                                  C.POINTER(C.c_double)]),
+    "fiu_server_stats": (C.c_int, [_vp, C.POINTER(ServerStats_t)]),
+    "fiu_server_destroy": (None, [_vp]),
     "fiu_tables": (C.c_int, [_vp, _vp, C.c_uint, _i32p, C.c_size_t, _u32p, _u32p]),
     "fiu_scan_tables": (C.c_int, [_vp, _vp, C.c_uint, C.POINTER(Distribution_t), C.c_int, _u32p, C.c_size_t]),
 }

@@ -9,7 +9,7 @@
 #include <vector>
 
 #include "../../include/fiuncho_gpu.h"
-#include "internal.h"
+#include "ctx.h"
 
 namespace fiu {
 thread_local unsigned long long* g_launch_counter = nullptr;
@@ -17,48 +17,7 @@ thread_local unsigned long long* g_launch_counter = nullptr;
 
 using namespace fiu;
 
-struct fiu_ctx {
-    int device = 0;
-    int sms = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    unsigned long long launches = 0;
-    // growable scratch of the search driver
-    Cand* cand = nullptr;  // candidate buffer
-    size_t cand_cap = 0;
-    Cand* tmp = nullptr;   // select_top working space
-    size_t tmp_cap = 0;
-    unsigned* ctl = nullptr;  // [0] count, [1] overflow, [2..] select scratch (262)
-    double* mi64 = nullptr;
-    size_t mi64_cap = 0;
-    unsigned* pinned = nullptr;  // host mirror of ctl[0..1]
-    // optional timing of the counting kernels (CUDA events on `stream`)
-    bool timing = false;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    double count_ms = 0;
-    unsigned long long count_launches = 0;
-    unsigned long long* evaluated = nullptr;  // device counter of combinations evaluated
-    int kernel = FIU_KERNEL_AUTO;
-};
-
-struct fiu_resident {
-    DevData d{};
-    uint64_t* ref = nullptr;
-    uint64_t* tr = nullptr;
-    long long* ftab = nullptr;
-    long long ftab_max = 0;
-    int one_hot = 0;
-    int device = 0;
-    uint32_t* single = nullptr;  // single-SNP cores (elided kernels)
-    uint4* pairs = nullptr;      // pair cores (elided order-3 kernel)
-};
-
-namespace {
-
-struct Scope {  // routes launch counting of this thread to the context
-    explicit Scope(fiu_ctx* c) { g_launch_counter = &c->launches; }
-    ~Scope() { g_launch_counter = nullptr; }
-};
+namespace fiu {
 
 int fail(fiu_ctx* ctx, int code, const std::string& msg) {
     if (ctx) ctx->err = msg;
@@ -70,14 +29,8 @@ int cuda_fail(fiu_ctx* ctx, cudaError_t e, const char* what) {
     return fail(ctx, code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CK(expr, what)                                   \
-    do {                                                 \
-        cudaError_t e_ = (expr);                         \
-        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
-    } while (0)
-
 template <typename T>
-int grow(fiu_ctx* ctx, T*& p, size_t& cap, size_t need) {
+static int grow(fiu_ctx* ctx, T*& p, size_t& cap, size_t need) {
     if (need <= cap) return FIU_OK;
     const size_t n = std::max(need, cap * 2);
     if (p) cudaFree(p);
@@ -89,7 +42,21 @@ int grow(fiu_ctx* ctx, T*& p, size_t& cap, size_t need) {
     return FIU_OK;
 }
 
-int bits_for(long long n) {
+int grow_bytes(fiu_ctx* ctx, char*& p, size_t& cap, size_t need) { return grow(ctx, p, cap, need); }
+
+int grow_host(fiu_ctx* ctx, size_t need) {
+    if (need <= ctx->host_arena_cap) return FIU_OK;
+    if (ctx->host_arena) cudaFreeHost(ctx->host_arena);
+    ctx->host_arena = nullptr;
+    ctx->host_arena_cap = 0;
+    const size_t n = std::max(need, (size_t)1 << 20);
+    cudaError_t e = cudaMallocHost((void**)&ctx->host_arena, n);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pinned host allocation");
+    ctx->host_arena_cap = n;
+    return FIU_OK;
+}
+
+static int bits_for(long long n) {
     int b = 1;
     while ((1ll << b) < n) ++b;
     return b;
@@ -248,7 +215,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     return FIU_OK;
 }
 
-}  // namespace
+}  // namespace fiu
 
 extern "C" {
 
@@ -285,6 +252,8 @@ void fiu_destroy(fiu_ctx* ctx) {
     cudaFree(ctx->ctl);
     cudaFree(ctx->mi64);
     cudaFree(ctx->evaluated);
+    cudaFree(ctx->arena);
+    if (ctx->host_arena) cudaFreeHost(ctx->host_arena);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);

@@ -7,6 +7,10 @@
 namespace fiu {
 
 constexpr int kMaxOrder = 8;
+// counting-kernel ids (same values as FIU_KERNEL_* in fiuncho_gpu.h)
+constexpr int FIU_KERNEL_FULL_ID = 1;
+constexpr int FIU_KERNEL_ELIDED_POPC_ID = 2;
+constexpr int FIU_KERNEL_ELIDED_HS_ID = 3;
 constexpr int kFixShift = 32;  // fixed-point scale of the c*ln(c) table: 2^32
 
 // Candidate of the running top-N: `key` is the fixed-point N*MI*2^32 (larger

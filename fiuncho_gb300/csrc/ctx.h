@@ -1,0 +1,76 @@
+// Host-side internals shared by the C ABI translation units: the context and
+// resident data set objects, error helpers and the single-scan driver.
+#pragma once
+
+#include <string>
+
+#include "../../include/fiuncho_gpu.h"
+#include "internal.h"
+
+struct fiu_ctx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    unsigned long long launches = 0;
+    // growable scratch of the search driver
+    fiu::Cand* cand = nullptr;  // candidate buffer
+    size_t cand_cap = 0;
+    fiu::Cand* tmp = nullptr;   // select_top working space
+    size_t tmp_cap = 0;
+    unsigned* ctl = nullptr;  // [0] count, [1] overflow, [2..] select scratch (262)
+    double* mi64 = nullptr;
+    size_t mi64_cap = 0;
+    unsigned* pinned = nullptr;  // host mirror of ctl[0..1]
+    // optional timing of the counting kernels (CUDA events on `stream`)
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double count_ms = 0;
+    unsigned long long count_launches = 0;
+    unsigned long long* evaluated = nullptr;  // device counter of combinations evaluated
+    int kernel = FIU_KERNEL_AUTO;
+    // batched-search arena (device) and its pinned host mirror
+    char* arena = nullptr;
+    size_t arena_cap = 0;
+    char* host_arena = nullptr;
+    size_t host_arena_cap = 0;
+};
+
+struct fiu_resident {
+    fiu::DevData d{};
+    uint64_t* ref = nullptr;
+    uint64_t* tr = nullptr;
+    long long* ftab = nullptr;
+    long long ftab_max = 0;
+    int one_hot = 0;
+    int device = 0;
+    uint32_t* single = nullptr;  // single-SNP cores (elided kernels)
+    uint4* pairs = nullptr;      // pair cores (elided order-3 kernel)
+};
+
+namespace fiu {
+
+struct Scope {  // routes launch counting of this thread to the context
+    explicit Scope(fiu_ctx* c) { g_launch_counter = &c->launches; }
+    ~Scope() { g_launch_counter = nullptr; }
+};
+
+#define CK(expr, what)                                          \
+    do {                                                        \
+        cudaError_t e_ = (expr);                                \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+int fail(fiu_ctx* ctx, int code, const std::string& msg);
+int cuda_fail(fiu_ctx* ctx, cudaError_t e, const char* what);
+int grow_bytes(fiu_ctx* ctx, char*& p, size_t& cap, size_t need);
+int grow_host(fiu_ctx* ctx, size_t need);
+int make_work(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
+              unsigned outputs, ScanWork& w);
+int choose_kernel(fiu_ctx* ctx, const fiu_resident* res, unsigned order, int requested, int& kernel);
+int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
+                unsigned outputs, int32_t* out_comb, float* out_vals, double* out_vals64, unsigned* out_count,
+                int kernel);
+cudaError_t prepare_round_kernels(size_t smem);
+
+}  // namespace fiu

@@ -17,6 +17,53 @@ struct CandSink {
     unsigned long long* evaluated;  // optional: += combinations evaluated
 };
 
+// ---- multi-scan engine (batch.cu, engine.cu) ----------------------------------
+struct ScoredRec {  // a re-scored candidate (FP64 MI, combination code, fixed-point key)
+    double v;
+    unsigned long long code;
+    long long key;
+};
+
+struct ScanDesc {  // per scan, read-only on the device
+    ScanWork w;
+    int kind;          // FIU_KERNEL_FULL / _ELIDED_POPC / _ELIDED_HS
+    unsigned keep;     // candidates kept between rounds (outputs + margin)
+    unsigned cap;      // candidate buffer capacity
+    unsigned outputs;
+    const uint32_t* single;
+    const uint4* pairs;
+    Cand* cand;        // [cap]
+    ScoredRec* scored; // [keep]
+    int* out_comb;     // [outputs * order]
+    float* out_val;    // [outputs]
+    double* out_val64; // [outputs]
+};
+
+struct ScanState {  // per scan, updated on the device between rounds
+    unsigned count;     // candidates held in cand
+    unsigned overflow;  // a round dropped candidates (cap exceeded)
+    unsigned have;      // kept candidates after the last selection
+    unsigned n_out;     // results written by the final pass
+    long long thr;      // current admission threshold (fixed-point key)
+    unsigned long long evaluated;  // combinations evaluated
+};
+
+struct RoundEntry {  // owned prefix ordinals [m0, m0 + n) of scan `scan`, items [begin, begin + n)
+    int scan;
+    int pad;
+    long long m0;
+    long long begin;
+};
+
+// batch.cu
+size_t round_smem(const ScanDesc& sd);
+cudaError_t launch_round(int family, const ScanDesc* scans, ScanState* states, const RoundEntry* ents, int n_ents,
+                         long long total, size_t smem, int sms, cudaStream_t s);
+cudaError_t launch_select_scans(const ScanDesc* scans, ScanState* states, int n_scans, int final_pass,
+                                cudaStream_t s);
+cudaError_t launch_finish_scans(const ScanDesc* scans, ScanState* states, const unsigned* slot_begin, int n_scans,
+                                unsigned total_slots, cudaStream_t s);
+
 // Launch-count bookkeeping (kernels of this library only).
 extern thread_local unsigned long long* g_launch_counter;
 inline void count_launch(unsigned n = 1) {

@@ -1,0 +1,459 @@
+// Served request stream with continuous batching (fiu_server_*).
+//
+// One worker thread owns a device context.  Scans are admitted from a FIFO
+// queue while their device footprint fits the budget; every admitted scan
+// occupies a slot of device-resident descriptors/state (ScanDesc/ScanState
+// of batch.cu) and keeps its data set, candidate buffer and running top-N on
+// the device until it completes.  Each loop iteration is one round over all
+// admitted scans: the round kernels process every scan's next chunk of
+// prefixes (chunks grow x4 per round, capped by a per-round work budget so a
+// large scan does not hold small ones back), then one selection CTA per slot
+// raises thresholds on the device.  Scans whose last chunk ran are finalised
+// (FP64 re-score + top-N), copied out, and release their memory and slot;
+// scans that arrived meanwhile are admitted before the next round.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "ctx.h"
+
+using namespace fiu;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+constexpr int kSlots = 256;                // concurrently admitted scans
+constexpr double kRoundBudget = 1.5e11;    // combinations x samples per scan per round
+
+struct ServeScan {
+    uint64_t ticket = 0;
+    std::vector<uint64_t> data;
+    fiu_dataset host{};
+    unsigned order = 0, outputs = 0;
+    Clock::time_point submitted, done;
+    fiu_resident* res = nullptr;
+    int slot = -1;
+    ScanWork w{};
+    int kind = 0;
+    unsigned keep = 0, cap = 0;
+    long long cursor = 0, chunk = 1, max_chunk = 1;
+    size_t bytes = 0;
+    char* buf = nullptr;
+    size_t off_scored = 0, off_comb = 0, off_val = 0, off_val64 = 0;
+    int status = FIU_OK;
+    bool finished = false;
+    std::vector<int32_t> comb;
+    std::vector<float> vals;
+    std::vector<double> vals64;
+    unsigned count = 0;
+};
+
+size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t footprint(const ServeScan& s) {
+    const size_t snps = s.host.snps, W = s.host.cases_words + s.host.ctrls_words;
+    size_t b = 2 * snps * 3 * W * 8 + (64 * W + 1) * 8 + snps * 16;
+    if (s.order == 3) b += snps * (snps - 1) / 2 * 16;
+    const size_t keep = s.outputs + std::max(32u, s.outputs / 8);
+    b += std::max<size_t>({32768, 16 * keep, snps + keep}) * sizeof(Cand) + keep * sizeof(ScoredRec) +
+         (size_t)s.outputs * (4 * s.order + 12) + 4096;
+    return b;
+}
+
+}  // namespace
+
+struct fiu_server {
+    fiu_ctx* ctx = nullptr;
+    uint64_t budget = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<ServeScan*> queue;
+    std::vector<ServeScan*> active;
+    std::map<uint64_t, ServeScan*> tickets;
+    uint64_t next_ticket = 1;
+    bool stop = false;
+    std::thread worker;
+    ScanDesc* d_desc = nullptr;
+    ScanState* d_state = nullptr;
+    unsigned* d_zero = nullptr;
+    RoundEntry* d_ents = nullptr;
+    size_t ents_cap = 0;
+    std::vector<int> free_slots;
+    // statistics (under mu)
+    uint64_t submitted = 0, completed = 0, failed = 0, rounds = 0, bytes_in_use = 0;
+    std::vector<double> lat_ms;
+    double combos_samples = 0;
+    int init_status = FIU_OK;
+};
+
+namespace {
+
+void release(fiu_server* sv, ServeScan* s) {
+    if (s->slot >= 0) {
+        ScanDesc zero{};
+        cudaMemcpyAsync(sv->d_desc + s->slot, &zero, sizeof(zero), cudaMemcpyHostToDevice, sv->ctx->stream);
+        cudaStreamSynchronize(sv->ctx->stream);
+        sv->free_slots.push_back(s->slot);
+        s->slot = -1;
+    }
+    if (s->buf) cudaFree(s->buf);
+    s->buf = nullptr;
+    if (s->res) fiu_dataset_free(sv->ctx, s->res);
+    s->res = nullptr;
+    std::vector<uint64_t>().swap(s->data);
+}
+
+void finish(fiu_server* sv, ServeScan* s, int status) {
+    fiu_ctx* ctx = sv->ctx;
+    s->status = status;
+    release(sv, s);
+    std::lock_guard<std::mutex> g(sv->mu);
+    s->done = Clock::now();
+    s->finished = true;
+    sv->bytes_in_use -= s->bytes;
+    if (status == FIU_OK) {
+        sv->completed++;
+        sv->lat_ms.push_back(std::chrono::duration<double, std::milli>(s->done - s->submitted).count());
+        sv->combos_samples += (double)binom(s->host.snps, s->order) * (double)(s->host.cases + s->host.ctrls);
+    } else {
+        sv->failed++;
+    }
+    (void)ctx;
+    sv->cv_done.notify_all();
+}
+
+// Uploads and plans an admitted scan; returns false when it finished right away.
+bool admit(fiu_server* sv, ServeScan* s) {
+    fiu_ctx* ctx = sv->ctx;
+    int rc = fiu_dataset_upload(ctx, &s->host, &s->res);
+    if (rc) {
+        finish(sv, s, rc);
+        return false;
+    }
+    fiu_distribution dist{(int)s->host.snps, (int)s->order - 1, 1, 0};
+    s->comb.assign((size_t)std::max(1u, s->outputs) * s->order, 0);
+    s->vals.assign(std::max(1u, s->outputs), 0.f);
+    s->vals64.assign(std::max(1u, s->outputs), 0.0);
+    if ((rc = make_work(ctx, s->res, s->order, &dist, s->outputs, s->w))) {
+        finish(sv, s, rc);
+        return false;
+    }
+    if (s->outputs == 0 || s->w.n_prefixes == 0) {
+        finish(sv, s, FIU_OK);
+        return false;
+    }
+    if ((rc = choose_kernel(ctx, s->res, s->order, ctx->kernel, s->kind))) {
+        finish(sv, s, rc);
+        return false;
+    }
+    if ((s->kind == FIU_KERNEL_FULL && s->order > 4) || sv->free_slots.empty()) {
+        // outside the round kernels: the single-scan path, right now
+        rc = search_impl(ctx, s->res, s->order, &dist, s->outputs, s->comb.data(), s->vals.data(), s->vals64.data(),
+                         &s->count, 0);
+        finish(sv, s, rc);
+        return false;
+    }
+    s->keep = s->outputs + std::max(32u, s->outputs / 8);
+    s->cap = (unsigned)std::max<size_t>({32768, (size_t)16 * s->keep, (size_t)s->host.snps + s->keep});
+    size_t b = a256((size_t)s->cap * sizeof(Cand));
+    s->off_scored = b;
+    b = a256(b + (size_t)s->keep * sizeof(ScoredRec));
+    s->off_comb = b;
+    b = a256(b + (size_t)s->outputs * s->order * sizeof(int));
+    s->off_val = b;
+    b = a256(b + (size_t)s->outputs * sizeof(float));
+    s->off_val64 = b;
+    b = a256(b + (size_t)s->outputs * sizeof(double));
+    if (cudaMalloc((void**)&s->buf, b) != cudaSuccess) {
+        finish(sv, s, FIU_ERR_NOMEM);
+        return false;
+    }
+    s->slot = sv->free_slots.back();
+    sv->free_slots.pop_back();
+    ScanDesc d{};
+    d.w = s->w;
+    d.kind = s->kind;
+    d.keep = s->keep;
+    d.cap = s->cap;
+    d.outputs = s->outputs;
+    d.single = s->res->single;
+    d.pairs = s->res->pairs;
+    d.cand = (Cand*)s->buf;
+    d.scored = (ScoredRec*)(s->buf + s->off_scored);
+    d.out_comb = (int*)(s->buf + s->off_comb);
+    d.out_val = (float*)(s->buf + s->off_val);
+    d.out_val64 = (double*)(s->buf + s->off_val64);
+    const ScanState st0{0, 0, 0, 0, (long long)0x8000000000000000ull, 0};
+    cudaMemcpyAsync(sv->d_desc + s->slot, &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(sv->d_state + s->slot, &st0, sizeof(st0), cudaMemcpyHostToDevice, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        finish(sv, s, FIU_ERR_CUDA);
+        return false;
+    }
+    const double per = (double)binom(s->w.dist_n, s->order) / std::max(1.0, (double)binom(s->w.dist_n, s->order - 1));
+    s->chunk = std::max<long long>(1, (long long)(s->keep / std::max(1.0, per)));
+    s->max_chunk = std::max<long long>(1, (long long)(kRoundBudget / std::max(1.0, per * (double)(s->host.cases + s->host.ctrls))));
+    return true;
+}
+
+// One round over the admitted scans; finalises the ones that completed.
+int run_round(fiu_server* sv) {
+    fiu_ctx* ctx = sv->ctx;
+    cudaStream_t st = ctx->stream;
+    std::vector<RoundEntry> ents;
+    std::vector<std::pair<size_t, long long>> groups;  // (first entry, items) per family
+    size_t smem = 0;
+    for (ServeScan* s : sv->active) {
+        ScanDesc d{};
+        d.w = s->w;
+        d.kind = s->kind;
+        smem = std::max(smem, round_smem(d));
+    }
+    std::vector<long long> take(sv->active.size(), 0);
+    for (size_t i = 0; i < sv->active.size(); ++i) {
+        ServeScan* s = sv->active[i];
+        take[i] = std::min({s->w.n_prefixes - s->cursor, s->chunk, s->max_chunk});
+    }
+    for (int fam = 0; fam < 2; ++fam) {
+        const size_t first = ents.size();
+        long long total = 0;
+        for (size_t i = 0; i < sv->active.size(); ++i) {
+            ServeScan* s = sv->active[i];
+            if (!take[i] || (s->kind == FIU_KERNEL_FULL) != (fam == 1)) continue;
+            ents.push_back(RoundEntry{s->slot, 0, s->cursor, total});
+            total += take[i];
+        }
+        groups.push_back({first, total});
+    }
+    int rc = FIU_OK;
+    if (ents.size() > sv->ents_cap) {
+        cudaFree(sv->d_ents);
+        sv->d_ents = nullptr;
+        sv->ents_cap = 0;
+        if (cudaMalloc((void**)&sv->d_ents, ents.size() * 2 * sizeof(RoundEntry)) != cudaSuccess) return FIU_ERR_NOMEM;
+        sv->ents_cap = ents.size() * 2;
+    }
+    CK(prepare_round_kernels(smem), "kernel attributes");
+    CK(cudaMemcpyAsync(sv->d_ents, ents.data(), ents.size() * sizeof(RoundEntry), cudaMemcpyHostToDevice, st),
+       "round entries");
+    for (int fam = 0; fam < 2; ++fam) {
+        const size_t first = groups[fam].first;
+        const size_t ne = (fam == 0 ? groups[1].first : ents.size()) - first;
+        if (ne) CK(launch_round(fam, sv->d_desc, sv->d_state, sv->d_ents + first, (int)ne, groups[fam].second, smem,
+                                ctx->sms, st), "round");
+    }
+    CK(launch_select_scans(sv->d_desc, sv->d_state, kSlots, 0, st), "selection");
+    std::vector<ServeScan*> done, still;
+    for (size_t i = 0; i < sv->active.size(); ++i) {
+        ServeScan* s = sv->active[i];
+        s->cursor += take[i];
+        s->chunk *= 4;
+        (s->cursor >= s->w.n_prefixes ? done : still).push_back(s);
+    }
+    std::vector<ScanState> hs(done.size());
+    for (size_t i = 0; i < done.size(); ++i) {
+        ServeScan* s = done[i];
+        CK(launch_select_scans(sv->d_desc + s->slot, sv->d_state + s->slot, 1, 1, st), "final selection");
+        CK(launch_finish_scans(sv->d_desc + s->slot, sv->d_state + s->slot, sv->d_zero, 1, s->keep, st), "finish");
+        CK(cudaMemcpyAsync(&hs[i], sv->d_state + s->slot, sizeof(ScanState), cudaMemcpyDeviceToHost, st), "state");
+    }
+    CK(cudaStreamSynchronize(st), "round");
+    for (size_t i = 0; i < done.size(); ++i) {
+        ServeScan* s = done[i];
+        if (hs[i].overflow) {  // candidate buffer overflowed: redo alone on the adaptive path
+            fiu_distribution dist{(int)s->host.snps, (int)s->order - 1, 1, 0};
+            rc = search_impl(ctx, s->res, s->order, &dist, s->outputs, s->comb.data(), s->vals.data(),
+                             s->vals64.data(), &s->count, 0);
+            finish(sv, s, rc);
+            continue;
+        }
+        s->count = std::min(hs[i].n_out, s->outputs);
+        cudaMemcpy(s->comb.data(), s->buf + s->off_comb, (size_t)s->count * s->order * sizeof(int),
+                   cudaMemcpyDeviceToHost);
+        cudaMemcpy(s->vals.data(), s->buf + s->off_val, (size_t)s->count * sizeof(float), cudaMemcpyDeviceToHost);
+        const cudaError_t e = cudaMemcpy(s->vals64.data(), s->buf + s->off_val64, (size_t)s->count * sizeof(double),
+                                         cudaMemcpyDeviceToHost);
+        finish(sv, s, e == cudaSuccess ? FIU_OK : FIU_ERR_CUDA);
+    }
+    sv->active.swap(still);
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        sv->rounds++;
+    }
+    return FIU_OK;
+}
+
+void worker_main(fiu_server* sv) {
+    Scope scope(sv->ctx);
+    for (;;) {
+        // admit while the head of the queue fits the budget
+        for (;;) {
+            ServeScan* s = nullptr;
+            {
+                std::unique_lock<std::mutex> g(sv->mu);
+                if (sv->stop) return;
+                if (sv->queue.empty() || sv->free_slots.empty()) break;
+                ServeScan* h = sv->queue.front();
+                if (sv->bytes_in_use + h->bytes > sv->budget && !sv->active.empty()) break;
+                sv->queue.pop_front();
+                sv->bytes_in_use += h->bytes;
+                s = h;
+            }
+            if (admit(sv, s)) sv->active.push_back(s);
+        }
+        if (sv->active.empty()) {
+            std::unique_lock<std::mutex> g(sv->mu);
+            sv->cv_work.wait_for(g, std::chrono::milliseconds(50),
+                                 [&] { return sv->stop || !sv->queue.empty(); });
+            if (sv->stop) return;
+            continue;
+        }
+        if (run_round(sv) != FIU_OK) {  // device error: fail every admitted scan
+            for (ServeScan* s : sv->active) finish(sv, s, FIU_ERR_CUDA);
+            sv->active.clear();
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
+    if (!out) return FIU_ERR_INVALID;
+    *out = nullptr;
+    auto* sv = new fiu_server;
+    int rc = fiu_create(device, &sv->ctx);
+    if (rc) {
+        delete sv;
+        return rc;
+    }
+    sv->budget = budget_bytes ? budget_bytes : 120ull * 1000 * 1000 * 1000;
+    cudaSetDevice(device);
+    if (cudaMalloc((void**)&sv->d_desc, kSlots * sizeof(ScanDesc)) != cudaSuccess ||
+        cudaMalloc((void**)&sv->d_state, kSlots * sizeof(ScanState)) != cudaSuccess ||
+        cudaMalloc((void**)&sv->d_zero, sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(sv->d_desc, 0, kSlots * sizeof(ScanDesc)) != cudaSuccess ||
+        cudaMemset(sv->d_state, 0, kSlots * sizeof(ScanState)) != cudaSuccess ||
+        cudaMemset(sv->d_zero, 0, sizeof(unsigned)) != cudaSuccess) {
+        cudaFree(sv->d_desc);
+        cudaFree(sv->d_state);
+        cudaFree(sv->d_zero);
+        fiu_destroy(sv->ctx);
+        delete sv;
+        return FIU_ERR_CUDA;
+    }
+    for (int i = kSlots - 1; i >= 0; --i) sv->free_slots.push_back(i);
+    sv->worker = std::thread([sv] {
+        cudaSetDevice(sv->ctx->device);
+        worker_main(sv);
+    });
+    *out = sv;
+    return FIU_OK;
+}
+
+int fiu_server_submit(fiu_server* sv, const fiu_dataset* d, unsigned order, unsigned outputs, uint64_t* ticket) {
+    if (!sv || !d || !d->data || !ticket) return FIU_ERR_INVALID;
+    if (order < 2 || order > FIU_MAX_ORDER || outputs > FIU_MAX_OUTPUTS) return FIU_ERR_INVALID;
+    auto* s = new ServeScan;
+    const size_t words = (size_t)d->snps * 3 * (d->cases_words + d->ctrls_words);
+    s->data.assign(d->data, d->data + words);
+    s->host = *d;
+    s->host.data = s->data.data();
+    s->order = order;
+    s->outputs = outputs;
+    s->bytes = footprint(*s);
+    s->submitted = Clock::now();
+    std::lock_guard<std::mutex> g(sv->mu);
+    if (s->bytes > sv->budget) {
+        delete s;
+        return FIU_ERR_NOMEM;
+    }
+    s->ticket = sv->next_ticket++;
+    sv->tickets[s->ticket] = s;
+    sv->queue.push_back(s);
+    sv->submitted++;
+    *ticket = s->ticket;
+    sv->cv_work.notify_one();
+    return FIU_OK;
+}
+
+int fiu_server_poll(fiu_server* sv, uint64_t ticket, int wait_ms, int32_t* out_comb, float* out_vals,
+                    double* out_vals64, unsigned* out_count, double* latency_ms) {
+    if (!sv) return FIU_ERR_INVALID;
+    std::unique_lock<std::mutex> g(sv->mu);
+    auto it = sv->tickets.find(ticket);
+    if (it == sv->tickets.end()) return FIU_ERR_INVALID;
+    ServeScan* s = it->second;
+    auto ready = [&] { return s->finished; };
+    if (wait_ms < 0) sv->cv_done.wait(g, ready);
+    else if (wait_ms > 0) sv->cv_done.wait_for(g, std::chrono::milliseconds(wait_ms), ready);
+    if (!s->finished) return FIU_ERR_TIMEOUT;
+    const int status = s->status;
+    if (status == FIU_OK) {
+        if (out_count) *out_count = s->count;
+        if (out_comb) std::memcpy(out_comb, s->comb.data(), (size_t)s->count * s->order * sizeof(int32_t));
+        if (out_vals) std::memcpy(out_vals, s->vals.data(), (size_t)s->count * sizeof(float));
+        if (out_vals64) std::memcpy(out_vals64, s->vals64.data(), (size_t)s->count * sizeof(double));
+    }
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(s->done - s->submitted).count();
+    sv->tickets.erase(it);
+    delete s;
+    return status;
+}
+
+int fiu_server_stats(fiu_server* sv, fiu_serve_stats* out) {
+    if (!sv || !out) return FIU_ERR_INVALID;
+    std::lock_guard<std::mutex> g(sv->mu);
+    *out = fiu_serve_stats{};
+    out->submitted = sv->submitted;
+    out->completed = sv->completed;
+    out->failed = sv->failed;
+    out->queued = sv->queue.size();
+    out->active = sv->submitted - sv->completed - sv->failed - sv->queue.size();
+    out->rounds = sv->rounds;
+    out->bytes_in_use = sv->bytes_in_use;
+    out->combos_samples = sv->combos_samples;
+    if (!sv->lat_ms.empty()) {
+        std::vector<double> v = sv->lat_ms;
+        std::sort(v.begin(), v.end());
+        auto q = [&](double f) { return v[std::min(v.size() - 1, (size_t)(f * (v.size() - 1) + 0.5))]; };
+        out->p50_ms = q(0.50);
+        out->p99_ms = q(0.99);
+        out->max_ms = v.back();
+        double sum = 0;
+        for (double x : v) sum += x;
+        out->mean_ms = sum / v.size();
+    }
+    return FIU_OK;
+}
+
+void fiu_server_destroy(fiu_server* sv) {
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    if (sv->worker.joinable()) sv->worker.join();
+    cudaSetDevice(sv->ctx->device);
+    for (ServeScan* s : sv->active) release(sv, s);
+    for (auto& kv : sv->tickets) {
+        if (kv.second->res || kv.second->buf) release(sv, kv.second);
+        delete kv.second;
+    }
+    cudaFree(sv->d_desc);
+    cudaFree(sv->d_state);
+    cudaFree(sv->d_zero);
+    cudaFree(sv->d_ents);
+    fiu_destroy(sv->ctx);
+    delete sv;
+}
+
+}  // extern "C"

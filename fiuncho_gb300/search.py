@@ -209,6 +209,29 @@ class GpuSearch:
             return out, v64[: n.value].copy()
         return out
 
+    def run_batch(self, requests, use_graph: bool = True):
+        """Many scans at once: requests = [(Resident, order, Distribution, outputs), ...].
+        Returns [(results, fp64 values)] in request order; raises if any scan failed."""
+        lib, ctx = self.ctx.lib, self.ctx
+        arr = (_lib.Scan_t * len(requests))()
+        bufs = []
+        for i, (res, order, dist, outputs) in enumerate(requests):
+            comb = np.zeros(max(outputs, 1) * order, np.int32)
+            vals = np.zeros(max(outputs, 1), np.float32)
+            v64 = np.zeros(max(outputs, 1), np.float64)
+            bufs.append((comb, vals, v64))
+            arr[i] = _lib.Scan_t(res.h, order, dist.c_struct(), outputs, _lib.ptr(comb, C.c_int32),
+                                 _lib.ptr(vals, C.c_float), _lib.ptr(v64, C.c_double), 0, 0)
+        ctx.check(lib.fiu_search_batch(ctx.h, arr, len(requests), 1 if use_graph else 0))
+        out = []
+        for i, (res, order, dist, outputs) in enumerate(requests):
+            if arr[i].status:
+                raise FiunchoError(arr[i].status, "scan %d: %s" % (i, lib.fiu_last_error(ctx.h).decode()))
+            n = arr[i].out_count
+            comb, vals, v64 = bufs[i]
+            out.append((_results(order, n, comb, vals), v64[:n].copy()))
+        return out
+
     # kernel-level entries ----------------------------------------------------
     def tables(self, resident: Resident, order: int, combos):
         combos = np.ascontiguousarray(combos, np.int32).reshape(-1, order)
@@ -263,6 +286,65 @@ class GpuSearch:
                                                    _lib.ptr(ctrls, C.c_uint32), cells, count, n_cases, n_ctrls,
                                                    mode, _lib.ptr(out, C.c_float), _lib.ptr(o64, C.c_double)))
         return out, o64
+
+
+class Server:
+    """Served request stream (fiu_server_*): submit whole-data-set scans at
+    any time; they are admitted against a device-memory budget and run with
+    continuous batching.  ``result`` returns (results, fp64 values, latency ms)."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.fiu_server_create(int(device), int(budget_bytes), C.byref(h))
+        if rc:
+            raise FiunchoError(rc, "cannot create a server on CUDA device %d" % device)
+        self.h = h
+        self._orders = {}
+        self._keep = {}
+
+    def submit(self, ds: Dataset, order: int, outputs: int) -> int:
+        cds, data = _c_dataset(ds)
+        t = C.c_uint64(0)
+        rc = self.lib.fiu_server_submit(self.h, C.byref(cds), int(order), int(outputs), C.byref(t))
+        if rc:
+            raise FiunchoError(rc, "submit rejected")
+        self._orders[t.value] = (order, outputs)
+        return t.value
+
+    def result(self, ticket: int, timeout_ms: int = -1):
+        order, outputs = self._orders[ticket]
+        comb = np.zeros(max(outputs, 1) * order, np.int32)
+        vals = np.zeros(max(outputs, 1), np.float32)
+        v64 = np.zeros(max(outputs, 1), np.float64)
+        n = C.c_uint(0)
+        lat = C.c_double(0)
+        rc = self.lib.fiu_server_poll(self.h, ticket, int(timeout_ms), _lib.ptr(comb, C.c_int32),
+                                      _lib.ptr(vals, C.c_float), _lib.ptr(v64, C.c_double), C.byref(n), C.byref(lat))
+        if rc == _lib.FIU_ERR_TIMEOUT:
+            return None
+        del self._orders[ticket]
+        if rc:
+            raise FiunchoError(rc, "scan %d failed" % ticket)
+        return _results(order, n.value, comb, vals), v64[: n.value].copy(), lat.value
+
+    def stats(self) -> dict:
+        st = _lib.ServerStats_t()
+        rc = self.lib.fiu_server_stats(self.h, C.byref(st))
+        if rc:
+            raise FiunchoError(rc, "stats")
+        return {f: getattr(st, f) for f, _ in _lib.ServerStats_t._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fiu_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class MPIEngine:

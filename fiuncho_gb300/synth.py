@@ -18,10 +18,11 @@ Named workloads (``WORKLOADS``):
 * ``order2_40000x16000`` -- 40 000 SNPs, 8 000 / 8 000, order 2, MAF ~
   Beta(0.5, 0.5) truncated to [0.01, 0.5] by rejection; five planted pairs
   with penetrance 0.6.  Top-1 000.
-* ``batch64``            -- 64 independent scans, seeds 1000+i: SNPs
+* ``batch_specs()``      -- 64 independent scans, seeds 1000+i: SNPs
   log-uniform in [500, 20 000], samples log-uniform in [1 000, 32 000], case
   fraction U(0.3, 0.7), order uniform in {2, 3, 4} (order-4 scans capped at
-  400 SNPs), MAF ~ U(0.05, 0.5).  Top-50 each.
+  400 SNPs), MAF ~ U(0.05, 0.5).  Top-50 each.  ``BATCH_BENCH`` scales the
+  SNP counts down for the benchmark.
 """
 from __future__ import annotations
 
@@ -60,20 +61,33 @@ WORKLOADS = {
 }
 
 
-def batch_specs(n_scans: int = 64, base_seed: int = 1000, outputs: int = 50) -> list:
-    """The uneven batch: one spec per scan, each drawn from its own seed."""
+def batch_specs(n_scans: int = 64, base_seed: int = 1000, outputs: int = 50, snp_range=(500, 20000),
+                order4_cap: int = 400, sample_range=(1000, 32000)) -> list:
+    """The uneven batch: one spec per scan, each drawn from its own seed (base_seed + i).
+
+    Defaults are the full-size batch (SNPs log-uniform in [500, 20 000], order-4
+    scans capped at 400 SNPs, samples log-uniform in [1 000, 32 000], case
+    fraction U(0.3, 0.7), order uniform in {2, 3, 4}); the ranges scale it down."""
     specs = []
     for i in range(n_scans):
         rng = np.random.default_rng(base_seed + i)
         order = int(rng.integers(2, 5))
-        hi = 400 if order == 4 else 20000
-        snps = int(round(math.exp(rng.uniform(math.log(500), math.log(hi))))) if hi > 500 else hi
+        hi = order4_cap if order == 4 else snp_range[1]
+        lo = min(snp_range[0], hi)
+        snps = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))))) if hi > lo else hi
         snps = max(order, min(snps, hi))
-        samples = int(round(math.exp(rng.uniform(math.log(1000), math.log(32000)))))
+        samples = int(round(math.exp(rng.uniform(math.log(sample_range[0]), math.log(sample_range[1])))))
         frac = float(rng.uniform(0.3, 0.7))
         cases = max(1, min(samples - 1, int(round(samples * frac))))
         specs.append(ScanSpec(snps, cases, samples - cases, order, outputs, seed=base_seed + i))
     return specs
+
+
+# The batch used by the benchmark: the same distributions with SNP counts
+# scaled to [200, 1 200] (order-4 scans capped at 150 SNPs) so that one batch
+# is ~1e13 combinations x samples (the full-size batch is ~1.2e16).
+BATCH_BENCH = dict(n_scans=64, base_seed=1000, outputs=50, snp_range=(200, 1200), order4_cap=150,
+                   sample_range=(1000, 32000))
 
 
 def _draw_maf(rng, n, kind):

@@ -121,6 +121,58 @@ int fiu_search_resident64(fiu_ctx *ctx, const fiu_resident *res, unsigned order,
                           const fiu_distribution *distribution, unsigned outputs, int32_t *out_combinations,
                           float *out_vals, double *out_vals64, unsigned *out_count);
 
+/* ---- many scans at once (batched form) ---------------------------------------
+ * Each scan is a search of its own resident data set with its own order,
+ * distribution and top-N; the scans progress together on the device in
+ * rounds (one persistent launch over every scan's next chunk of prefixes, then
+ * an on-device top-N selection per scan), optionally as one CUDA graph.
+ * Results are identical to fiu_search_resident on each scan alone. */
+typedef struct {
+    const fiu_resident *res;         /* in: resident data set */
+    unsigned order;                  /* in: interaction order */
+    fiu_distribution distribution;   /* in: k must be order-1 */
+    unsigned outputs;                /* in: top-N */
+    int32_t *out_combinations;       /* out (host): outputs * order */
+    float *out_vals;                 /* out (host): outputs */
+    double *out_vals64;              /* out (host, optional): outputs */
+    unsigned out_count;              /* out: results written */
+    int status;                      /* out: FIU_OK or FIU_ERR_* of this scan */
+} fiu_scan;
+/* use_graph: 1 = capture the rounds into a CUDA graph and launch it once.
+ * Returns FIU_OK when every scan ran (see each scan's status). */
+int fiu_search_batch(fiu_ctx *ctx, fiu_scan *scans, unsigned n_scans, int use_graph);
+
+/* ---- served request stream (continuous batching) --------------------------------
+ * A server owns one device context and one worker thread.  Submitted scans
+ * (host data copied at submit) wait in a queue until their device footprint
+ * fits the memory budget; admitted scans keep their data set, candidate
+ * buffers and running top-N resident and progress in rounds shared with every
+ * other admitted scan, so a scan that arrives while others run starts in the
+ * next round.  Each scan's result is identical to fiu_search on it alone.
+ * Thread-safe: submit/poll/stats may be called from any thread. */
+typedef struct fiu_server fiu_server;
+typedef struct {
+    uint64_t submitted, completed, failed, queued, active;
+    uint64_t rounds;              /* rounds executed */
+    uint64_t bytes_in_use;        /* device bytes held by admitted scans */
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* submit -> result latency of completed scans */
+    double combos_samples;        /* combinations x samples completed */
+} fiu_serve_stats;
+/* budget_bytes: device memory the admitted scans may hold (0 = 120 GB). */
+int fiu_server_create(int device, uint64_t budget_bytes, fiu_server **out);
+/* Queues a scan of the whole data set (Distribution(snps, order-1, 1, 0)). */
+int fiu_server_submit(fiu_server *srv, const fiu_dataset *dataset, unsigned order, unsigned outputs,
+                      uint64_t *ticket);
+/* Waits up to wait_ms (0 = do not wait, < 0 = forever) for a ticket; FIU_OK and
+ * the results once done (the ticket is then released), FIU_ERR_TIMEOUT if not
+ * yet done, the scan's error code if it failed, FIU_ERR_INVALID for an unknown
+ * ticket.  latency_ms (optional) receives submit-to-result time. */
+int fiu_server_poll(fiu_server *srv, uint64_t ticket, int wait_ms, int32_t *out_combinations, float *out_vals,
+                    double *out_vals64, unsigned *out_count, double *latency_ms);
+int fiu_server_stats(fiu_server *srv, fiu_serve_stats *out);
+/* Stops the worker after the current round; pending scans are dropped. */
+void fiu_server_destroy(fiu_server *srv);
+
 /* ---- kernel-level entries ------------------------------------------------------- */
 /* GenotypeTable<uint64_t>::combine (include/fiuncho/GenotypeTable.h:123-124,
  * src/base/gt_combine.cpp:3-27): t1 has size1 rows per class, t2 3 rows per class,

