@@ -68,6 +68,8 @@ _SIGS = {
     "fiu_launch_count": (C.c_uint64, [_vp]),
     "fiu_stream": (_vp, [_vp]),
     "fiu_set_kernel": (C.c_int, [_vp, C.c_int]),
+    "fiu_set_autotune": (C.c_int, [_vp, C.c_int]),
+    "fiu_last_tile": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fiu_set_kernel_timing": (C.c_int, [_vp, C.c_int]),
     "fiu_kernel_timing": (C.c_int, [_vp, _f64p, _u64p, _u64p]),
     "fiu_probe_popc_rate": (C.c_int, [_vp, _f64p]),

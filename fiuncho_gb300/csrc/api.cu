@@ -1,6 +1,7 @@
 // C ABI of the library (include/fiuncho_gpu.h): contexts, resident data sets,
 // the search driver and the kernel-level entries.
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -120,10 +121,94 @@ int choose_kernel(fiu_ctx* ctx, const fiu_resident* res_c, unsigned order, int r
     return FIU_OK;
 }
 
-cudaError_t launch_kernel(int kernel, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
+cudaError_t launch_kernel(int kernel, int tp, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
                           const CandSink& sink, uint32_t* dump, cudaStream_t s, int sms) {
-    if (kernel == FIU_KERNEL_FULL) return launch_count(0, w, m0, m1, sink, dump, s, sms);
-    return launch_elided(kernel == FIU_KERNEL_ELIDED_HS, w, m0, m1, sink, dump, res->single, res->pairs, s, sms);
+    if (kernel == FIU_KERNEL_FULL) return launch_count(tp, w, m0, m1, sink, dump, s, sms);
+    return launch_elided(kernel == FIU_KERNEL_ELIDED_HS, tp, w, m0, m1, sink, dump, res->single, res->pairs, s, sms);
+}
+
+static size_t group_smem(int kernel, const ScanWork& w) {
+    if (kernel == FIU_KERNEL_FULL) {
+        int rows = 1;
+        for (int t = 0; t < w.order - 1; ++t) rows *= 3;
+        return (size_t)(rows < 9 ? rows : 9) * 64 * sizeof(uint64_t);
+    }
+    return elided_smem(w.order, w.d.cw, w.d.tw);
+}
+
+static bool tile_ok(int kernel, int tp, const ScanWork& w) {
+    if (kernel == FIU_KERNEL_FULL && w.order > 5 && tp != 256) return false;
+    return (size_t)(256 / tp) * group_smem(kernel, w) <= kMaxGroupSmem;
+}
+
+// Heuristic tile: the smallest width that still covers a prefix's typical
+// run of last SNPs, (n - k + 1) / k on average.
+static int heuristic_tp(int kernel, const ScanWork& w) {
+    const double L = (double)(w.d.snps - w.order + 1) / w.order;
+    int tp = L >= 384 ? 256 : L >= 160 ? 128 : L >= 64 ? 64 : 32;
+    while (tp < 256 && !tile_ok(kernel, tp, w)) tp *= 2;
+    return tp;
+}
+
+int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp) {
+    int rc = choose_kernel(ctx, res, (unsigned)w.order, requested_kernel, kernel);
+    if (rc) return rc;
+    tp = heuristic_tp(kernel, w);
+    const double work = (double)binom(w.dist_n, w.order) / std::max(1, w.dist_step) * (w.d.n_cases + w.d.n_ctrls);
+    if (!ctx->autotune || work < 2e11 || w.n_prefixes < 64) return FIU_OK;
+    auto lg = [](double x) { int b = 0; while (x >= 2) { x /= 2; ++b; } return b; };
+    const bool family_elided = kernel != FIU_KERNEL_FULL;
+    const unsigned long long key = ((unsigned long long)w.order << 56) | ((unsigned long long)family_elided << 48) |
+                                   ((unsigned long long)(requested_kernel & 0xff) << 40) |
+                                   ((unsigned long long)lg(w.d.cw + w.d.tw) << 20) | (unsigned long long)lg(w.d.snps);
+    auto it = ctx->tuned.find(key);
+    if (it != ctx->tuned.end()) {
+        kernel = it->second.first;
+        tp = it->second.second;
+        return FIU_OK;
+    }
+    // candidates: l-tile widths x (for one-hot data, unless a kernel was forced) both counting schemes
+    std::vector<std::pair<int, int>> cand;
+    std::vector<int> kernels{kernel};
+    if (family_elided && requested_kernel == FIU_KERNEL_AUTO) kernels = {FIU_KERNEL_ELIDED_HS, FIU_KERNEL_ELIDED_POPC};
+    for (int k : kernels)
+        for (int t : {32, 64, 128, 256})
+            if (tile_ok(k, t, w)) cand.push_back({k, t});
+    // uniform sample of the prefixes: every stride-th owned prefix
+    ScanWork sw = w;
+    const long long want = (long long)ctx->sms * 16;
+    const long long stride = std::max<long long>(1, w.n_prefixes / want);
+    sw.dist_step = w.dist_step * (int)std::min<long long>(stride, 1 << 20);
+    sw.n_prefixes = (w.n_prefixes - 1) / stride + 1;
+    const CandSink none{ctx->cand, ctx->ctl + 8, ctx->ctl + 9, 0, (long long)0x7fffffffffffffffll, nullptr};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0), "tuning events");
+    CK(cudaEventCreate(&e1), "tuning events");
+    float best = 1e30f;
+    for (auto& c : cand) {
+        float ms = 0;
+        cudaError_t e = launch_kernel(c.first, c.second, res, sw, 0, sw.n_prefixes, none, nullptr, ctx->stream, ctx->sms);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_kernel(c.first, c.second, res, sw, 0, sw.n_prefixes, none, nullptr, ctx->stream, ctx->sms);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(ctx, e, "autotuning");
+        }
+        if (ms < best) {
+            best = ms;
+            kernel = c.first;
+            tp = c.second;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tuned[key] = {kernel, tp};
+    return FIU_OK;
 }
 
 // The search on a resident data set (ThreadedSearch::run semantics).
@@ -140,7 +225,10 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     if (rc) return rc;
     if (outputs == 0 || w.n_prefixes == 0) return FIU_OK;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
-    if ((rc = choose_kernel(ctx, res, order, kernel ? kernel : ctx->kernel, kernel))) return rc;
+    int tp = 256;
+    if ((rc = choose_tile(ctx, res, w, kernel ? kernel : ctx->kernel, kernel, tp))) return rc;
+    ctx->last_kernel = kernel;
+    ctx->last_tp = tp;
     const unsigned keep = outputs + std::max(32u, outputs / 8);
     const size_t cap = std::max<size_t>({65536, (size_t)16 * keep, (size_t)res->d.snps + keep});
     if ((rc = grow(ctx, ctx->cand, ctx->cand_cap, cap)) ||
@@ -163,7 +251,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
         CK(cudaMemcpyAsync(count, ctx->pinned, 2 * sizeof(unsigned), cudaMemcpyHostToDevice, s), "reset counters");
         CandSink sink{ctx->cand, count, overflow, (unsigned)cap, thr, ctx->timing ? ctx->evaluated : nullptr};
         if (ctx->timing) CK(cudaEventRecord(ctx->ev0, s), "event");
-        CK(launch_kernel(kernel, res, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
+        CK(launch_kernel(kernel, tp, res, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
         if (ctx->timing) CK(cudaEventRecord(ctx->ev1, s), "event");
         CK(cudaMemcpyAsync(ctx->pinned, count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read counters");
         CK(cudaStreamSynchronize(s), "count kernel");
@@ -264,6 +352,19 @@ void fiu_destroy(fiu_ctx* ctx) {
 const char* fiu_last_error(const fiu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 uint64_t fiu_launch_count(const fiu_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int fiu_set_autotune(fiu_ctx* ctx, int enable) {
+    if (!ctx) return FIU_ERR_INVALID;
+    ctx->autotune = enable != 0;
+    return FIU_OK;
+}
+
+int fiu_last_tile(const fiu_ctx* ctx, int* kernel, int* tp) {
+    if (!ctx) return FIU_ERR_INVALID;
+    if (kernel) *kernel = ctx->last_kernel;
+    if (tp) *tp = ctx->last_tp;
+    return FIU_OK;
+}
 
 int fiu_set_kernel(fiu_ctx* ctx, int kernel) {
     if (!ctx) return FIU_ERR_INVALID;
@@ -545,14 +646,18 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
     if (need == 0) return FIU_OK;
     if (need > ((size_t)1 << 31)) return fail(ctx, FIU_ERR_UNSUPPORTED, "scan too large to dump");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    int tp = (kernel >> 8) & 0x1ff;
+    kernel &= 0xff;
     if ((rc = choose_kernel(ctx, res, order, kernel, kernel))) return rc;
+    if (tp != 32 && tp != 64 && tp != 128 && tp != 256) tp = heuristic_tp(kernel, w);
+    if (!tile_ok(kernel, tp, w)) return fail(ctx, FIU_ERR_UNSUPPORTED, "l-tile width not available for this request");
     cudaStream_t s = ctx->stream;
     uint32_t* d = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&d, need * 4, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d, out, need * 4, cudaMemcpyHostToDevice, s);
     CandSink sink{ctx->cand, ctx->ctl, ctx->ctl + 1, 0, (long long)0x7fffffffffffffffll, nullptr};
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ctl, 0, 2 * sizeof(unsigned), s);
-    if (e == cudaSuccess) e = launch_kernel(kernel, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
+    if (e == cudaSuccess) e = launch_kernel(kernel, tp, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * 4, cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(d, s);
     cudaError_t e2 = cudaStreamSynchronize(s);

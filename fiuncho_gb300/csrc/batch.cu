@@ -20,45 +20,44 @@ namespace fiu {
 constexpr int kRoundThreads = 256;
 static_assert(kRoundThreads == kThreads && kRoundThreads == kEThreads, "one block shape for all prefix bodies");
 
-size_t round_smem(const ScanDesc& sd) {
-    if (sd.kind == FIU_KERNEL_FULL_ID) {
-        int rows = 1;
-        for (int t = 0; t < sd.w.order - 1; ++t) rows *= 3;
-        return (size_t)(rows < 9 ? rows : 9) * kWordChunk * sizeof(uint64_t);
-    }
-    return (size_t)(1 << (sd.w.order - 1)) * (sd.w.d.cw + sd.w.d.tw) * sizeof(uint64_t);
-}
-
-// Round kernels are specialised per family so that each keeps the registers
-// of its own prefix bodies: family 0 = reduced-work kernels (orders 2-3),
-// family 1 = full-table kernel (orders 2-4; higher orders take the single-scan path).
-template <int FAMILY>
-__device__ __forceinline__ void run_prefix(const ScanDesc& sd, long long m, const CandSink& sink, uint64_t* sm) {
+// Round kernels are specialised per family and per l-tile width TP so that
+// each keeps the registers of its own prefix bodies: family 0 = reduced-work
+// kernels (orders 2-3, Harley-Seal counting), family 1 = full-table kernel
+// (orders 2-4; higher orders take the single-scan path).  A CTA holds
+// 256 / TP groups, each working on its own prefix.
+template <int FAMILY, int TP>
+__device__ __forceinline__ void run_prefix(const ScanDesc& sd, long long m, const CandSink& sink, uint64_t* sm,
+                                           int grp) {
     if (FAMILY == 0) {
-        if (sd.kind == FIU_KERNEL_ELIDED_HS_ID) {
-            if (sd.w.order == 2) elided_prefix<2, true>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sm);
-            else elided_prefix<3, true>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sm);
-        } else {
-            if (sd.w.order == 2) elided_prefix<2, false>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sm);
-            else elided_prefix<3, false>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sm);
-        }
+        if (sd.w.order == 2) elided_prefix<2, true, TP>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sm, grp);
+        else elided_prefix<3, true, TP>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sm, grp);
     } else {
         switch (sd.w.order) {
-            case 2: full_prefix<2>(sd.w, m, sink, nullptr, sm); break;
-            case 3: full_prefix<3>(sd.w, m, sink, nullptr, sm); break;
-            case 4: full_prefix<4>(sd.w, m, sink, nullptr, sm); break;
+            case 2: full_prefix<2, TP>(sd.w, m, sink, nullptr, sm, grp); break;
+            case 3: full_prefix<3, TP>(sd.w, m, sink, nullptr, sm, grp); break;
+            case 4: full_prefix<4, TP>(sd.w, m, sink, nullptr, sm, grp); break;
             default: break;
         }
     }
 }
 
-template <int FAMILY>
+// Shared-memory words of one group for a scan.
+__host__ __device__ inline size_t group_words(const ScanDesc& sd) {
+    if (sd.kind == FIU_KERNEL_FULL_ID) return (size_t)full_group_words(sd.w.order);
+    return (size_t)(1 << (sd.w.order - 1)) * (sd.w.d.cw + sd.w.d.tw);
+}
+
+size_t round_smem(const ScanDesc& sd) { return (size_t)(kRoundThreads / sd.tp) * group_words(sd) * sizeof(uint64_t); }
+
+template <int FAMILY, int TP>
 __global__ void __launch_bounds__(kRoundThreads, 2) round_kernel(const ScanDesc* __restrict__ scans,
                                                                  ScanState* states,
                                                                  const RoundEntry* __restrict__ ents, int n_ents,
                                                                  long long total) {
     extern __shared__ uint64_t sm[];
-    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
+    constexpr int G = kRoundThreads / TP;
+    const int grp = threadIdx.x / TP;
+    for (long long g = (long long)blockIdx.x * G + grp; g < total; g += (long long)gridDim.x * G) {
         int lo = 0, hi = n_ents - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -70,34 +69,45 @@ __global__ void __launch_bounds__(kRoundThreads, 2) round_kernel(const ScanDesc*
         ScanState* st = states + e.scan;
         const CandSink sink{sd.cand, &st->count, &st->overflow, sd.cap,
                             *reinterpret_cast<volatile long long*>(&st->thr), &st->evaluated};
-        run_prefix<FAMILY>(sd, e.m0 + (g - e.begin), sink, sm);
+        run_prefix<FAMILY, TP>(sd, e.m0 + (g - e.begin), sink, sm + grp * group_words(sd), grp);
     }
 }
 
-static size_t g_round_attr[2] = {0, 0};
-static int g_round_per_sm[2] = {0, 0};
+static size_t g_round_attr[2][4] = {};
+static int g_round_per_sm[2][4] = {};
 static bool g_select_attr = false, g_finish_attr = false;
 
-struct RecBetter;
 __global__ void select_scans_kernel(const ScanDesc* __restrict__ scans, ScanState* states, int final_pass);
 __global__ void finish_scans_kernel(const ScanDesc* __restrict__ scans, ScanState* states);
 
+static int tp_index(int tp) { return tp == 32 ? 0 : tp == 64 ? 1 : tp == 128 ? 2 : 3; }
+
+static const void* round_fn(int family, int ti) {
+    static const void* fns[2][4] = {
+        {(const void*)round_kernel<0, 32>, (const void*)round_kernel<0, 64>, (const void*)round_kernel<0, 128>,
+         (const void*)round_kernel<0, 256>},
+        {(const void*)round_kernel<1, 32>, (const void*)round_kernel<1, 64>, (const void*)round_kernel<1, 128>,
+         (const void*)round_kernel<1, 256>}};
+    return fns[family][ti];
+}
+
 // Sets the dynamic shared-memory limits of the multi-scan kernels (never
-// inside a stream capture) and caches the round kernel's occupancy.
+// inside a stream capture) and caches the round kernels' occupancy.
 cudaError_t prepare_round_kernels(size_t smem) {
     cudaError_t e = cudaSuccess;
-    for (int f = 0; f < 2; ++f) {
-        if (smem > g_round_attr[f] || !g_round_per_sm[f]) {
-            const size_t want = smem > g_round_attr[f] ? smem : g_round_attr[f];
-            const void* fn = f == 0 ? (const void*)round_kernel<0> : (const void*)round_kernel<1>;
-            e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
-            if (e != cudaSuccess) return e;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_round_per_sm[f], fn, kRoundThreads, want);
-            if (e != cudaSuccess) return e;
-            if (g_round_per_sm[f] < 1) g_round_per_sm[f] = 1;
-            g_round_attr[f] = want;
+    for (int f = 0; f < 2; ++f)
+        for (int t = 0; t < 4; ++t) {
+            if (smem > g_round_attr[f][t] || !g_round_per_sm[f][t]) {
+                const size_t want = smem > g_round_attr[f][t] ? smem : g_round_attr[f][t];
+                const void* fn = round_fn(f, t);
+                e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+                if (e != cudaSuccess) return e;
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_round_per_sm[f][t], fn, kRoundThreads, want);
+                if (e != cudaSuccess) return e;
+                if (g_round_per_sm[f][t] < 1) g_round_per_sm[f][t] = 1;
+                g_round_attr[f][t] = want;
+            }
         }
-    }
     if (!g_select_attr) {
         e = cudaFuncSetAttribute(select_scans_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(kSortCap * sizeof(Cand)));
@@ -113,15 +123,37 @@ cudaError_t prepare_round_kernels(size_t smem) {
     return e;
 }
 
-cudaError_t launch_round(int family, const ScanDesc* scans, ScanState* states, const RoundEntry* ents, int n_ents,
-                         long long total, size_t smem, int sms, cudaStream_t s) {
+template <int FAMILY, int TP>
+static void launch_round_t(unsigned grid, size_t smem, const ScanDesc* scans, ScanState* states,
+                           const RoundEntry* ents, int n_ents, long long total, cudaStream_t s) {
+    round_kernel<FAMILY, TP><<<grid, kRoundThreads, smem, s>>>(scans, states, ents, n_ents, total);
+}
+
+cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* states, const RoundEntry* ents,
+                         int n_ents, long long total, size_t smem, int sms, cudaStream_t s) {
     if (total <= 0 || n_ents <= 0) return cudaSuccess;
-    if (family < 0 || family > 1 || smem > g_round_attr[family] || !g_round_per_sm[family])
+    const int ti = tp_index(tp);
+    if (family < 0 || family > 1 || smem > g_round_attr[family][ti] || !g_round_per_sm[family][ti])
         return cudaErrorInvalidConfiguration;  // prepare_round_kernels first
-    const long long cap = (long long)sms * g_round_per_sm[family];
-    const unsigned grid = (unsigned)(total < cap ? total : cap);
-    if (family == 0) round_kernel<0><<<grid, kRoundThreads, g_round_attr[0], s>>>(scans, states, ents, n_ents, total);
-    else round_kernel<1><<<grid, kRoundThreads, g_round_attr[1], s>>>(scans, states, ents, n_ents, total);
+    const long long G = kRoundThreads / tp;
+    const long long ctas = (total + G - 1) / G, cap = (long long)sms * g_round_per_sm[family][ti];
+    const unsigned grid = (unsigned)(ctas < cap ? ctas : cap);
+    const size_t sm = g_round_attr[family][ti];
+    if (family == 0) {
+        switch (ti) {
+            case 0: launch_round_t<0, 32>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 1: launch_round_t<0, 64>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 2: launch_round_t<0, 128>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            default: launch_round_t<0, 256>(grid, sm, scans, states, ents, n_ents, total, s); break;
+        }
+    } else {
+        switch (ti) {
+            case 0: launch_round_t<1, 32>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 1: launch_round_t<1, 64>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 2: launch_round_t<1, 128>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            default: launch_round_t<1, 256>(grid, sm, scans, states, ents, n_ents, total, s); break;
+        }
+    }
     count_launch();
     return cudaGetLastError();
 }

@@ -18,42 +18,58 @@
 
 namespace fiu {
 
-template <int K>
+template <int K, int TP>
 __global__ void __launch_bounds__(kThreads) count_full(ScanWork w, long long m0, long long m1, CandSink sink,
                                                        uint32_t* dump) {
-    constexpr int ROWS = pow3(K - 1);
-    __shared__ uint64_t sp[(ROWS < 9 ? ROWS : 9) * kWordChunk];
-    for (long long m = m0 + blockIdx.x; m < m1; m += gridDim.x) full_prefix<K>(w, m, sink, dump, sp);
+    extern __shared__ uint64_t sp[];  // (kThreads / TP) groups x full_group_words(K)
+    constexpr int G = kThreads / TP;
+    const int grp = threadIdx.x / TP;
+    for (long long m = m0 + (long long)blockIdx.x * G + grp; m < m1; m += (long long)gridDim.x * G)
+        full_prefix<K, TP>(w, m, sink, dump, sp + grp * full_group_words(K), grp);
 }
 
-template <int K>
+template <int K, int TP>
 static cudaError_t launch_full(const ScanWork& w, long long m0, long long m1, const CandSink& sink, uint32_t* dump,
                                cudaStream_t s, int sms) {
+    constexpr int G = kThreads / TP;
+    const size_t smem = (size_t)G * full_group_words(K) * sizeof(uint64_t);
     static int per_sm = 0;
     if (!per_sm) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, count_full<K>, kThreads, 0);
+        cudaError_t e = cudaFuncSetAttribute(count_full<K, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, count_full<K, TP>, kThreads, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
-    const long long items = m1 - m0;
-    if (items <= 0) return cudaSuccess;
-    const long long grid = items < (long long)sms * per_sm ? items : (long long)sms * per_sm;
-    count_full<K><<<(unsigned)grid, kThreads, 0, s>>>(w, m0, m1, sink, dump);
+    const long long ctas = (m1 - m0 + G - 1) / G;
+    if (ctas <= 0) return cudaSuccess;
+    const long long grid = ctas < (long long)sms * per_sm ? ctas : (long long)sms * per_sm;
+    count_full<K, TP><<<(unsigned)grid, kThreads, smem, s>>>(w, m0, m1, sink, dump);
     count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_count(int kernel, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+template <int K>
+static cudaError_t launch_full_tp(int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+                                  uint32_t* dump, cudaStream_t s, int sms) {
+    switch (tp) {
+        case 32: return launch_full<K, 32>(w, m0, m1, sink, dump, s, sms);
+        case 64: return launch_full<K, 64>(w, m0, m1, sink, dump, s, sms);
+        case 128: return launch_full<K, 128>(w, m0, m1, sink, dump, s, sms);
+        default: return launch_full<K, 256>(w, m0, m1, sink, dump, s, sms);
+    }
+}
+
+cudaError_t launch_count(int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
                          uint32_t* dump, cudaStream_t s, int sms) {
-    if (kernel != 0) return cudaErrorInvalidValue;
     switch (w.order) {
-        case 2: return launch_full<2>(w, m0, m1, sink, dump, s, sms);
-        case 3: return launch_full<3>(w, m0, m1, sink, dump, s, sms);
-        case 4: return launch_full<4>(w, m0, m1, sink, dump, s, sms);
-        case 5: return launch_full<5>(w, m0, m1, sink, dump, s, sms);
-        case 6: return launch_full<6>(w, m0, m1, sink, dump, s, sms);
-        case 7: return launch_full<7>(w, m0, m1, sink, dump, s, sms);
-        case 8: return launch_full<8>(w, m0, m1, sink, dump, s, sms);
+        case 2: return launch_full_tp<2>(tp, w, m0, m1, sink, dump, s, sms);
+        case 3: return launch_full_tp<3>(tp, w, m0, m1, sink, dump, s, sms);
+        case 4: return launch_full_tp<4>(tp, w, m0, m1, sink, dump, s, sms);
+        case 5: return launch_full_tp<5>(tp, w, m0, m1, sink, dump, s, sms);
+        case 6: return launch_full<6, 256>(w, m0, m1, sink, dump, s, sms);
+        case 7: return launch_full<7, 256>(w, m0, m1, sink, dump, s, sms);
+        case 8: return launch_full<8, 256>(w, m0, m1, sink, dump, s, sms);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -2,7 +2,9 @@
 // resident data set objects, error helpers and the single-scan driver.
 #pragma once
 
+#include <map>
 #include <string>
+#include <utility>
 
 #include "../../include/fiuncho_gpu.h"
 #include "internal.h"
@@ -29,6 +31,10 @@ struct fiu_ctx {
     unsigned long long count_launches = 0;
     unsigned long long* evaluated = nullptr;  // device counter of combinations evaluated
     int kernel = FIU_KERNEL_AUTO;
+    // autotuner: (order, family, words bucket, snps bucket) -> (kernel, tp)
+    bool autotune = true;
+    int last_kernel = 0, last_tp = 0;  // tile of the last single-scan search
+    std::map<unsigned long long, std::pair<int, int>> tuned;
     // batched-search arena (device) and its pinned host mirror
     char* arena = nullptr;
     size_t arena_cap = 0;
@@ -68,6 +74,12 @@ int grow_host(fiu_ctx* ctx, size_t need);
 int make_work(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
               unsigned outputs, ScanWork& w);
 int choose_kernel(fiu_ctx* ctx, const fiu_resident* res, unsigned order, int requested, int& kernel);
+// Picks the counting kernel variant and l-tile width (threads per prefix) of a
+// request: measured on a strided sample of its prefixes (cached per shape
+// bucket) when autotuning is on and the request is large, else a heuristic.
+int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp);
+cudaError_t launch_kernel(int kernel, int tp, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
+                          const CandSink& sink, uint32_t* dump, cudaStream_t s, int sms);
 int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
                 unsigned outputs, int32_t* out_comb, float* out_vals, double* out_vals64, unsigned* out_count,
                 int kernel);

@@ -100,46 +100,62 @@ cudaError_t build_cores(const DevData& d, uint32_t* single, uint4* pairs, int sm
     return cudaGetLastError();
 }
 
-template <int K, bool HS>
+template <int K, bool HS, int TP>
 __global__ void __launch_bounds__(kEThreads) count_elided(ScanWork w, long long m0, long long m1, CandSink sink,
                                                          uint32_t* dump, const uint32_t* __restrict__ single,
                                                          const uint4* __restrict__ pairs) {
-    extern __shared__ uint64_t sp[];  // [2^(K-1)][cw + tw]
-    for (long long m = m0 + blockIdx.x; m < m1; m += gridDim.x)
-        elided_prefix<K, HS>(w, m, sink, dump, single, pairs, sp);
+    extern __shared__ uint64_t sp[];  // (kEThreads / TP) groups x 2^(K-1) x (cw + tw)
+    constexpr int G = kEThreads / TP;
+    const int grp = threadIdx.x / TP;
+    const size_t words = (size_t)(1 << (K - 1)) * (w.d.cw + w.d.tw);
+    for (long long m = m0 + (long long)blockIdx.x * G + grp; m < m1; m += (long long)gridDim.x * G)
+        elided_prefix<K, HS, TP>(w, m, sink, dump, single, pairs, sp + grp * words, grp);
 }
 
 size_t elided_smem(int order, int cw, int tw) { return (size_t)(1 << (order - 1)) * (cw + tw) * sizeof(uint64_t); }
 
-template <int K, bool HS>
+template <int K, bool HS, int TP>
 static cudaError_t launch_el(const ScanWork& w, long long m0, long long m1, const CandSink& sink, uint32_t* dump,
                              const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms) {
-    const size_t smem = elided_smem(K, w.d.cw, w.d.tw);
+    constexpr int G = kEThreads / TP;
+    const size_t smem = G * elided_smem(K, w.d.cw, w.d.tw);
+    if (smem > kMaxGroupSmem) return cudaErrorInvalidConfiguration;
     static int per_sm = 0;
     static size_t per_sm_smem = 0;
     if (!per_sm || per_sm_smem != smem) {
-        cudaError_t e = cudaFuncSetAttribute(count_elided<K, HS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(count_elided<K, HS, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, count_elided<K, HS>, kEThreads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, count_elided<K, HS, TP>, kEThreads, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
         per_sm_smem = smem;
     }
-    const long long items = m1 - m0;
-    if (items <= 0) return cudaSuccess;
-    const long long grid = items < (long long)sms * per_sm ? items : (long long)sms * per_sm;
-    count_elided<K, HS><<<(unsigned)grid, kEThreads, smem, s>>>(w, m0, m1, sink, dump, single, pairs);
+    const long long ctas = (m1 - m0 + G - 1) / G;
+    if (ctas <= 0) return cudaSuccess;
+    const long long grid = ctas < (long long)sms * per_sm ? ctas : (long long)sms * per_sm;
+    count_elided<K, HS, TP><<<(unsigned)grid, kEThreads, smem, s>>>(w, m0, m1, sink, dump, single, pairs);
     count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_elided(bool hs, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+template <int K, bool HS>
+static cudaError_t launch_el_tp(int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+                                uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms) {
+    switch (tp) {
+        case 32: return launch_el<K, HS, 32>(w, m0, m1, sink, dump, single, pairs, s, sms);
+        case 64: return launch_el<K, HS, 64>(w, m0, m1, sink, dump, single, pairs, s, sms);
+        case 128: return launch_el<K, HS, 128>(w, m0, m1, sink, dump, single, pairs, s, sms);
+        default: return launch_el<K, HS, 256>(w, m0, m1, sink, dump, single, pairs, s, sms);
+    }
+}
+
+cudaError_t launch_elided(bool hs, int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
                           uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms) {
-    if (w.order == 2) return hs ? launch_el<2, true>(w, m0, m1, sink, dump, single, pairs, s, sms)
-                                : launch_el<2, false>(w, m0, m1, sink, dump, single, pairs, s, sms);
-    if (w.order == 3) return hs ? launch_el<3, true>(w, m0, m1, sink, dump, single, pairs, s, sms)
-                                : launch_el<3, false>(w, m0, m1, sink, dump, single, pairs, s, sms);
+    if (w.order == 2) return hs ? launch_el_tp<2, true>(tp, w, m0, m1, sink, dump, single, pairs, s, sms)
+                                : launch_el_tp<2, false>(tp, w, m0, m1, sink, dump, single, pairs, s, sms);
+    if (w.order == 3) return hs ? launch_el_tp<3, true>(tp, w, m0, m1, sink, dump, single, pairs, s, sms)
+                                : launch_el_tp<3, false>(tp, w, m0, m1, sink, dump, single, pairs, s, sms);
     return cudaErrorInvalidValue;
 }
 

@@ -63,10 +63,11 @@ __device__ __forceinline__ uint32_t pcore(const uint4& v, int cls, int x, int y)
 // 2^(K-1) prefix core rows of both classes are staged whole in shared memory.
 // One prefix (owned ordinal m) of count_elided; synchronises the block.
 // `sp` holds 2^(K-1) * (cw + tw) words.
-template <int K, bool HS>
+// Processed by the TP threads of group `grp` (TP = l-tile width); synchronises that group only.
+template <int K, bool HS, int TP>
 __device__ __forceinline__ void elided_prefix(const ScanWork& w, long long m, const CandSink& sink, uint32_t* dump,
                                               const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
-                                              uint64_t* sp) {
+                                              uint64_t* sp, int grp) {
     constexpr int P = K - 1;
     constexpr int PR = 1 << P;   // prefix core rows
     constexpr int CC = PR * 2;   // counted cells per class
@@ -75,15 +76,16 @@ __device__ __forceinline__ void elided_prefix(const ScanWork& w, long long m, co
     const int S = d.snps, WT = d.cw + d.tw;
     const size_t per_snp = 3 * (size_t)WT;
     const int lane = threadIdx.x & 31;
+    const int gt = threadIdx.x % TP;
     const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
     {
         int c[K];
         unrank((long long)w.dist_offset + m * (long long)w.dist_step, w.dist_n, P, c);
         const int last = c[P - 1];
         if (last + 1 >= S) return;  // uniform across the CTA
-        if (sink.evaluated && threadIdx.x == 0) atomicAdd(sink.evaluated, (unsigned long long)(S - 1 - last));
-        __syncthreads();
-        for (int e = threadIdx.x; e < PR * WT; e += kEThreads) {
+        if (sink.evaluated && gt == 0) atomicAdd(sink.evaluated, (unsigned long long)(S - 1 - last));
+        group_sync<TP>(grp);
+        for (int e = gt; e < PR * WT; e += TP) {
             const int r = e / WT, ww = e - r * WT;
             const bool cls = ww >= d.cw;
             const int W = cls ? d.tw : d.cw, wd = cls ? ww - d.cw : ww;
@@ -95,7 +97,7 @@ __device__ __forceinline__ void elided_prefix(const ScanWork& w, long long m, co
             }
             sp[e] = v;
         }
-        __syncthreads();
+        group_sync<TP>(grp);
         // prefix-only marginals
         uint32_t si[2][2], sj[2][2];
         uint4 pij = make_uint4(0, 0, 0, 0);
@@ -108,8 +110,8 @@ __device__ __forceinline__ void elided_prefix(const ScanWork& w, long long m, co
             }
         if (K == 3) pij = __ldg(pairs + pair_index(c[0], c[1], S));
 
-        for (int l0 = last + 1; l0 < S; l0 += kEThreads) {
-            const int l = l0 + threadIdx.x;
+        for (int l0 = last + 1; l0 < S; l0 += TP) {
+            const int l = l0 + gt;
             const bool valid = l < S;
             long long key = w.base_key;
             uint32_t cnt[2][CC];

@@ -20,7 +20,7 @@ namespace {
 struct Plan {
     int idx;           // index in the caller's array
     ScanWork w;
-    int kind;
+    int kind, tp;
     unsigned keep, cap, outputs;
     const fiu_resident* res;
     size_t off_cand, off_scored, off_comb, off_val, off_val64;  // byte offsets in the arena
@@ -53,8 +53,8 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             continue;
         }
         if (sc.outputs == 0 || w.n_prefixes == 0) continue;
-        int kind = 0;
-        if ((rc = choose_kernel(ctx, sc.res, sc.order, ctx->kernel, kind))) {
+        int kind = 0, tp = 256;
+        if ((rc = choose_tile(ctx, sc.res, w, ctx->kernel, kind, tp))) {
             sc.status = rc;
             continue;
         }
@@ -66,6 +66,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
         p.idx = (int)i;
         p.w = w;
         p.kind = kind;
+        p.tp = tp;
         p.keep = sc.outputs + std::max(32u, sc.outputs / 8);
         p.cap = (unsigned)std::max<size_t>({32768, (size_t)16 * p.keep, (size_t)sc.res->d.snps + p.keep});
         p.outputs = sc.outputs;
@@ -89,7 +90,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
         std::vector<RoundEntry> ents;
         std::vector<size_t> grp_first;      // entries of group g = [grp_first[g], grp_first[g+1])
         std::vector<long long> grp_total;   // items of group g
-        std::vector<int> grp_family;
+        std::vector<int> grp_family, grp_tp;
         std::vector<long long> cursor(n, 0), chunk(n);
         for (int s = 0; s < n; ++s) {
             const auto& w = plans[s].w;
@@ -104,17 +105,20 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
                 const long long left = plans[s].w.n_prefixes - cursor[s];
                 if (left > 0) take[s] = std::min(left, chunk[s]);
             }
-            for (int fam = 0; fam < 2; ++fam) {
-                long long total = 0;
-                grp_first.push_back(ents.size());
-                for (int s = 0; s < n; ++s) {
-                    if (!take[s] || (plans[s].kind == FIU_KERNEL_FULL) != (fam == 1)) continue;
-                    ents.push_back(RoundEntry{s, 0, cursor[s], total});
-                    total += take[s];
+            for (int fam = 0; fam < 2; ++fam)
+                for (int tp : {32, 64, 128, 256}) {
+                    long long total = 0;
+                    grp_first.push_back(ents.size());
+                    for (int s = 0; s < n; ++s) {
+                        if (!take[s] || (plans[s].kind == FIU_KERNEL_FULL) != (fam == 1) || plans[s].tp != tp)
+                            continue;
+                        ents.push_back(RoundEntry{s, 0, cursor[s], total});
+                        total += take[s];
+                    }
+                    grp_total.push_back(total);
+                    grp_family.push_back(fam);
+                    grp_tp.push_back(tp);
                 }
-                grp_total.push_back(total);
-                grp_family.push_back(fam);
-            }
             for (int s = 0; s < n; ++s) {
                 cursor[s] += take[s];
                 chunk[s] *= 4;
@@ -141,6 +145,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             ScanDesc& d = descs[s];
             d.w = p.w;
             d.kind = p.kind;
+            d.tp = p.tp;
             d.keep = p.keep;
             d.cap = p.cap;
             d.outputs = p.outputs;
@@ -177,9 +182,9 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             for (size_t g = 0; g + 1 < grp_first.size() && e == cudaSuccess; ++g) {
                 const int ne = (int)(grp_first[g + 1] - grp_first[g]);
                 if (ne)
-                    e = launch_round(grp_family[g], d_desc, d_state, d_ents + grp_first[g], ne, grp_total[g], smem,
-                                     ctx->sms, st);
-                if (e == cudaSuccess && grp_family[g] == 1) e = launch_select_scans(d_desc, d_state, n, 0, st);
+                    e = launch_round(grp_family[g], grp_tp[g], d_desc, d_state, d_ents + grp_first[g], ne,
+                                     grp_total[g], smem, ctx->sms, st);
+                if (e == cudaSuccess && g % 8 == 7) e = launch_select_scans(d_desc, d_state, n, 0, st);
             }
             if (e == cudaSuccess) e = launch_select_scans(d_desc, d_state, n, 1, st);
             if (e == cudaSuccess) e = launch_finish_scans(d_desc, d_state, d_slots, n, total_slots, st);

@@ -12,6 +12,11 @@ __host__ __device__ constexpr int pow3(int k) { return k == 0 ? 1 : 3 * pow3(k -
 constexpr int kThreads = 256;   // one last SNP per thread, 256 per l-block
 constexpr int kWordChunk = 64;  // prefix words staged per pass
 
+// Shared-memory words one group of the full-table kernel stages.
+__host__ __device__ constexpr int full_group_words(int order) {
+    return (pow3(order - 1) < 9 ? pow3(order - 1) : 9) * kWordChunk;
+}
+
 // ---------------------------------------------------------------------------
 // Kernel 0: full 3^K table for any data.  One CTA iterates owned prefixes
 // (grid-stride over prefix ordinals [m0, m1)); per prefix it stages the
@@ -20,11 +25,12 @@ constexpr int kWordChunk = 64;  // prefix words staged per pass
 // last-SNP rows from the SNP-fastest transposed copy (coalesced 256 B per warp).
 // Prefix rows are processed in groups of up to 9 so that the accumulators
 // (2 classes x 27) stay in registers for every order.
-// One prefix (owned ordinal m) of count_full: every block thread takes part
-// (the function synchronises the block).  `sp` holds RG * kWordChunk words.
-template <int K>
+// One prefix (owned ordinal m) of count_full, processed by the TP threads of
+// group `grp` (TP = last SNPs per pass, the l-tile width); the function
+// synchronises that group only.  `sp` holds RG * kWordChunk words.
+template <int K, int TP>
 __device__ __forceinline__ void full_prefix(const ScanWork& w, long long m, const CandSink& sink, uint32_t* dump,
-                                            uint64_t* sp) {
+                                            uint64_t* sp, int grp) {
     constexpr int P = K - 1;
     constexpr int ROWS = pow3(P);
     constexpr int RG = ROWS < 9 ? ROWS : 9;
@@ -34,14 +40,15 @@ __device__ __forceinline__ void full_prefix(const ScanWork& w, long long m, cons
     const int S = d.snps;
     const size_t per_snp = 3 * (size_t)(d.cw + d.tw);
     const int lane = threadIdx.x & 31;
+    const int gt = threadIdx.x % TP;
     {
         int c[K];
         unrank((long long)w.dist_offset + m * (long long)w.dist_step, w.dist_n, P, c);
         const int last = c[P - 1];
-        if (sink.evaluated && threadIdx.x == 0 && last + 1 < S)
+        if (sink.evaluated && gt == 0 && last + 1 < S)
             atomicAdd(sink.evaluated, (unsigned long long)(S - 1 - last));
-        for (int l0 = last + 1; l0 < S; l0 += kThreads) {
-            const int l = l0 + threadIdx.x;
+        for (int l0 = last + 1; l0 < S; l0 += TP) {
+            const int l = l0 + gt;
             const bool valid = l < S;
             long long key = w.base_key;
             for (int g = 0; g < NG; ++g) {
@@ -54,8 +61,8 @@ __device__ __forceinline__ void full_prefix(const ScanWork& w, long long m, cons
                     const int roff = cls ? 3 * d.cw : 0;
                     for (int w0 = 0; w0 < W; w0 += kWordChunk) {
                         const int wn = min(kWordChunk, W - w0);
-                        __syncthreads();
-                        for (int e = threadIdx.x; e < RG * wn; e += kThreads) {
+                        group_sync<TP>(grp);
+                        for (int e = gt; e < RG * wn; e += TP) {
                             const int rr = e / wn, ww = e - rr * wn;
                             int rem = g * RG + rr;
                             uint64_t v = ~0ull;
@@ -67,7 +74,7 @@ __device__ __forceinline__ void full_prefix(const ScanWork& w, long long m, cons
                             }
                             sp[rr * kWordChunk + ww] = v;
                         }
-                        __syncthreads();
+                        group_sync<TP>(grp);
                         if (valid) {
                             const uint64_t* col = d.tr + (size_t)(roff + w0) * S + l;
                             for (int ww = 0; ww < wn; ++ww) {

@@ -27,6 +27,7 @@ struct ScoredRec {  // a re-scored candidate (FP64 MI, combination code, fixed-p
 struct ScanDesc {  // per scan, read-only on the device
     ScanWork w;
     int kind;          // FIU_KERNEL_FULL / _ELIDED_POPC / _ELIDED_HS
+    int tp;            // threads per prefix (l-tile width): 32, 64, 128 or 256
     unsigned keep;     // candidates kept between rounds (outputs + margin)
     unsigned cap;      // candidate buffer capacity
     unsigned outputs;
@@ -57,12 +58,26 @@ struct RoundEntry {  // owned prefix ordinals [m0, m0 + n) of scan `scan`, items
 
 // batch.cu
 size_t round_smem(const ScanDesc& sd);
-cudaError_t launch_round(int family, const ScanDesc* scans, ScanState* states, const RoundEntry* ents, int n_ents,
-                         long long total, size_t smem, int sms, cudaStream_t s);
+// family: 0 reduced-work kernels (orders 2-3), 1 full table (orders 2-4); tp as in ScanDesc.
+cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* states, const RoundEntry* ents,
+                         int n_ents, long long total, size_t smem, int sms, cudaStream_t s);
 cudaError_t launch_select_scans(const ScanDesc* scans, ScanState* states, int n_scans, int final_pass,
                                 cudaStream_t s);
 cudaError_t launch_finish_scans(const ScanDesc* scans, ScanState* states, const unsigned* slot_begin, int n_scans,
                                 unsigned total_slots, cudaStream_t s);
+
+// Synchronises the TP threads of group `grp` of a 256-thread block: the whole
+// block, one warp, or a named barrier (ids 1..8) for 64 / 128 threads.
+template <int TP>
+__device__ __forceinline__ void group_sync(int grp) {
+    if (TP >= 256) {
+        __syncthreads();
+    } else if (TP == 32) {
+        __syncwarp();
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(TP) : "memory");
+    }
+}
 
 // Launch-count bookkeeping (kernels of this library only).
 extern thread_local unsigned long long* g_launch_counter;
@@ -70,16 +85,19 @@ inline void count_launch(unsigned n = 1) {
     if (g_launch_counter) *g_launch_counter += n;
 }
 
-// count.cu -- contingency tables + fused fixed-point MI + candidate filter.
-// kernel 0: generic full 3^k table (any one-hot or not data, orders 2..8).
-cudaError_t launch_count(int kernel, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+// Largest dynamic shared memory a counting kernel may use (all groups).
+constexpr size_t kMaxGroupSmem = 200 * 1024;
+
+// count.cu -- generic full 3^k table kernel (any data, orders 2..8) with the
+// fused fixed-point MI and the candidate filter; tp = threads per prefix
+// (32, 64, 128 or 256; orders above 5 always use 256).
+cudaError_t launch_count(int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
                          uint32_t* dump, cudaStream_t s, int sms);
-long long combos_per_prefix_hint(const ScanWork& w);
 
 // elided.cu -- reduced-work kernels for one-hot data, orders 2 and 3.
 cudaError_t build_cores(const DevData& d, uint32_t* single, uint4* pairs, int sms, cudaStream_t s);
 size_t elided_smem(int order, int cw, int tw);
-cudaError_t launch_elided(bool hs, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+cudaError_t launch_elided(bool hs, int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
                           uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms);
 
 // layout.cu -- device layouts of a data set.

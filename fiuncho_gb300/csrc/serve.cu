@@ -40,7 +40,7 @@ struct ServeScan {
     fiu_resident* res = nullptr;
     int slot = -1;
     ScanWork w{};
-    int kind = 0;
+    int kind = 0, tp = 256;
     unsigned keep = 0, cap = 0;
     long long cursor = 0, chunk = 1, max_chunk = 1;
     size_t bytes = 0;
@@ -148,7 +148,7 @@ bool admit(fiu_server* sv, ServeScan* s) {
         finish(sv, s, FIU_OK);
         return false;
     }
-    if ((rc = choose_kernel(ctx, s->res, s->order, ctx->kernel, s->kind))) {
+    if ((rc = choose_tile(ctx, s->res, s->w, ctx->kernel, s->kind, s->tp))) {
         finish(sv, s, rc);
         return false;
     }
@@ -179,6 +179,7 @@ bool admit(fiu_server* sv, ServeScan* s) {
     ScanDesc d{};
     d.w = s->w;
     d.kind = s->kind;
+    d.tp = s->tp;
     d.keep = s->keep;
     d.cap = s->cap;
     d.outputs = s->outputs;
@@ -213,6 +214,7 @@ int run_round(fiu_server* sv) {
         ScanDesc d{};
         d.w = s->w;
         d.kind = s->kind;
+        d.tp = s->tp;
         smem = std::max(smem, round_smem(d));
     }
     std::vector<long long> take(sv->active.size(), 0);
@@ -220,17 +222,20 @@ int run_round(fiu_server* sv) {
         ServeScan* s = sv->active[i];
         take[i] = std::min({s->w.n_prefixes - s->cursor, s->chunk, s->max_chunk});
     }
-    for (int fam = 0; fam < 2; ++fam) {
-        const size_t first = ents.size();
-        long long total = 0;
-        for (size_t i = 0; i < sv->active.size(); ++i) {
-            ServeScan* s = sv->active[i];
-            if (!take[i] || (s->kind == FIU_KERNEL_FULL) != (fam == 1)) continue;
-            ents.push_back(RoundEntry{s->slot, 0, s->cursor, total});
-            total += take[i];
+    std::vector<std::pair<int, int>> gkey;  // (family, tp) of each group
+    for (int fam = 0; fam < 2; ++fam)
+        for (int tp : {32, 64, 128, 256}) {
+            const size_t first = ents.size();
+            long long total = 0;
+            for (size_t i = 0; i < sv->active.size(); ++i) {
+                ServeScan* s = sv->active[i];
+                if (!take[i] || (s->kind == FIU_KERNEL_FULL) != (fam == 1) || s->tp != tp) continue;
+                ents.push_back(RoundEntry{s->slot, 0, s->cursor, total});
+                total += take[i];
+            }
+            groups.push_back({first, total});
+            gkey.push_back({fam, tp});
         }
-        groups.push_back({first, total});
-    }
     int rc = FIU_OK;
     if (ents.size() > sv->ents_cap) {
         cudaFree(sv->d_ents);
@@ -242,11 +247,11 @@ int run_round(fiu_server* sv) {
     CK(prepare_round_kernels(smem), "kernel attributes");
     CK(cudaMemcpyAsync(sv->d_ents, ents.data(), ents.size() * sizeof(RoundEntry), cudaMemcpyHostToDevice, st),
        "round entries");
-    for (int fam = 0; fam < 2; ++fam) {
-        const size_t first = groups[fam].first;
-        const size_t ne = (fam == 0 ? groups[1].first : ents.size()) - first;
-        if (ne) CK(launch_round(fam, sv->d_desc, sv->d_state, sv->d_ents + first, (int)ne, groups[fam].second, smem,
-                                ctx->sms, st), "round");
+    for (size_t g = 0; g < groups.size(); ++g) {
+        const size_t first = groups[g].first;
+        const size_t ne = (g + 1 < groups.size() ? groups[g + 1].first : ents.size()) - first;
+        if (ne) CK(launch_round(gkey[g].first, gkey[g].second, sv->d_desc, sv->d_state, sv->d_ents + first, (int)ne,
+                                groups[g].second, smem, ctx->sms, st), "round");
     }
     CK(launch_select_scans(sv->d_desc, sv->d_state, kSlots, 0, st), "selection");
     std::vector<ServeScan*> done, still;

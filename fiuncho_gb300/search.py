@@ -242,14 +242,22 @@ class GpuSearch:
                                                _lib.ptr(cc, C.c_uint32), _lib.ptr(tt, C.c_uint32)))
         return cc, tt
 
-    def scan_tables(self, resident: Resident, order: int, distribution: Distribution, kernel: int = 0):
+    def set_autotune(self, enable: bool):
+        self.ctx.check(self.ctx.lib.fiu_set_autotune(self.ctx.h, 1 if enable else 0))
+
+    def last_tile(self):
+        k, t = C.c_int(0), C.c_int(0)
+        self.ctx.check(self.ctx.lib.fiu_last_tile(self.ctx.h, C.byref(k), C.byref(t)))
+        return k.value, t.value
+
+    def scan_tables(self, resident: Resident, order: int, distribution: Distribution, kernel: int = 0, tp: int = 0):
         import math
         total = math.comb(distribution.n, distribution.k)
         owned = (total - 1 - distribution.offset) // distribution.step + 1 if distribution.offset < total else 0
         cells = 3 ** order
         out = np.full(owned * resident.snps * 2 * cells, 0xFFFFFFFF, np.uint32)
         dist = distribution.c_struct()
-        self.ctx.check(self.ctx.lib.fiu_scan_tables(self.ctx.h, resident.h, order, C.byref(dist), kernel,
+        self.ctx.check(self.ctx.lib.fiu_scan_tables(self.ctx.h, resident.h, order, C.byref(dist), kernel + 256 * tp,
                                                     _lib.ptr(out, C.c_uint32), out.size))
         return out.reshape(owned, resident.snps, 2, cells)
 

@@ -97,6 +97,13 @@ int fiu_probe_popc_rate(fiu_ctx *ctx, double *word_ops_per_s);
  * fail with FIU_ERR_UNSUPPORTED. */
 int fiu_set_kernel(fiu_ctx *ctx, int kernel);
 
+/* Autotuning of the counting kernel's variant and l-tile width (threads per
+ * prefix: 32, 64, 128 or 256) on a sample of each large request (default on;
+ * results never depend on it).  fiu_last_tile reports the kernel and width the
+ * last single-scan search used. */
+int fiu_set_autotune(fiu_ctx *ctx, int enable);
+int fiu_last_tile(const fiu_ctx *ctx, int *kernel, int *tp);
+
 /* ---- data sets -------------------------------------------------------------- */
 /* Copies a host data set to the device (Dataset<uint64_t>::read output ->
  * device buffers) and derives the device layouts the kernels read. */
@@ -212,7 +219,8 @@ int fiu_mi_compute_noalloc(const uint32_t *d_cases, const uint32_t *d_ctrls, siz
  * (count x order ascending indices), computed on the device. */
 int fiu_tables(fiu_ctx *ctx, const fiu_resident *res, unsigned order, const int32_t *combinations, size_t count,
                uint32_t *cases_out, uint32_t *ctrls_out);
-/* The hot kernel's own tables for every combination of a (small) search:
+/* The hot kernel's own tables for every combination of a (small) search
+ * (kernel = FIU_KERNEL_* + 256 * l-tile width, width 0 = automatic):
  * out[((m * snps) + l) * 2 * 3^order + class * 3^order + cell] for owned
  * prefix ordinal m and last SNP l (entries with l <= prefix end stay as given). */
 int fiu_scan_tables(fiu_ctx *ctx, const fiu_resident *res, unsigned order, const fiu_distribution *distribution,

@@ -54,7 +54,7 @@ def bins():
 
 def test_cpp_gpusearch_reference_checks(bins, raw_file, golden_testdata, tmp_path):
     m = tmp_path / "mpi3snp.txt"
-    m.write_text("".join("%d %d %d %r\n" % (a, b, c, v) for (a, b, c), v in
+    m.write_text("".join("%d %d %d %.9g\n" % (int(a), int(b), int(c), float(v)) for (a, b, c), v in
                          zip(golden_testdata["mpi3snp_combos"], golden_testdata["mpi3snp_vals"])))
     r = subprocess.run([bins["test_gpusearch"], raw_file, str(m)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "PASS" in r.stdout, r.stdout + r.stderr

@@ -298,3 +298,30 @@ def test_order3_300x8000_top100(gs, oracle):
     ds = Dataset.from_genotypes(geno, is_case)
     res, v64 = gs.run(ds, 3, Distribution(ds.snps, 2), 100, with_fp64=True)
     _check_topn(oracle, ds, 3, 100, res, v64, threads=16)
+
+
+@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 3), (3, 3), (3, 2)])
+def test_tiles_agree(oracle, order, kernel):
+    """Every l-tile width (threads per prefix 32/64/128/256) of each kernel gives
+    the same tables, and searches with autotuning on/off give identical lists."""
+    from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident
+    rng = np.random.default_rng(order * 10 + kernel)
+    snps, n_case, n_ctrl = 45, 333, 700
+    maf = rng.uniform(0.05, 0.5, snps)[:, None]
+    u = rng.random((snps, n_case + n_ctrl))
+    geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
+    ds = Dataset.from_genotypes(geno, np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)])
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    dist = Distribution(snps, order - 1)
+    tabs = [g.scan_tables(res, order, dist, kernel=kernel, tp=tp) for tp in (32, 64, 128, 256)]
+    mask = tabs[0] != 0xFFFFFFFF
+    for t in tabs[1:]:
+        assert np.array_equal(t[mask], tabs[0][mask])
+    g.set_kernel(kernel)
+    a = g.run(res, order, dist, 30, with_fp64=True)
+    g.set_autotune(False)
+    b = g.run(res, order, dist, 30, with_fp64=True)
+    assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
+    r = [type("R", (), {"combination": x.combination, "val": x.val})() for x in a[0]]
+    _check_topn(oracle, ds, order, 30, r, a[1])
