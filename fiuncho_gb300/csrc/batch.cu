@@ -49,11 +49,14 @@ __host__ __device__ inline size_t group_words(const ScanDesc& sd) {
 
 size_t round_smem(const ScanDesc& sd) { return (size_t)(kRoundThreads / sd.tp) * group_words(sd) * sizeof(uint64_t); }
 
+// The groups of one CTA may work on prefixes of different scans at once, so
+// every group owns a fixed slice of `stride` words (the launch's shared memory
+// divided by the groups), never a slice sized by its current scan.
 template <int FAMILY, int TP>
 __global__ void __launch_bounds__(kRoundThreads, 2) round_kernel(const ScanDesc* __restrict__ scans,
                                                                  ScanState* states,
                                                                  const RoundEntry* __restrict__ ents, int n_ents,
-                                                                 long long total) {
+                                                                 long long total, size_t stride) {
     extern __shared__ uint64_t sm[];
     constexpr int G = kRoundThreads / TP;
     const int grp = threadIdx.x / TP;
@@ -69,7 +72,7 @@ __global__ void __launch_bounds__(kRoundThreads, 2) round_kernel(const ScanDesc*
         ScanState* st = states + e.scan;
         const CandSink sink{sd.cand, &st->count, &st->overflow, sd.cap,
                             *reinterpret_cast<volatile long long*>(&st->thr), &st->evaluated};
-        run_prefix<FAMILY, TP>(sd, e.m0 + (g - e.begin), sink, sm + grp * group_words(sd), grp);
+        run_prefix<FAMILY, TP>(sd, e.m0 + (g - e.begin), sink, sm + grp * stride, grp);
     }
 }
 
@@ -126,7 +129,8 @@ cudaError_t prepare_round_kernels(size_t smem) {
 template <int FAMILY, int TP>
 static void launch_round_t(unsigned grid, size_t smem, const ScanDesc* scans, ScanState* states,
                            const RoundEntry* ents, int n_ents, long long total, cudaStream_t s) {
-    round_kernel<FAMILY, TP><<<grid, kRoundThreads, smem, s>>>(scans, states, ents, n_ents, total);
+    const size_t stride = smem / sizeof(uint64_t) / (kRoundThreads / TP);
+    round_kernel<FAMILY, TP><<<grid, kRoundThreads, smem, s>>>(scans, states, ents, n_ents, total, stride);
 }
 
 cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* states, const RoundEntry* ents,

@@ -215,7 +215,9 @@ __device__ __forceinline__ void elided_prefix(const ScanWork& w, long long m, co
                 }
 #pragma unroll
                 for (int q = 0; q < CELLS; ++q) {
-                    const uint32_t a = full[0][q], b = full[1][q];
+                    // derived cells of consistent one-hot data never exceed the class
+                    // size; the clamp keeps any inconsistency inside the table
+                    const uint32_t a = min(full[0][q], ncls[0]), b = min(full[1][q], ncls[1]);
                     key += __ldg(d.ftab + a) + __ldg(d.ftab + b) - __ldg(d.ftab + a + b);
                 }
                 if (dump) {
