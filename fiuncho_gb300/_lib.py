@@ -18,7 +18,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "fiuncho_gpu.h")
 FIU_OK, FIU_ERR_INVALID, FIU_ERR_NOMEM, FIU_ERR_CUDA, FIU_ERR_UNSUPPORTED, FIU_ERR_TIMEOUT, FIU_ERR_CANCELLED = \
     range(7)
 FIU_MAX_ORDER = 8
-KERNEL_AUTO, KERNEL_FULL, KERNEL_ELIDED_POPC, KERNEL_ELIDED_HS = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_FULL, KERNEL_ELIDED_POPC, KERNEL_ELIDED_HS, KERNEL_TENSOR = 0, 1, 2, 3, 4
 FIU_MAX_OUTPUTS = 7000
 FIU_NOALLOC_MAX_SAMPLES = 65536
 

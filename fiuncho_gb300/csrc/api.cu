@@ -102,8 +102,9 @@ int choose_kernel(fiu_ctx* ctx, const fiu_resident* res_c, unsigned order, int r
     const bool elided_ok = res->one_hot && (order == 2 || order == 3) && res->d.n_cases <= 65535 &&
                            res->d.n_ctrls <= 65535 && elided_smem(order, res->d.cw, res->d.tw) <= 160 * 1024;
     kernel = requested ? requested : (elided_ok ? FIU_KERNEL_ELIDED_HS : FIU_KERNEL_FULL);
-    if (kernel < FIU_KERNEL_FULL || kernel > FIU_KERNEL_ELIDED_HS)
-        return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
+    if (kernel < FIU_KERNEL_FULL || kernel > FIU_KERNEL_TENSOR) return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
+    if (kernel == FIU_KERNEL_TENSOR && order != 3)
+        return fail(ctx, FIU_ERR_UNSUPPORTED, "the tensor-core kernel serves order 3");
     if (kernel == FIU_KERNEL_FULL) return FIU_OK;
     if (!elided_ok)
         return fail(ctx, FIU_ERR_UNSUPPORTED, "elided kernels need one-hot data, order 2 or 3, classes <= 65535");
@@ -150,7 +151,32 @@ static int heuristic_tp(int kernel, const ScanWork& w) {
     return tp;
 }
 
-int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp) {
+static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
+    return res->one_hot && w.order == 3 && w.dist_step == 1 && w.dist_offset == 0 && w.dist_n == res->d.snps &&
+           res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 && res->d.snps < (1 << 21);
+}
+
+int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp,
+                bool allow_tensor) {
+    if (requested_kernel == FIU_KERNEL_TENSOR || (requested_kernel == FIU_KERNEL_AUTO && allow_tensor &&
+                                                   tensor_ok(res, w))) {
+        if (!allow_tensor || !tensor_ok(res, w))
+            return fail(ctx, FIU_ERR_UNSUPPORTED,
+                        "the tensor-core kernel needs one-hot data, order 3 and the whole data set on one worker");
+        int rc = choose_kernel(ctx, res, 3, FIU_KERNEL_ELIDED_HS, kernel);  // builds the core tables
+        if (rc) return rc;
+        fiu_resident* r = const_cast<fiu_resident*>(res);
+        if (!r->t3_items) {
+            std::vector<long long> ib;
+            r->t3_total = tensor3_items(r->d.snps, ib);
+            cudaError_t e = cudaMalloc((void**)&r->t3_items, ib.size() * sizeof(long long));
+            if (e == cudaSuccess) e = cudaMemcpy(r->t3_items, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor work items");
+        }
+        kernel = FIU_KERNEL_TENSOR;
+        tp = 256;
+        return FIU_OK;
+    }
     int rc = choose_kernel(ctx, res, (unsigned)w.order, requested_kernel, kernel);
     if (rc) return rc;
     tp = heuristic_tp(kernel, w);
@@ -226,9 +252,13 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     if (outputs == 0 || w.n_prefixes == 0) return FIU_OK;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     int tp = 256;
-    if ((rc = choose_tile(ctx, res, w, kernel ? kernel : ctx->kernel, kernel, tp))) return rc;
+    if ((rc = choose_tile(ctx, res, w, kernel ? kernel : ctx->kernel, kernel, tp, true))) return rc;
     ctx->last_kernel = kernel;
     ctx->last_tp = tp;
+    const bool tensor = kernel == FIU_KERNEL_TENSOR;
+    const long long units = tensor ? res->t3_total : w.n_prefixes;
+    int* t_status = (int*)(ctx->ctl + 16);
+    if (tensor) CK(cudaMemsetAsync(t_status, 0, sizeof(int), ctx->stream), "status reset");
     const unsigned keep = outputs + std::max(32u, outputs / 8);
     const size_t cap = std::max<size_t>({65536, (size_t)16 * keep, (size_t)res->d.snps + keep});
     if ((rc = grow(ctx, ctx->cand, ctx->cand_cap, cap)) ||
@@ -242,16 +272,21 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     long long thr = (long long)0x8000000000000000ull;
     unsigned have = 0;
     const double per_prefix = (double)binom(w.dist_n, order) / std::max<double>(1.0, (double)binom(w.dist_n, order - 1));
-    long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_prefix)));
+    const double per_unit = tensor ? (double)kT3ItemCombos : per_prefix;
+    long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_unit)));
     long long m = 0;
-    while (m < w.n_prefixes) {
-        const long long m1 = std::min(w.n_prefixes, m + chunk);
+    while (m < units) {
+        const long long m1 = std::min(units, m + chunk);
         ctx->pinned[0] = have;
         ctx->pinned[1] = 0;
         CK(cudaMemcpyAsync(count, ctx->pinned, 2 * sizeof(unsigned), cudaMemcpyHostToDevice, s), "reset counters");
         CandSink sink{ctx->cand, count, overflow, (unsigned)cap, thr, ctx->timing ? ctx->evaluated : nullptr};
         if (ctx->timing) CK(cudaEventRecord(ctx->ev0, s), "event");
-        CK(launch_kernel(kernel, tp, res, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
+        if (tensor)
+            CK(launch_tensor3(w, res->t3_items, m, m1, sink, nullptr, res->single, res->pairs, t_status, s, ctx->sms),
+               "tensor kernel launch");
+        else
+            CK(launch_kernel(kernel, tp, res, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
         if (ctx->timing) CK(cudaEventRecord(ctx->ev1, s), "event");
         CK(cudaMemcpyAsync(ctx->pinned, count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read counters");
         CK(cudaStreamSynchronize(s), "count kernel");
@@ -281,6 +316,12 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
         m = m1;
         if (fresh < cap / 8) chunk *= 4;
         else if (fresh > cap / 2) chunk = std::max<long long>(1, chunk / 2);
+    }
+    if (tensor) {
+        int st = 0;
+        CK(cudaMemcpyAsync(&st, t_status, sizeof(int), cudaMemcpyDeviceToHost, s), "status");
+        CK(cudaStreamSynchronize(s), "status");
+        if (st) return fail(ctx, FIU_ERR_TIMEOUT, "tensor kernel: a tensor-memory wait ran past its limit");
     }
     // Final order of the kept set, then FP64 re-score of every kept candidate.
     CK(select_top(ctx->cand, have, keep, ctx->tmp, scratch, s), "top-N selection");
@@ -368,7 +409,7 @@ int fiu_last_tile(const fiu_ctx* ctx, int* kernel, int* tp) {
 
 int fiu_set_kernel(fiu_ctx* ctx, int kernel) {
     if (!ctx) return FIU_ERR_INVALID;
-    if (kernel < FIU_KERNEL_AUTO || kernel > FIU_KERNEL_ELIDED_HS) return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
+    if (kernel < FIU_KERNEL_AUTO || kernel > FIU_KERNEL_TENSOR) return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
     ctx->kernel = kernel;
     return FIU_OK;
 }
@@ -474,6 +515,7 @@ void fiu_dataset_free(fiu_ctx* ctx, fiu_resident* r) {
     cudaFree(r->ftab);
     cudaFree(r->single);
     cudaFree(r->pairs);
+    cudaFree(r->t3_items);
     delete r;
 }
 
@@ -648,16 +690,27 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     int tp = (kernel >> 8) & 0x1ff;
     kernel &= 0xff;
-    if ((rc = choose_kernel(ctx, res, order, kernel, kernel))) return rc;
-    if (tp != 32 && tp != 64 && tp != 128 && tp != 256) tp = heuristic_tp(kernel, w);
-    if (!tile_ok(kernel, tp, w)) return fail(ctx, FIU_ERR_UNSUPPORTED, "l-tile width not available for this request");
+    if (kernel == FIU_KERNEL_TENSOR) {
+        if ((rc = choose_tile(ctx, res, w, kernel, kernel, tp, true))) return rc;
+    } else {
+        if ((rc = choose_kernel(ctx, res, order, kernel, kernel))) return rc;
+        if (tp != 32 && tp != 64 && tp != 128 && tp != 256) tp = heuristic_tp(kernel, w);
+        if (!tile_ok(kernel, tp, w)) return fail(ctx, FIU_ERR_UNSUPPORTED, "l-tile width not available for this request");
+    }
     cudaStream_t s = ctx->stream;
     uint32_t* d = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&d, need * 4, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d, out, need * 4, cudaMemcpyHostToDevice, s);
     CandSink sink{ctx->cand, ctx->ctl, ctx->ctl + 1, 0, (long long)0x7fffffffffffffffll, nullptr};
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ctl, 0, 2 * sizeof(unsigned), s);
-    if (e == cudaSuccess) e = launch_kernel(kernel, tp, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
+    if (e == cudaSuccess && kernel == FIU_KERNEL_TENSOR) {
+        e = cudaMemsetAsync(ctx->ctl + 16, 0, sizeof(int), s);
+        if (e == cudaSuccess)
+            e = launch_tensor3(w, res->t3_items, 0, res->t3_total, sink, d, res->single, res->pairs, (int*)(ctx->ctl + 16),
+                               s, ctx->sms);
+    } else if (e == cudaSuccess) {
+        e = launch_kernel(kernel, tp, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * 4, cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(d, s);
     cudaError_t e2 = cudaStreamSynchronize(s);

@@ -11,6 +11,7 @@ constexpr int kMaxOrder = 8;
 constexpr int FIU_KERNEL_FULL_ID = 1;
 constexpr int FIU_KERNEL_ELIDED_POPC_ID = 2;
 constexpr int FIU_KERNEL_ELIDED_HS_ID = 3;
+constexpr int FIU_KERNEL_TENSOR_ID = 4;
 constexpr int kFixShift = 32;  // fixed-point scale of the c*ln(c) table: 2^32
 
 // Candidate of the running top-N: `key` is the fixed-point N*MI*2^32 (larger

@@ -52,6 +52,8 @@ struct fiu_resident {
     int device = 0;
     uint32_t* single = nullptr;  // single-SNP cores (elided kernels)
     uint4* pairs = nullptr;      // pair cores (elided order-3 kernel)
+    long long* t3_items = nullptr;  // work-item prefix sums of the tensor order-3 kernel
+    long long t3_total = 0;
 };
 
 namespace fiu {
@@ -77,7 +79,8 @@ int choose_kernel(fiu_ctx* ctx, const fiu_resident* res, unsigned order, int req
 // Picks the counting kernel variant and l-tile width (threads per prefix) of a
 // request: measured on a strided sample of its prefixes (cached per shape
 // bucket) when autotuning is on and the request is large, else a heuristic.
-int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp);
+int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp,
+                bool allow_tensor = false);
 cudaError_t launch_kernel(int kernel, int tp, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
                           const CandSink& sink, uint32_t* dump, cudaStream_t s, int sms);
 int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,

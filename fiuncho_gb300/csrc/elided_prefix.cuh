@@ -57,6 +57,46 @@ __device__ __forceinline__ uint32_t pcore(const uint4& v, int cls, int x, int y)
     return (k & 1) ? (w >> 16) : (w & 0xffffu);
 }
 
+// Full order-3 table of one class from its 8 core cells core[(x*2+y)*2+z]
+// (genotypes 0/1), the pair cores of (i,j), (i,l), (j,l), the single cores of
+// i, j, l and the class size: t[(x*3+y)*3+z] for x, y, z in {0,1,2}.
+__device__ __forceinline__ void expand3(const uint32_t* core, const uint4& pij, const uint4& pil, const uint4& pjl,
+                                        uint32_t si0, uint32_t si1, uint32_t sj0, uint32_t sj1, uint32_t sl0,
+                                        uint32_t sl1, uint32_t n, int cls, uint32_t* t) {
+    const uint32_t si[2] = {si0, si1}, sj[2] = {sj0, sj1};
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) {
+#pragma unroll
+            for (int z = 0; z < 2; ++z) t[(x * 3 + y) * 3 + z] = core[(x * 2 + y) * 2 + z];
+            t[(x * 3 + y) * 3 + 2] = pcore(pij, cls, x, y);
+        }
+#pragma unroll
+    for (int x = 0; x < 2; ++x) {
+#pragma unroll
+        for (int z = 0; z < 2; ++z) t[(x * 3 + 2) * 3 + z] = pcore(pil, cls, x, z);
+        t[(x * 3 + 2) * 3 + 2] = si[x];
+    }
+#pragma unroll
+    for (int y = 0; y < 2; ++y) {
+#pragma unroll
+        for (int z = 0; z < 2; ++z) t[(2 * 3 + y) * 3 + z] = pcore(pjl, cls, y, z);
+        t[(2 * 3 + y) * 3 + 2] = sj[y];
+    }
+    t[24] = sl0;
+    t[25] = sl1;
+    t[26] = n;
+#pragma unroll
+    for (int xy = 0; xy < 9; ++xy) t[xy * 3 + 2] -= t[xy * 3 + 0] + t[xy * 3 + 1];
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int z = 0; z < 3; ++z) t[(x * 3 + 2) * 3 + z] -= t[(x * 3 + 0) * 3 + z] + t[(x * 3 + 1) * 3 + z];
+#pragma unroll
+    for (int yz = 0; yz < 9; ++yz) t[18 + yz] -= t[yz] + t[9 + yz];
+}
+
 // ---------------------------------------------------------------------------
 // The reduced-work counting kernel.  Same scheduling as count_full: CTA per
 // owned prefix (grid-stride over ordinals), one last SNP l per thread; the

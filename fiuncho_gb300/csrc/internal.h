@@ -1,6 +1,8 @@
 // Host-side declarations shared by the library's translation units.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace fiu {
@@ -99,6 +101,13 @@ cudaError_t build_cores(const DevData& d, uint32_t* single, uint4* pairs, int sm
 size_t elided_smem(int order, int cw, int tw);
 cudaError_t launch_elided(bool hs, int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
                           uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms);
+
+// tensor3.cu -- order-3 core cells on tcgen05 (one-hot data, whole data set, one worker).
+constexpr int kT3ItemCombos = 2048;  // combinations per work item, about (32 x 128 / 2)
+long long tensor3_items(int n, std::vector<long long>& item_begin);
+cudaError_t launch_tensor3(const ScanWork& w, const long long* item_begin, long long g0, long long g1,
+                           const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
+                           int* status, cudaStream_t s, int sms);
 
 // layout.cu -- device layouts of a data set.
 cudaError_t launch_transpose(const uint64_t* ref, uint64_t* tr, int snps, int rows, cudaStream_t s);
