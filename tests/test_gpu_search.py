@@ -65,11 +65,12 @@ def test_combine_and_popcnt_bit_exact(gs, oracle, golden_testdata):
     assert np.all(cc[27:] == 0) and np.all(tt[27:] == 0)
 
 
-@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 2), (3, 2), (2, 3), (3, 3)])
+@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 2), (3, 2), (2, 3), (3, 3), (3, 4)])
 def test_hot_kernel_tables_bit_exact_reference(gs, golden_testdata, order, kernel):
     """Each counting kernel's own contingency tables for EVERY combination of the
     reference's test data == the reference's combine_and_popcnt tables
-    (kernel 1: full table; 2, 3: core cells + exact marginals, POPC / Harley-Seal)."""
+    (kernel 1: full table; 2, 3: core cells + exact marginals, POPC / Harley-Seal;
+    4: core cells on the tcgen05 tensor cores)."""
     from fiuncho_gb300 import Distribution, Resident
     ds = _ds_from_golden(golden_testdata)
     res = Resident(gs.ctx, ds)
@@ -248,7 +249,7 @@ def test_kernels_agree(oracle, n_case, n_ctrl, snps):
     ds = Dataset.from_genotypes(geno, is_case)
     for order in (2, 3):
         outs, tabs = [], []
-        for kernel in (1, 2, 3):
+        for kernel in ((1, 2, 3) if order == 2 else (1, 2, 3, 4)):
             g = GpuSearch(0, kernel=kernel)
             res = Resident(g.ctx, ds)
             assert res.one_hot
@@ -262,6 +263,25 @@ def test_kernels_agree(oracle, n_case, n_ctrl, snps):
             assert o[0] == outs[0][0] and np.array_equal(o[1], outs[0][1])
         r = [type("R", (), {"combination": c, "val": v})() for c, v in zip(outs[0][0], outs[0][1])]
         _check_topn(oracle, ds, order, 40, r, outs[0][1])
+
+
+def test_tensor_kernel_scope(gs, golden_synth):
+    """The tcgen05 kernel serves one-hot order-3 searches of the whole data set by one
+    worker; a step > 1 distribution falls back to the reduced-work kernel automatically
+    and is refused when the tensor kernel is forced."""
+    from fiuncho_gb300 import Dataset, Distribution, FiunchoError, GpuSearch, Resident
+    ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    g.run(res, 3, Distribution(ds.snps, 2), 10)
+    assert g.last_tile()[0] == 4
+    g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
+    assert g.last_tile()[0] in (2, 3)
+    g.set_kernel(4)
+    with pytest.raises(FiunchoError):
+        g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
+    with pytest.raises(FiunchoError):
+        g.run(res, 2, Distribution(ds.snps, 1), 10)
 
 
 def test_elided_rejects_non_one_hot(gs):
