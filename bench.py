@@ -10,8 +10,11 @@ Output: one JSON line (rank 0).  ``value`` is combinations x samples per second
 with the data set resident in HBM; ``e2e`` is the same metric through the
 public host-buffer call (``fiu_search``: pinned host data set -> device ->
 search -> results to host, all inside the timed region).  ``roofline`` is the
-HBM roofline of the dominant kernel and ``int_roofline`` its integer
-(AND+POPC) roofline against a peak measured live on this GPU.
+roofline of the dominant (counting) kernel: for the tcgen05 kernel the tensor
+bound (2^k multiply-adds per combination and sample, e4m3 peak = 2 x the
+measured dense bf16 rate); for the CUDA-core kernels the HBM bound, with
+``int_roofline`` their integer (AND+POPC) roofline against a peak measured
+live on this GPU.
 ``cpu_baseline`` times the CPU oracle (a C restatement of the reference's
 scalar search) on a bounded prefix sample of the same workload on the host
 cores.
@@ -283,6 +286,7 @@ def run_gpu(args, spec):
         return
     # ---- roofline of the dominant (counting) kernel
     k = spec.order
+    kernel_id, kernel_tp = gs.last_tile()
     ops_per_combo = 3 ** k * (math.ceil(spec.cases / 32) + math.ceil(spec.ctrls / 32))
     avg_launch_s = (kms.value / 1e3) / max(1, klaunch.value)
     ops_per_launch = kcombos.value * ops_per_combo / max(1, klaunch.value)
@@ -301,6 +305,24 @@ def run_gpu(args, spec):
         traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(args.workload)
     except (OSError, ValueError):
         pass
+    if kernel_id == _lib.KERNEL_TENSOR:
+        # 2^k core cells per combination, each a dot product over the samples of its class:
+        # 2^k multiply-adds (2 * 2^k flops) per combination and sample, e4m3 operands.
+        flops_per_launch = kcombos.value * 2 * 2 ** k * spec.samples / max(1, klaunch.value)
+        tc_achieved = flops_per_launch / avg_launch_s / 1e12 if avg_launch_s > 0 else 0.0
+        tc_peak = 2.0 * peaks.get("bf16_tflops", 1900.0)
+        roofline = {"bound": "tensor", "achieved": tc_achieved, "peak": tc_peak, "unit": "TFLOP/s",
+                    "frac": tc_achieved / tc_peak, "traffic": traffic,
+                    "flops_per_combination_sample": 2 * 2 ** k,
+                    "peak_source": "2 x measured dense bf16 (%s; e4m3 dense rate = 2 x bf16), of measured"
+                                   % ("MEASURED_PEAKS.json" if "bf16_tflops" in peaks else "fallback 1.9 PF"),
+                    "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                            "frac": hbm_achieved / hbm_peak}}
+    else:
+        roofline = {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": hbm_achieved / hbm_peak, "traffic": traffic,
+                    "note": "algorithmic bytes = the data set read once per scan; the kernel is integer-pipe "
+                            "bound (int_roofline)"}
     top = out[0] if out else None
     cpu = cpu_sample(spec, ds, seconds=args.cpu_seconds) if args.cpu_seconds > 0 and ws == 1 else None
     batch = None if (args.no_batch or ws > 1) else run_batch_and_serve(args, gs, ctx)
@@ -317,15 +339,15 @@ def run_gpu(args, spec):
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ds_bytes,
                 "d2h_bytes_per_step": spec.outputs * (4 * spec.order + 4) + 8 * 2},
-        "roofline": {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": hbm_achieved / hbm_peak, "traffic": traffic,
-                     "note": "algorithmic bytes = the data set read once per scan; the kernel is integer-pipe "
-                             "bound (int_roofline)"},
+        "roofline": roofline,
         "int_roofline": {"bound": "int", "achieved": int_achieved / 1e12, "peak": peak_rate.value / 1e12,
                          "unit": "T word-ops/s", "frac": int_achieved / peak_rate.value if peak_rate.value else None,
                          "work": "3^k*(ceil(cases/32)+ceil(ctrls/32)) 32-bit AND+POPC per combination",
                          "peak_source": "fiu_probe_popc_rate on this GPU (AND+POPC+ADD microbenchmark)"},
-        "kernel": {"id": args.kernel or "auto", "one_hot": res.one_hot, "count_ms_total": kms.value, "count_launches": klaunch.value, "combinations": kcombos.value},
+        "kernel": {"requested": args.kernel or "auto", "ran": {1: "full", 2: "elided_popc", 3: "elided_hs",
+                                                               4: "tensor"}.get(kernel_id, kernel_id),
+                   "threads_per_prefix": kernel_tp, "one_hot": res.one_hot, "count_ms_total": kms.value,
+                   "count_launches": klaunch.value, "combinations": kcombos.value},
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
         "batched": batch,
