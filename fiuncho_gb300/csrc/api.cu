@@ -153,7 +153,8 @@ static int heuristic_tp(int kernel, const ScanWork& w) {
 
 static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
     return res->one_hot && w.order == 3 && w.dist_step == 1 && w.dist_offset == 0 && w.dist_n == res->d.snps &&
-           res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 && res->d.snps < (1 << 21);
+           res->d.n_cases >= 1 && res->d.n_ctrls >= 1 && res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 &&
+           res->d.snps < (1 << 21);
 }
 
 int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp,
@@ -166,12 +167,17 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
         int rc = choose_kernel(ctx, res, 3, FIU_KERNEL_ELIDED_HS, kernel);  // builds the core tables
         if (rc) return rc;
         fiu_resident* r = const_cast<fiu_resident*>(res);
-        if (!r->t3_items) {
-            std::vector<long long> ib;
-            r->t3_total = tensor3_items(r->d.snps, ib);
-            cudaError_t e = cudaMalloc((void**)&r->t3_items, ib.size() * sizeof(long long));
-            if (e == cudaSuccess) e = cudaMemcpy(r->t3_items, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
-            if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor work items");
+        if (!r->t3) {
+            auto* plan = new (std::nothrow) T3Plan;
+            if (!plan) return fail(ctx, FIU_ERR_NOMEM, "tensor plan");
+            cudaError_t e = tensor3_prepare(r->d, *plan, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) {
+                tensor3_release(*plan);
+                delete plan;
+                return cuda_fail(ctx, e, "tensor operand planes");
+            }
+            r->t3 = plan;
         }
         kernel = FIU_KERNEL_TENSOR;
         tp = 256;
@@ -256,7 +262,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     ctx->last_kernel = kernel;
     ctx->last_tp = tp;
     const bool tensor = kernel == FIU_KERNEL_TENSOR;
-    const long long units = tensor ? res->t3_total : w.n_prefixes;
+    const long long units = tensor ? res->t3->total : w.n_prefixes;
     int* t_status = (int*)(ctx->ctl + 16);
     if (tensor) CK(cudaMemsetAsync(t_status, 0, sizeof(int), ctx->stream), "status reset");
     const unsigned keep = outputs + std::max(32u, outputs / 8);
@@ -283,7 +289,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
         CandSink sink{ctx->cand, count, overflow, (unsigned)cap, thr, ctx->timing ? ctx->evaluated : nullptr};
         if (ctx->timing) CK(cudaEventRecord(ctx->ev0, s), "event");
         if (tensor)
-            CK(launch_tensor3(w, res->t3_items, m, m1, sink, nullptr, res->single, res->pairs, t_status, s, ctx->sms),
+            CK(launch_tensor3(w, *res->t3, m, m1, sink, nullptr, res->single, res->pairs, t_status, s, ctx->sms),
                "tensor kernel launch");
         else
             CK(launch_kernel(kernel, tp, res, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
@@ -457,6 +463,14 @@ int fiu_probe_popc_rate(fiu_ctx* ctx, double* rate) {
     return FIU_OK;
 }
 
+int fiu_probe_lg2_error(fiu_ctx* ctx, unsigned max_c, double* max_abs_err) {
+    if (!ctx || !max_abs_err) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(probe_lg2_error(max_c, max_abs_err, ctx->stream), "lg2 probe");
+    return FIU_OK;
+}
+
 int fiu_dataset_upload(fiu_ctx* ctx, const fiu_dataset* h, fiu_resident** out) {
     if (!ctx || !out) return FIU_ERR_INVALID;
     Scope scope(ctx);
@@ -515,7 +529,10 @@ void fiu_dataset_free(fiu_ctx* ctx, fiu_resident* r) {
     cudaFree(r->ftab);
     cudaFree(r->single);
     cudaFree(r->pairs);
-    cudaFree(r->t3_items);
+    if (r->t3) {
+        tensor3_release(*r->t3);
+        delete r->t3;
+    }
     delete r;
 }
 
@@ -706,7 +723,7 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
     if (e == cudaSuccess && kernel == FIU_KERNEL_TENSOR) {
         e = cudaMemsetAsync(ctx->ctl + 16, 0, sizeof(int), s);
         if (e == cudaSuccess)
-            e = launch_tensor3(w, res->t3_items, 0, res->t3_total, sink, d, res->single, res->pairs, (int*)(ctx->ctl + 16),
+            e = launch_tensor3(w, *res->t3, 0, res->t3->total, sink, d, res->single, res->pairs, (int*)(ctx->ctl + 16),
                                s, ctx->sms);
     } else if (e == cudaSuccess) {
         e = launch_kernel(kernel, tp, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);

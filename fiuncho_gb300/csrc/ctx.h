@@ -52,8 +52,7 @@ struct fiu_resident {
     int device = 0;
     uint32_t* single = nullptr;  // single-SNP cores (elided kernels)
     uint4* pairs = nullptr;      // pair cores (elided order-3 kernel)
-    long long* t3_items = nullptr;  // work-item prefix sums of the tensor order-3 kernel
-    long long t3_total = 0;
+    fiu::T3Plan* t3 = nullptr;  // operand planes and work items of the tensor order-3 kernel
 };
 
 namespace fiu {

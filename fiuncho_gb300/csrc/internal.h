@@ -1,6 +1,8 @@
 // Host-side declarations shared by the library's translation units.
 #pragma once
 
+#include <cuda.h>
+
 #include <vector>
 
 #include "common.cuh"
@@ -103,11 +105,28 @@ cudaError_t launch_elided(bool hs, int tp, const ScanWork& w, long long m0, long
                           uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms);
 
 // tensor3.cu -- order-3 core cells on tcgen05 (one-hot data, whole data set, one worker).
-constexpr int kT3ItemCombos = 2048;  // combinations per work item, about (32 x 128 / 2)
-long long tensor3_items(int n, std::vector<long long>& item_begin);
-cudaError_t launch_tensor3(const ScanWork& w, const long long* item_begin, long long g0, long long g1,
-                           const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
-                           int* status, cudaStream_t s, int sms);
+constexpr int kT3ItemCombos = 1536;  // combinations per work item, about (32 x 96 / 2)
+// Device state of the tensor kernel for one data set: the e4m3 operand planes
+// (row 2*snp+g = "genotype of snp == g" per sample, cases then controls, each
+// class padded to a multiple of 128 samples), their TMA descriptors and the
+// work-item prefix sums.
+struct T3Plan {
+    uint8_t* planes = nullptr;
+    int pitch = 0;        // bytes per plane row
+    int k_cases = 0;      // padded case samples (= byte offset of the control region)
+    long long* item_begin = nullptr;
+    long long total = 0;  // work items
+    CUtensorMap map_l;    // box 128 B x 192 rows, 128-byte swizzle (l operand)
+    CUtensorMap map_j;    // box 128 B x 64 rows, 128-byte swizzle (j rows of the (i,j) operand)
+    CUtensorMap map_i;    // box 128 B x 2 rows, no swizzle (i rows)
+};
+cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s);
+void tensor3_release(T3Plan& plan);
+cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
+                           uint32_t* dump, const uint32_t* single, const uint4* pairs, int* status, cudaStream_t s,
+                           int sms);
+// Largest absolute error of the kernel's single-precision log2 over all its inputs (counts <= max_c).
+cudaError_t probe_lg2_error(unsigned max_c, double* max_abs_err, cudaStream_t s);
 
 // layout.cu -- device layouts of a data set.
 cudaError_t launch_transpose(const uint64_t* ref, uint64_t* tr, int snps, int rows, cudaStream_t s);

@@ -3,68 +3,146 @@
 // For one-hot data the 8 core cells of a combination (i, j, l) -- genotypes
 // x, y, z in {0, 1} -- are dot products over the samples of one class:
 //     core[x][y][z] = sum_s a_ix(s) a_jy(s) a_lz(s),
-// where a_gx(s) is bit "genotype of SNP g == x" of sample s.  A work item is
-// (i, 32 consecutive j, 128 consecutive l); it is one GEMM per class
-//     D[(j,x,y), (l,z)] = sum_s A[(j,x,y), s] B[(l,z), s],
-// with A = a_ix & a_jy (128 rows) and B = a_lz (256 rows) expanded from bits
-// to e4m3 0/1 (0x38 = 1.0) in shared memory, in the canonical K-major
-// no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix), and
-// accumulated exactly in FP32 in tensor memory: cases in columns 0-255,
-// controls in columns 256-511 (M = 128, N = 256, K = 32 per instruction).
-// Two shared-memory stages of 128 samples pipeline the bit expansion of step
-// s+1 against the MMAs of step s (one mbarrier per stage, committed by the
-// issuing thread).  The epilogue reads the accumulators with tcgen05.ld,
-// transposes each quad of rows (x, y) through shared memory so that one
-// thread sees the 8 cells of a combination, and derives the full 27-cell
-// table exactly with the pair/single cores (as the reduced-work CUDA-core
-// kernel does), then the fixed-point MI and the top-N filter.
+// where a_gx(s) is 1 when sample s has genotype x at SNP g.  A work item is
+// (i, 32 consecutive j, 96 consecutive l); per class it is one GEMM
+//     D[(j,x,y), (l,z)] = sum_s A[(j,x,y), s] B[(l,z), s]    (M 128, N 192),
+// accumulated exactly in FP32 in tensor memory.
+//
+// Operands.  Each data set is expanded once into e4m3 operand planes in HBM:
+// row 2*snp+g holds 0x38 (1.0) where the sample has genotype g, else 0; cases
+// then controls, each class padded to a multiple of 128 samples.  B rows are
+// plane rows 2l+z, loaded by TMA with 128-byte swizzle straight into the
+// layout tcgen05 reads (K-major, SWIZZLE_128B descriptors).  A rows are the
+// bytewise AND of the i and j plane rows (0x38 & 0x38 = 0x38), built by four
+// producer warps from TMA-staged j rows into the same swizzled layout.
+//
+// Warp roles (448 threads, one CTA per SM): warp 0 issues the TMA copies,
+// warp 1 issues tcgen05.mma (kind::f8f6f4, K 32 per instruction, 4 per
+// 128-sample stage) and commits, warps 2-5 build A, warps 6-13 run the
+// epilogue.  Four shared-memory stages are handed over with mbarriers.
+// Tensor memory (512 columns): case accumulators in columns 0-191, control
+// accumulators in 192-383, and a 16-bit copy of the case counts in 384-479:
+// as soon as an item's case GEMM is done the epilogue packs its counts there
+// and frees columns 0-191, so the next item's case GEMM overlaps the current
+// item's epilogue.
+//
+// Epilogue.  Each thread reads the accumulators of one row (j, x, y); a
+// swizzled shared-memory transpose gives each thread the 16 core counts of one
+// combination.  The full 27-cell tables are derived exactly from the pair and
+// single cores (inclusion-exclusion, as the CUDA-core reduced-work kernel
+// does).  A single-precision estimate of the fixed-point MI key (lg2.approx)
+// with a proven error bound rejects the combinations that cannot reach the
+// current threshold; the others get the exact 64-bit fixed-point key from the
+// integer c*ln(c) table, so the kept set is exactly the one of the exact key.
 //
 // Reference semantics: GenotypeTable::combine_and_popcnt for order 3
-// (src/base/gt_popcnt.cpp:4-35) over the combinations ThreadedSearch visits
-// (include/fiuncho/ThreadedSearch.h:157-180) with one worker.
+// (src/base/gt_popcnt.cpp:4-35) and MutualInformation::compute
+// (src/base/mutual_information.cpp:8-39) over the combinations ThreadedSearch
+// visits (include/fiuncho/ThreadedSearch.h:157-180) with one worker.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
 #include "elided_prefix.cuh"
 
 namespace fiu {
 
-constexpr int kT3Threads = 256;
-constexpr int kT3J = 32, kT3L = 128;          // SNPs per tile
-constexpr int kT3M = 4 * kT3J, kT3N = 2 * kT3L;  // 128 x 256 GEMM tile
-constexpr int kT3KB = 128;                    // samples (= e4m3 bytes) per stage
-constexpr int kT3StageA = kT3M * kT3KB, kT3StageB = kT3N * kT3KB;
-constexpr int kT3Stage = kT3StageA + kT3StageB;  // 48 KB
-constexpr int kT3Lut = 256 * 8;
-constexpr int kT3Ebuf = 8 * 1024 * 4;            // per-warp transpose buffers
-constexpr size_t kT3Smem = 2 * kT3Stage + kT3Lut + kT3Ebuf;  // 130 KB: one CTA per SM
-constexpr unsigned kT3Spin = 1u << 24;           // bounded mbarrier waits
+constexpr int kT3J = 32, kT3L = 96;              // SNPs per tile
+constexpr int kT3M = 4 * kT3J, kT3N = 2 * kT3L;  // 128 x 192 GEMM tile
+constexpr int kT3KB = 128;                       // samples (= e4m3 bytes) per stage
+constexpr int kT3Stages = 4;
+constexpr int kT3SB = kT3N * kT3KB;              // 24 KB  l rows
+constexpr int kT3SA = kT3M * kT3KB;              // 16 KB  (i,j) rows
+constexpr int kT3SJ = 2 * kT3J * kT3KB;          //  8 KB  staged j rows
+constexpr int kT3Stage = kT3SB + kT3SA + kT3SJ;  // 48 KB, a multiple of 1 KB
+constexpr int kT3SI = 2 * kT3KB;                 // i rows of a stage (no swizzle)
+constexpr int kT3EpiWarps = 8, kT3BuildWarps = 4;
+constexpr int kT3Threads = 32 * (2 + kT3BuildWarps + kT3EpiWarps);  // 448
+constexpr int kT3Ebuf = 4096;                    // per epilogue warp: 8 j x 8 l x 4 (x,y) x 16 B
+constexpr size_t kT3Smem = 1024 + (size_t)kT3Stages * (kT3Stage + kT3SI) + (size_t)kT3EpiWarps * kT3Ebuf;
+constexpr int kT3ColCtrl = kT3N, kT3ColStash = 2 * kT3N;  // tensor-memory column bases
+constexpr unsigned long long kT3LimitNs = 2000000000ull;   // 2 s per wait
+constexpr uint32_t kT3Idesc = (1u << 4) | ((uint32_t)(kT3N >> 3) << 17) | ((uint32_t)(kT3M >> 4) << 24);
+
+static_assert(kT3Smem <= 227 * 1024 - 256, "tensor kernel shared memory");
+static_assert(kT3ColStash + kT3N / 2 <= 512, "tensor memory columns");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// tcgen05 shared-memory descriptor: start >> 4, leading (K-direction core
-// matrix) byte offset >> 4 at bit 16, stride (8-row group) byte offset >> 4 at
-// bit 32, descriptor version 1 at bit 46, no swizzle.
-__device__ __forceinline__ uint64_t t3_desc(uint32_t saddr) {
-    return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((8 * 128) >> 4) << 32) |
-           ((uint64_t)1 << 46);
+__device__ __forceinline__ unsigned long long t3_now() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
-// Instruction descriptor, kind::f8f6f4: D = F32 (bit 4), A = B = E4M3 (0),
-// both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-constexpr uint32_t kT3Idesc = (1u << 4) | ((uint32_t)(kT3N >> 3) << 17) | ((uint32_t)(kT3M >> 4) << 24);
+__device__ __forceinline__ bool t3_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p;}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (unsigned it = 0; it < kT3Spin; ++it) {
-        uint32_t ok;
-        asm volatile("{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p;}"
-                     : "=r"(ok)
-                     : "r"(bar), "r"(parity)
-                     : "memory");
-        if (ok) return true;
+// Bounded wait on an mbarrier phase.  A wait that runs past the limit raises
+// the CTA's abort flag; every other waiter then gives up at once.
+__device__ __forceinline__ bool t3_wait(uint32_t bar, uint32_t parity, volatile int* abort) {
+    const unsigned long long t0 = t3_now();
+    for (;;) {
+        if (t3_try(bar, parity)) return true;
+        if (*abort) return false;
+        if (t3_now() - t0 > kT3LimitNs) {
+            *abort = 1;
+            return false;
+        }
     }
-    return false;
+}
+
+// Bounded wait that ignores the abort flag (draining copies and MMAs in flight).
+__device__ __forceinline__ bool t3_drain(uint32_t bar, uint32_t parity) {
+    const unsigned long long t0 = t3_now();
+    for (;;) {
+        if (t3_try(bar, parity)) return true;
+        if (t3_now() - t0 > kT3LimitNs) return false;
+    }
+}
+
+__device__ __forceinline__ void t3_tma(uint32_t dst, const CUtensorMap* m, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(dst),
+        "l"((uint64_t)m), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// tcgen05 shared-memory descriptor, K-major with 128-byte swizzle: start >> 4,
+// leading byte offset 16 (unused for swizzled K-major), stride byte offset
+// 1024 (8 rows of 128 bytes), version 1 at bit 46, layout SWIZZLE_128B (2) at
+// bits 61-63.  Within the 128-byte swizzle atom the K offset is added to the
+// start address (tiles are 1024-byte aligned).
+__device__ __forceinline__ uint64_t t3_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ float u2f(uint32_t v) {  // exact for v < 2^23
+    return __uint_as_float(0x4B000000u | v) - 8388608.0f;
+}
+
+__device__ __forceinline__ uint32_t f2u(float f) {  // f an exact integer in [0, 2^23)
+    return __float_as_uint(f + 8388608.0f) & 0x7FFFFFu;
+}
+
+__device__ __forceinline__ float t3_lg2(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
 
 // Work items of one i: J-tile a starts at j0 = i+1+32a and has
-// ceil((n-1-j0)/128) L-tiles starting at l0 = j0+1+128b.
+// ceil((n-1-j0)/96) L-tiles starting at l0 = j0+1+96b.
 __device__ __forceinline__ void t3_decode(const long long* __restrict__ item_begin, int n, long long g, int& i,
                                           int& j0, int& l0) {
     int lo = 0, hi = n - 1;
@@ -87,210 +165,451 @@ __device__ __forceinline__ void t3_decode(const long long* __restrict__ item_beg
     }
 }
 
-__global__ void __launch_bounds__(kT3Threads, 1)
-    tensor3_kernel(ScanWork w, const long long* __restrict__ item_begin, long long g0, long long g1, CandSink sink,
-                   uint32_t* dump, const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
-                   int* status) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
-    __shared__ uint32_t tmem_base;
-    const DevData& d = w.d;
-    const int n = d.snps, cw = d.cw, tw = d.tw;
-    const size_t per_snp = 3 * (size_t)(cw + tw);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    uint64_t* lut = reinterpret_cast<uint64_t*>(smem + 2 * kT3Stage);
-    uint32_t* ebuf = reinterpret_cast<uint32_t*>(smem + 2 * kT3Stage + kT3Lut) + warp * 1024;
-    for (int e = tid; e < 256; e += kT3Threads) {
-        uint64_t v = 0;
-        for (int b = 0; b < 8; ++b)
-            if ((e >> b) & 1) v |= 0x38ull << (8 * b);
-        lut[e] = v;
+// 16-byte chunk of the epilogue transpose buffer holding the 4 counts
+// (cases z0, z1, controls z0, z1) of row (jl, xy) and column group k; the XOR
+// makes both the row-wise writes and the combination-wise reads free of bank
+// conflicts (8 distinct chunk positions per quarter-warp).
+__device__ __forceinline__ int t3_chunk(int jl, int k, int xy) {
+    return (((jl * 8 + k) * 4) + xy) ^ (((k >> 1) & 3) | ((jl & 1) << 2));
+}
+
+// Float view of the packed 16-bit pair cores [class][x][y].
+__device__ __forceinline__ float pcf(const uint4& v, int k) {
+    const uint32_t w = (&v.x)[k >> 1];
+    return u2f((k & 1) ? (w >> 16) : (w & 0xffffu));
+}
+
+// Full 27-cell table of one class in single precision (every value an exact
+// integer), the derivation of expand3: core[(x*2+y)*2+z], pair cores of
+// (i,j), (i,l), (j,l), singles of i, j, l, class size.
+__device__ __forceinline__ void expand3f(const float* core, const uint4& pij, const uint4& pil, const uint4& pjl,
+                                         const float* si, const float* sj, const float* sl, float ncls, int cls,
+                                         float* t) {
+    const int o = 4 * cls;
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) {
+            t[(x * 3 + y) * 3 + 0] = core[(x * 2 + y) * 2 + 0];
+            t[(x * 3 + y) * 3 + 1] = core[(x * 2 + y) * 2 + 1];
+            t[(x * 3 + y) * 3 + 2] = pcf(pij, o + x * 2 + y);
+        }
+#pragma unroll
+    for (int x = 0; x < 2; ++x) {
+#pragma unroll
+        for (int z = 0; z < 2; ++z) t[(x * 3 + 2) * 3 + z] = pcf(pil, o + x * 2 + z);
+        t[(x * 3 + 2) * 3 + 2] = si[x];
     }
+#pragma unroll
+    for (int y = 0; y < 2; ++y) {
+#pragma unroll
+        for (int z = 0; z < 2; ++z) t[(2 * 3 + y) * 3 + z] = pcf(pjl, o + y * 2 + z);
+        t[(2 * 3 + y) * 3 + 2] = sj[y];
+    }
+    t[24] = sl[0];
+    t[25] = sl[1];
+    t[26] = ncls;
+#pragma unroll
+    for (int xy = 0; xy < 9; ++xy) t[xy * 3 + 2] -= t[xy * 3 + 0] + t[xy * 3 + 1];
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int z = 0; z < 3; ++z) t[(x * 3 + 2) * 3 + z] -= t[(x * 3 + 0) * 3 + z] + t[(x * 3 + 1) * 3 + z];
+#pragma unroll
+    for (int yz = 0; yz < 9; ++yz) t[18 + yz] -= t[yz] + t[9 + yz];
+}
+
+struct T3Maps {
+    CUtensorMap l, j, i;
+};
+
+__global__ void __launch_bounds__(kT3Threads, 1)
+    tensor3_kernel(const __grid_constant__ T3Maps maps, ScanWork w, const long long* __restrict__ item_begin,
+                   long long g0, long long g1, int k_cases, CandSink sink, float thr_f, uint32_t* dump,
+                   const uint32_t* __restrict__ single, const uint4* __restrict__ pairs, int* status) {
+    extern __shared__ uint8_t smraw[];
+    __shared__ __align__(8) uint64_t full_t[kT3Stages], full_a[kT3Stages], empty[kT3Stages];
+    __shared__ __align__(8) uint64_t case_full, case_empty, ctrl_full, ctrl_empty, done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+    uint8_t* si_base = sm + kT3Stages * kT3Stage;
+    uint32_t* ebuf_all = reinterpret_cast<uint32_t*>(si_base + kT3Stages * kT3SI);
+    volatile int* abort = &abort_flag;
+    const DevData& d = w.d;
+    const int n = d.snps;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ks_c = k_cases / kT3KB;     // 128-sample steps of the case class
+    const int ks_t = (d.tw + 1) / 2;      // ... of the control class
+    const int ksteps = ks_c + ks_t;
+
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(512));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[0])), "r"(1));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[1])), "r"(1));
+        for (int s = 0; s < kT3Stages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_t[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_a[s])), "r"(kT3BuildWarps));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&case_full)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&case_empty)), "r"(kT3EpiWarps));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&ctrl_full)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&ctrl_empty)), "r"(kT3EpiWarps));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
         asm volatile("fence.mbarrier_init.release.cluster;");
+        abort_flag = 0;
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
-    const int ks_c = (cw + 1) / 2, ks_t = (tw + 1) / 2;  // K-steps (2 words = 128 samples) per class
-    unsigned step = 0;                                  // K-steps issued by this CTA
     bool ok = true;
-    const uint32_t n_cls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
 
-    for (long long g = g0 + blockIdx.x; g < g1; g += gridDim.x) {
-        int i, j0, l0;
-        t3_decode(item_begin, n, g, i, j0, l0);
-        // ---- GEMMs: cases then controls
-        for (int ks = 0; ks < ks_c + ks_t; ++ks, ++step) {
-            const int cls = ks >= ks_c;
-            const int W = cls ? tw : cw;
-            const int wb = 2 * (cls ? ks - ks_c : ks);
-            const size_t roff = cls ? 3 * (size_t)cw : 0;
-            const int s = step & 1;
-            uint8_t* sA = smem + s * kT3Stage;
-            uint8_t* sB = sA + kT3StageA;
-            if (step >= 2 && !mbar_wait(smem_u32(&mbar[s]), ((step >> 1) - 1) & 1)) ok = false;
-            // expand: task t -> (row, word half); 8 consecutive tasks fill one 128-byte core-matrix column
-            for (int t = tid; t < (kT3M + kT3N) * 2; t += kT3Threads) {
-                const int isB = t >= kT3M * 2;
-                const int tt = isB ? t - kT3M * 2 : t;
-                const int r = (tt & 7) + 8 * (tt >> 4), h = (tt >> 3) & 1;
-                const int word = wb + h;
-                uint64_t bits = 0;
-                if (word < W) {
-                    if (isB) {
-                        const int l = l0 + (r >> 1), z = r & 1;
-                        if (l < n) bits = __ldg(d.ref + (size_t)l * per_snp + roff + (size_t)z * W + word);
-                    } else {
-                        const int j = j0 + (r >> 2), x = (r >> 1) & 1, y = r & 1;
-                        if (j < n)
-                            bits = __ldg(d.ref + (size_t)i * per_snp + roff + (size_t)x * W + word) &
-                                   __ldg(d.ref + (size_t)j * per_snp + roff + (size_t)y * W + word);
+    if (warp == 0) {
+        // ---------------------------------------------------------------- TMA producer
+        if (lane == 0) {
+            long long step = 0;
+            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+                int i, j0, l0;
+                t3_decode(item_begin, n, g, i, j0, l0);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const int s = (int)(step % kT3Stages);
+                    const long long u = step / kT3Stages;
+                    if (u > 0 && !t3_wait(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
+                        ok = false;
+                        break;
                     }
-                }
-                uint8_t* base = (isB ? sB : sA) + (r >> 3) * 1024 + (r & 7) * 16 + h * 512;
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    uint4 v;
-                    const uint64_t lo = lut[(bits >> (16 * c)) & 0xff], hi = lut[(bits >> (16 * c + 8)) & 0xff];
-                    v.x = (uint32_t)lo;
-                    v.y = (uint32_t)(lo >> 32);
-                    v.z = (uint32_t)hi;
-                    v.w = (uint32_t)(hi >> 32);
-                    *reinterpret_cast<uint4*>(base + c * 128) = v;
+                    const int k0 = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
+                    uint8_t* st = sm + s * kT3Stage;
+                    const uint32_t bar = smem_u32(&full_t[s]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                                 "r"((uint32_t)(kT3SB + kT3SJ + kT3SI))
+                                 : "memory");
+                    t3_tma(smem_u32(st), &maps.l, k0, 2 * l0, bar);
+                    t3_tma(smem_u32(st + kT3SB + kT3SA), &maps.j, k0, 2 * j0, bar);
+                    t3_tma(smem_u32(si_base + s * kT3SI), &maps.i, k0, 2 * i, bar);
+                    ++step;
                 }
             }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncthreads();
-            if (tid == 0) {
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t dcol = tmem + (cls ? 256u : 0u);
-                const int first = cls ? ks == ks_c : ks == 0;
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                    const uint64_t ad = t3_desc(smem_u32(sA) + kk * 256), bd = t3_desc(smem_u32(sB) + kk * 256);
-                    const uint32_t acc = (first && kk == 0) ? 0u : 1u;
-                    asm volatile("{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
-                                 "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
-                                 "l"(ad), "l"(bd), "r"(kT3Idesc), "r"(acc));
-                }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                    smem_u32(&mbar[s])));
+            // no copy may be in flight when the CTA exits: wait for the last use of every stage
+            for (int s = 0; s < kT3Stages; ++s) {
+                if (step <= s) continue;
+                const long long last = s + ((step - 1 - s) / kT3Stages) * kT3Stages;
+                if (!t3_drain(smem_u32(&full_t[s]), (uint32_t)((last / kT3Stages) & 1))) ok = false;
             }
         }
-        // ---- all MMAs of the item done (commits track every earlier MMA of the thread)
-        if (!mbar_wait(smem_u32(&mbar[(step - 1) & 1]), ((step - 1) >> 1) & 1)) ok = false;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        // ---- epilogue: warp w reads TMEM lanes 32(w%4).. (rows), l columns [64(w/4), 64(w/4)+64)
-        const int q = warp & 3, hh = warp >> 2;
-        const int jl = lane >> 2, xy = lane & 3;
-        for (int cc = 0; cc < 8; ++cc) {
-            const uint32_t col = (uint32_t)(128 * hh + 16 * cc);
-            uint32_t vc[16], vt[16];
-            const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + col;
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                : "=r"(vc[0]), "=r"(vc[1]), "=r"(vc[2]), "=r"(vc[3]), "=r"(vc[4]), "=r"(vc[5]), "=r"(vc[6]),
-                  "=r"(vc[7]), "=r"(vc[8]), "=r"(vc[9]), "=r"(vc[10]), "=r"(vc[11]), "=r"(vc[12]), "=r"(vc[13]),
-                  "=r"(vc[14]), "=r"(vc[15])
-                : "r"(ta));
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                : "=r"(vt[0]), "=r"(vt[1]), "=r"(vt[2]), "=r"(vt[3]), "=r"(vt[4]), "=r"(vt[5]), "=r"(vt[6]),
-                  "=r"(vt[7]), "=r"(vt[8]), "=r"(vt[9]), "=r"(vt[10]), "=r"(vt[11]), "=r"(vt[12]), "=r"(vt[13]),
-                  "=r"(vt[14]), "=r"(vt[15])
-                : "r"(ta + 256u));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            // transpose: ebuf[((jl*8 + k)*2 + cls)*8 + xy*2 + z]  (FP32 accumulators hold exact integers)
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-#pragma unroll
-                for (int z = 0; z < 2; ++z) {
-                    ebuf[((jl * 8 + k) * 2 + 0) * 8 + xy * 2 + z] = (uint32_t)__uint_as_float(vc[2 * k + z]);
-                    ebuf[((jl * 8 + k) * 2 + 1) * 8 + xy * 2 + z] = (uint32_t)__uint_as_float(vt[2 * k + z]);
-                }
-            __syncwarp();
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const int ci = lane + 32 * u, cj = ci >> 3, k = ci & 7;
-                const int j = j0 + 8 * q + cj, l = l0 + 64 * hh + 8 * cc + k;
-                const bool valid = j < n && l < n && l > j;
-                long long key = w.base_key;
-                if (valid) {
-                    uint32_t core[2][8];
-#pragma unroll
-                    for (int cls = 0; cls < 2; ++cls) {
-                        const uint4 a = *reinterpret_cast<const uint4*>(ebuf + ((cj * 8 + k) * 2 + cls) * 8);
-                        const uint4 b = *reinterpret_cast<const uint4*>(ebuf + ((cj * 8 + k) * 2 + cls) * 8 + 4);
-                        core[cls][0] = a.x; core[cls][1] = a.y; core[cls][2] = a.z; core[cls][3] = a.w;
-                        core[cls][4] = b.x; core[cls][5] = b.y; core[cls][6] = b.z; core[cls][7] = b.w;
+    } else if (warp == 1) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            long long step = 0, item = 0;
+            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+                for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                    const int cls = ks >= ks_c;
+                    if (item > 0 && (ks == 0 || ks == ks_c)) {  // accumulator columns free again?
+                        if (!t3_wait(smem_u32(cls ? &ctrl_empty : &case_empty), (uint32_t)((item - 1) & 1), abort)) {
+                            ok = false;
+                            break;
+                        }
                     }
-                    const uint4 pij = __ldg(pairs + pair_index(i, j, n)), pil = __ldg(pairs + pair_index(i, l, n)),
-                                pjl = __ldg(pairs + pair_index(j, l, n));
-                    uint32_t t[2][27];
+                    const int s = (int)(step % kT3Stages);
+                    if (!t3_wait(smem_u32(&full_a[s]), (uint32_t)((step / kT3Stages) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t sa = smem_u32(sm + s * kT3Stage + kT3SB), sb = smem_u32(sm + s * kT3Stage);
+                    const uint32_t dcol = tmem + (cls ? (uint32_t)kT3ColCtrl : 0u);
+                    const bool first = ks == 0 || ks == ks_c;
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint64_t ad = t3_desc(sa + 32 * kk), bd = t3_desc(sb + 32 * kk);
+                        const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+                        asm volatile(
+                            "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
+                            "l"(ad), "l"(bd), "r"(kT3Idesc), "r"(acc));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                        smem_u32(&empty[s])));
+                    if (ks == ks_c - 1 || ks == ksteps - 1)
+                        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                            smem_u32(ks == ks_c - 1 ? &case_full : &ctrl_full)));
+                }
+            }
+            // every MMA of this thread complete before the tensor memory is released
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&done)));
+            if (!t3_drain(smem_u32(&done), 0)) ok = false;
+        }
+    } else if (warp < 2 + kT3BuildWarps) {
+        // ---------------------------------------------------------------- A builders
+        const int t = tid - 64;  // 0..127
+        const int c = t & 7;     // 16-byte chunk; 8 consecutive threads cover one 128-byte row
+        long long step = 0;
+        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+            for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                const int s = (int)(step % kT3Stages);
+                if (!t3_wait(smem_u32(&full_t[s]), (uint32_t)((step / kT3Stages) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t* st = sm + s * kT3Stage;
+                const uint8_t* sJ = st + kT3SB + kT3SA;
+                const uint8_t* sI = si_base + s * kT3SI;
+                uint8_t* sA = st + kT3SB;
+                const uint4 i0 = *reinterpret_cast<const uint4*>(sI + c * 16);
+                const uint4 i1 = *reinterpret_cast<const uint4*>(sI + kT3KB + c * 16);
+#pragma unroll
+                for (int r = t >> 3; r < 2 * kT3J; r += 16) {  // j row r = (jj, y)
+                    const uint4 jv = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((c ^ (r & 7)) << 4));
+                    const int m0 = 4 * (r >> 1) + (r & 1), m1 = m0 + 2;  // A rows (jj, x, y), x = 0, 1
+                    uint4 v;
+                    v.x = jv.x & i0.x;
+                    v.y = jv.y & i0.y;
+                    v.z = jv.z & i0.z;
+                    v.w = jv.w & i0.w;
+                    *reinterpret_cast<uint4*>(sA + m0 * 128 + ((c ^ (m0 & 7)) << 4)) = v;
+                    v.x = jv.x & i1.x;
+                    v.y = jv.y & i1.y;
+                    v.z = jv.z & i1.z;
+                    v.w = jv.w & i1.w;
+                    *reinterpret_cast<uint4*>(sA + m1 * 128 + ((c ^ (m1 & 7)) << 4)) = v;
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_a[s])) : "memory");
+            }
+        }
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        const int e = warp - (2 + kT3BuildWarps);  // 0..7
+        const int q = warp & 3;                    // tensor-memory lane quarter this warp may access
+        const int hh = e >> 2;                     // column half: l offsets [48 hh, 48 hh + 48)
+        uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+        const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
+        const float ncf[2] = {(float)d.n_cases, (float)d.n_ctrls};
+        const float tiny = 9.5367431640625e-07f;  // 2^-20: x*lg2(x + tiny) = 0 at x = 0
+        // row (writer) view: jl = lane/4, xy = lane%4; combination (reader) view: jl = lane/4, kp = lane%4
+        const int jl = lane >> 2, xy = lane & 3, kp = lane & 3;
+        long long item = 0;
+        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+            int i, j0, l0;
+            t3_decode(item_begin, n, g, i, j0, l0);
+            // ---- phase 1: case counts -> 16-bit stash, case columns free for the next item
+            if (!t3_wait(smem_u32(&case_full), (uint32_t)(item & 1), abort)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+            for (int cc = 0; cc < 6; ++cc) {
+                const uint32_t col = (uint32_t)(96 * hh + 16 * cc);
+                uint32_t v[16], p[8];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(lane_base + col));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    p[k] = f2u(__uint_as_float(v[2 * k])) | (f2u(__uint_as_float(v[2 * k + 1])) << 16);
+                asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(
+                                 lane_base + (uint32_t)kT3ColStash + (uint32_t)(48 * hh + 8 * cc)),
+                             "r"(p[0]), "r"(p[1]), "r"(p[2]), "r"(p[3]), "r"(p[4]), "r"(p[5]), "r"(p[6]), "r"(p[7]));
+            }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&case_empty)) : "memory");
+            // ---- per-item constants of this thread's j
+            const int j = j0 + 8 * q + jl;
+            const bool j_ok = j < n;
+            uint4 pij = make_uint4(0, 0, 0, 0);
+            float si[2][2], sj[2][2];
+            {
+                const uint4 a = __ldg(reinterpret_cast<const uint4*>(single) + i);
+                uint4 b = make_uint4(0, 0, 0, 0);
+                if (j_ok) {
+                    b = __ldg(reinterpret_cast<const uint4*>(single) + j);
+                    pij = __ldg(pairs + pair_index(i, j, n));
+                }
+                si[0][0] = u2f(a.x);
+                si[0][1] = u2f(a.y);
+                si[1][0] = u2f(a.z);
+                si[1][1] = u2f(a.w);
+                sj[0][0] = u2f(b.x);
+                sj[0][1] = u2f(b.y);
+                sj[1][0] = u2f(b.z);
+                sj[1][1] = u2f(b.w);
+            }
+            // ---- phase 2: control counts + stash -> transpose -> tables -> keys
+            if (!t3_wait(smem_u32(&ctrl_full), (uint32_t)(item & 1), abort)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+            for (int cc = 0; cc < 6; ++cc) {
+                {
+                    const uint32_t col = (uint32_t)(96 * hh + 16 * cc);
+                    uint32_t vt[16], su[8];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
+                        "15}, [%16];"
+                        : "=r"(vt[0]), "=r"(vt[1]), "=r"(vt[2]), "=r"(vt[3]), "=r"(vt[4]), "=r"(vt[5]), "=r"(vt[6]),
+                          "=r"(vt[7]), "=r"(vt[8]), "=r"(vt[9]), "=r"(vt[10]), "=r"(vt[11]), "=r"(vt[12]),
+                          "=r"(vt[13]), "=r"(vt[14]), "=r"(vt[15])
+                        : "r"(lane_base + (uint32_t)kT3ColCtrl + col));
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                        : "=r"(su[0]), "=r"(su[1]), "=r"(su[2]), "=r"(su[3]), "=r"(su[4]), "=r"(su[5]), "=r"(su[6]),
+                          "=r"(su[7])
+                        : "r"(lane_base + (uint32_t)kT3ColStash + (uint32_t)(48 * hh + 8 * cc)));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (cc == 5) {  // last read of this item's accumulators: control columns free
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ctrl_empty))
+                                         : "memory");
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        uint4 c4;
+                        c4.x = su[k] & 0xffffu;
+                        c4.y = su[k] >> 16;
+                        c4.z = f2u(__uint_as_float(vt[2 * k]));
+                        c4.w = f2u(__uint_as_float(vt[2 * k + 1]));
+                        *reinterpret_cast<uint4*>(ebuf + 4 * t3_chunk(jl, k, xy)) = c4;
+                    }
+                }
+                __syncwarp();
+#pragma unroll 1
+                for (int b = 0; b < 2; ++b) {
+                    const int k = 2 * kp + b;
+                    const int l = l0 + 48 * hh + 8 * cc + k;
+                    const bool valid = j_ok && l < n && l > j;
+                    float core[2][8];
+#pragma unroll
+                    for (int x4 = 0; x4 < 4; ++x4) {
+                        const uint4 c4 = *reinterpret_cast<const uint4*>(ebuf + 4 * t3_chunk(jl, k, x4));
+                        core[0][2 * x4] = u2f(c4.x);
+                        core[0][2 * x4 + 1] = u2f(c4.y);
+                        core[1][2 * x4] = u2f(c4.z);
+                        core[1][2 * x4 + 1] = u2f(c4.w);
+                    }
+                    uint4 pil = make_uint4(0, 0, 0, 0), pjl = pil, sl4 = pil;
+                    if (valid) {
+                        pil = __ldg(pairs + pair_index(i, l, n));
+                        pjl = __ldg(pairs + pair_index(j, l, n));
+                        sl4 = __ldg(reinterpret_cast<const uint4*>(single) + l);
+                    }
+                    const float sl[2][2] = {{u2f(sl4.x), u2f(sl4.y)}, {u2f(sl4.z), u2f(sl4.w)}};
+                    float t[2][27];
 #pragma unroll
                     for (int cls = 0; cls < 2; ++cls)
-                        expand3(core[cls], pij, pil, pjl, __ldg(single + i * 4 + cls * 2),
-                                __ldg(single + i * 4 + cls * 2 + 1), __ldg(single + j * 4 + cls * 2),
-                                __ldg(single + j * 4 + cls * 2 + 1), __ldg(single + l * 4 + cls * 2),
-                                __ldg(single + l * 4 + cls * 2 + 1), n_cls[cls], cls, t[cls]);
+                        expand3f(core[cls], pij, pil, pjl, si[cls], sj[cls], sl[cls], ncf[cls], cls, t[cls]);
+                    // single-precision estimate of sum over cells of T[a] + T[b] - T[a+b], in units of ln2 * 2^32
+                    float kf = 0.f;
 #pragma unroll
                     for (int c = 0; c < 27; ++c) {
-                        const uint32_t a = min(t[0][c], n_cls[0]), b = min(t[1][c], n_cls[1]);
-                        key += __ldg(d.ftab + a) + __ldg(d.ftab + b) - __ldg(d.ftab + a + b);
+                        const float a = t[0][c], bb = t[1][c], s = a + bb;
+                        kf = fmaf(a, t3_lg2(a + tiny), kf);
+                        kf = fmaf(bb, t3_lg2(bb + tiny), kf);
+                        kf = fmaf(-s, t3_lg2(s + tiny), kf);
                     }
-                    if (dump) {
-                        uint32_t* o = dump + ((size_t)pair_index(i, j, n) * n + l) * 54;
+                    const bool cand = valid && (dump != nullptr || kf >= thr_f);
+                    long long key = w.base_key;
+                    bool pass = false;
+                    if (cand) {
 #pragma unroll
                         for (int c = 0; c < 27; ++c) {
-                            o[c] = t[0][c];
-                            o[27 + c] = t[1][c];
+                            const uint32_t a = min(f2u(fmaxf(t[0][c], 0.f)), ncls[0]);
+                            const uint32_t bb = min(f2u(fmaxf(t[1][c], 0.f)), ncls[1]);
+                            key += __ldg(d.ftab + a) + __ldg(d.ftab + bb) - __ldg(d.ftab + a + bb);
+                        }
+                        pass = key >= sink.thr;
+                        if (dump) {
+                            uint32_t* o = dump + ((size_t)pair_index(i, j, n) * n + l) * 54;
+#pragma unroll
+                            for (int c = 0; c < 27; ++c) {
+                                o[c] = f2u(t[0][c]);
+                                o[27 + c] = f2u(t[1][c]);
+                            }
+                        }
+                    }
+                    if (sink.evaluated) {
+                        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+                        if (lane == 0 && vmask) atomicAdd(sink.evaluated, (unsigned long long)__popc(vmask));
+                    }
+                    const unsigned mask = __ballot_sync(0xffffffffu, pass);
+                    if (mask) {
+                        const int leader = __ffs(mask) - 1;
+                        unsigned base = 0;
+                        if (lane == leader) base = atomicAdd(sink.count, (unsigned)__popc(mask));
+                        base = __shfl_sync(0xffffffffu, base, leader);
+                        if (pass) {
+                            const unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+                            if (idx < sink.cap) {
+                                const int cmb[3] = {i, j, l};
+                                sink.buf[idx] = Cand{key, pack_code(cmb, 3, w.bits)};
+                            } else {
+                                atomicOr(sink.overflow, 1u);
+                            }
                         }
                     }
                 }
-                const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-                if (sink.evaluated && lane == 0 && vmask) atomicAdd(sink.evaluated, (unsigned long long)__popc(vmask));
-                const bool pass = valid && key >= sink.thr;
-                const unsigned mask = __ballot_sync(0xffffffffu, pass);
-                if (mask) {
-                    const int leader = __ffs(mask) - 1;
-                    unsigned base = 0;
-                    if (lane == leader) base = atomicAdd(sink.count, (unsigned)__popc(mask));
-                    base = __shfl_sync(0xffffffffu, base, leader);
-                    if (pass) {
-                        const unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
-                        if (idx < sink.cap) {
-                            const int cmb[3] = {i, j, l};
-                            sink.buf[idx] = Cand{key, pack_code(cmb, 3, w.bits)};
-                        } else {
-                            atomicOr(sink.overflow, 1u);
-                        }
-                    }
-                }
+                __syncwarp();
             }
-            __syncwarp();
         }
-        // the next item's first MMA overwrites the accumulators: all reads done first
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
     }
-    if (!ok) atomicOr(status, 1);
+    if (!ok) *abort = 1;
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+    if (tid == 0 && abort_flag) atomicOr(status, 1);
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
+// Operand planes: one thread per 16 output bytes (16 samples of one row).
+__global__ void t3_planes_kernel(DevData d, uint8_t* planes, int pitch, int k_cases) {
+    const long long chunks = (long long)pitch / 16;
+    const long long total = 2ll * d.snps * chunks;
+    const size_t per_snp = 3 * (size_t)(d.cw + d.tw);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long row = e / chunks;
+        const int ch = (int)(e - row * chunks);
+        const int snp = (int)(row >> 1), g = (int)(row & 1);
+        const int o = 16 * ch;
+        const bool ctrl = o >= k_cases;
+        const int k = ctrl ? o - k_cases : o;
+        const int W = ctrl ? d.tw : d.cw;
+        const int word = k >> 6;
+        uint32_t bits = 0;
+        if (word < W)
+            bits = (uint32_t)(__ldg(d.ref + (size_t)snp * per_snp + (ctrl ? 3 * (size_t)d.cw : 0) + (size_t)g * W +
+                                    word) >>
+                              (k & 63)) &
+                   0xffffu;
+        uint4 v;
+        uint32_t* pv = &v.x;
+#pragma unroll
+        for (int qd = 0; qd < 4; ++qd) pv[qd] = (((bits >> (4 * qd)) & 0xfu) * 0x00204081u & 0x01010101u) * 0x38u;
+        *reinterpret_cast<uint4*>(planes + (size_t)row * pitch + o) = v;
+    }
+}
+
 // Items per i (host): prefix sums item_begin[0..n], item_begin[n] = total.
-long long tensor3_items(int n, std::vector<long long>& item_begin) {
+static long long t3_items(int n, std::vector<long long>& item_begin) {
     item_begin.assign((size_t)n + 1, 0);
     long long total = 0;
     for (int i = 0; i < n; ++i) {
@@ -301,9 +620,111 @@ long long tensor3_items(int n, std::vector<long long>& item_begin) {
     return total;
 }
 
-cudaError_t launch_tensor3(const ScanWork& w, const long long* item_begin, long long g0, long long g1,
-                           const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
-                           int* status, cudaStream_t s, int sms) {
+static PFN_cuTensorMapEncodeTiled_v12000 t3_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+static cudaError_t t3_map(CUtensorMap* m, uint8_t* base, int rows, int pitch, int box_rows, bool swizzle) {
+    auto enc = t3_encoder();
+    if (!enc) return cudaErrorNotSupported;
+    cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)pitch};
+    cuuint32_t box[2] = {(cuuint32_t)kT3KB, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
+    plan.k_cases = kT3KB * ((d.cw + 1) / 2);
+    plan.pitch = plan.k_cases + kT3KB * ((d.tw + 1) / 2);
+    std::vector<long long> ib;
+    plan.total = t3_items(d.snps, ib);
+    cudaError_t e = cudaMalloc((void**)&plan.item_begin, ib.size() * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMemcpy(plan.item_begin, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&plan.planes, (size_t)2 * d.snps * plan.pitch);
+    if (e != cudaSuccess) return e;
+    const long long total = 2ll * d.snps * (plan.pitch / 16);
+    const int grid = (int)std::min<long long>((total + 255) / 256, 4096);
+    t3_planes_kernel<<<grid, 256, 0, s>>>(d, plan.planes, plan.pitch, plan.k_cases);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int rows = 2 * d.snps;
+    if ((e = t3_map(&plan.map_l, plan.planes, rows, plan.pitch, kT3N, true)) != cudaSuccess) return e;
+    if ((e = t3_map(&plan.map_j, plan.planes, rows, plan.pitch, 2 * kT3J, true)) != cudaSuccess) return e;
+    return t3_map(&plan.map_i, plan.planes, rows, plan.pitch, 2, false);
+}
+
+void tensor3_release(T3Plan& plan) {
+    cudaFree(plan.planes);
+    cudaFree(plan.item_begin);
+    plan.planes = nullptr;
+    plan.item_begin = nullptr;
+}
+
+// Bound on |single-precision estimate - exact key / (ln2 * 2^32)| over the 81
+// terms of one combination: with N the number of samples every partial sum is
+// at most 2 N lg2 N (81 roundings of at most 2^-24 of it), lg2.approx is
+// within 2^-18 of log2 on every input the kernel can see (measured worst case
+// 1.93e-6, checked exhaustively against FP64 by fiu_probe_lg2_error), the
+// x + 2^-20 shift moves each term by at most 2^-20 / ln 2 (counts below 16)
+// or one rounding of the count, and the integer table rounds each term by
+// 1/2.  Doubled.
+static double t3_margin(int n_samples) {
+    const double N = n_samples, lgN = std::log2(std::max(2.0, N)), B = 2 * N * lgN;
+    const double u = std::ldexp(1.0, -24), e20 = std::ldexp(1.0, -20), e_lg2 = std::ldexp(1.0, -18);
+    const double err = 81 * u * B + 2 * N * (18 * u + e_lg2) + 81 * e20 / std::log(2.0) +
+                       2 * N * std::ldexp(1.0, -23) / std::log(2.0) + 81 * 0.5 / (std::log(2.0) * 4294967296.0);
+    return 2 * err + 1e-3;
+}
+
+// Every input of t3_lg2 in the kernel is x = (float)(c + 2^-20) for an integer
+// count c in [0, max_c]; largest |t3_lg2(x) - log2(x)| over them, log2 in FP64.
+__global__ void t3_lg2_probe_kernel(unsigned max_c, unsigned long long* worst_bits) {
+    double worst = 0;
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c <= max_c; c += gridDim.x * blockDim.x) {
+        const float x = (float)c + 9.5367431640625e-07f;
+        const double err = fabs((double)t3_lg2(x) - log2((double)x));
+        worst = fmax(worst, err);
+    }
+    atomicMax(worst_bits, (unsigned long long)__double_as_longlong(worst));  // non-negative doubles order as integers
+}
+
+cudaError_t probe_lg2_error(unsigned max_c, double* max_abs_err, cudaStream_t s) {
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    unsigned long long h = 0;
+    e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) {
+        t3_lg2_probe_kernel<<<256, 256, 0, s>>>(max_c, d);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    double v;
+    memcpy(&v, &h, sizeof(v));
+    *max_abs_err = v;
+    return e;
+}
+
+cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
+                           uint32_t* dump, const uint32_t* single, const uint4* pairs, int* status, cudaStream_t s,
+                           int sms) {
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);
@@ -312,8 +733,13 @@ cudaError_t launch_tensor3(const ScanWork& w, const long long* item_begin, long 
     }
     const long long items = g1 - g0;
     if (items <= 0) return cudaSuccess;
+    const double scale = 1.0 / (std::log(2.0) * 4294967296.0);
+    const double thr = ((double)sink.thr - (double)w.base_key) * scale - t3_margin(w.d.n_cases + w.d.n_ctrls);
+    const float thr_f = (float)std::max(-3.0e38, std::min(3.0e38, thr));
+    T3Maps maps{plan.map_l, plan.map_j, plan.map_i};
     const unsigned grid = (unsigned)(items < sms ? items : sms);
-    tensor3_kernel<<<grid, kT3Threads, kT3Smem, s>>>(w, item_begin, g0, g1, sink, dump, single, pairs, status);
+    tensor3_kernel<<<grid, kT3Threads, kT3Smem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, sink, thr_f, dump,
+                                                     single, pairs, status);
     count_launch();
     return cudaGetLastError();
 }

@@ -345,3 +345,64 @@ def test_tiles_agree(oracle, order, kernel):
     assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
     r = [type("R", (), {"combination": x.combination, "val": x.val})() for x in a[0]]
     _check_topn(oracle, ds, order, 30, r, a[1])
+
+
+def test_lg2_prefilter_bound(gs):
+    """The tensor kernel's single-precision MI estimate assumes its log2 is within
+    2^-18 of the exact value on every input it can see (counts up to 2^17 - 1,
+    shifted by 2^-20); checked exhaustively against double precision."""
+    import ctypes as C
+    err = C.c_double(-1)
+    gs.ctx.check(gs.ctx.lib.fiu_probe_lg2_error(gs.ctx.h, (1 << 17) - 1, C.byref(err)))
+    assert 0 <= err.value < 2.0 ** -18, err.value
+
+
+def _one_hot_dataset(seed, snps, n_case, n_ctrl):
+    from fiuncho_gb300 import Dataset
+    rng = np.random.default_rng(seed)
+    maf = rng.uniform(0.05, 0.5, snps)[:, None]
+    u = rng.random((snps, n_case + n_ctrl))
+    geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
+    return Dataset.from_genotypes(geno, np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)])
+
+
+@pytest.mark.parametrize("snps,n_case,n_ctrl", [(3, 1, 1), (4, 65, 63), (33, 130, 1), (34, 64, 64),
+                                                (97, 200, 129), (100, 129, 300)])
+def test_tensor_tile_edges(oracle, snps, n_case, n_ctrl):
+    """tcgen05 kernel vs the full-table kernel at tile edges (SNP counts around the
+    32 x 96 work item, one-sample classes, odd word counts padded to 128 samples):
+    identical tables for every combination and identical top-N lists."""
+    from fiuncho_gb300 import Distribution, GpuSearch, Resident
+    ds = _one_hot_dataset(snps * 7 + n_case, snps, n_case, n_ctrl)
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    dist = Distribution(snps, 2)
+    full = g.scan_tables(res, 3, dist, kernel=1)
+    tens = g.scan_tables(res, 3, dist, kernel=4)
+    mask = full != 0xFFFFFFFF
+    assert np.array_equal(tens[mask], full[mask])
+    out = min(20, math.comb(snps, 3))
+    g.set_kernel(1)
+    a = g.run(res, 3, dist, out, with_fp64=True)
+    g.set_kernel(4)
+    b = g.run(res, 3, dist, out, with_fp64=True)
+    assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
+    _check_topn(oracle, ds, 3, out, b[0], b[1])
+
+
+def test_tensor_prefilter_many_chunks(oracle):
+    """A top-5 search over 260 SNPs runs many chunks with a tight threshold, where the
+    single-precision prefilter rejects nearly every combination: the result equals the
+    exact reduced-work kernel's and the oracle's."""
+    from fiuncho_gb300 import Distribution, GpuSearch, Resident
+    ds = _one_hot_dataset(5, 260, 1500, 1700)
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    dist = Distribution(260, 2)
+    g.set_kernel(3)
+    a = g.run(res, 3, dist, 5, with_fp64=True)
+    g.set_kernel(4)
+    b = g.run(res, 3, dist, 5, with_fp64=True)
+    assert g.last_tile()[0] == 4
+    assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
+    _check_topn(oracle, ds, 3, 5, b[0], b[1], threads=16)
