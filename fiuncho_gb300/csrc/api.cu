@@ -180,7 +180,7 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
             r->t3 = plan;
         }
         kernel = FIU_KERNEL_TENSOR;
-        tp = 256;
+        tp = r->t3->pack ? 256 : 192;  // GEMM width N: one accumulator for both classes, or one per class
         return FIU_OK;
     }
     int rc = choose_kernel(ctx, res, (unsigned)w.order, requested_kernel, kernel);
@@ -278,7 +278,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     long long thr = (long long)0x8000000000000000ull;
     unsigned have = 0;
     const double per_prefix = (double)binom(w.dist_n, order) / std::max<double>(1.0, (double)binom(w.dist_n, order - 1));
-    const double per_unit = tensor ? (double)kT3ItemCombos : per_prefix;
+    const double per_unit = tensor ? res->t3->item_combos : per_prefix;
     long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_unit)));
     long long m = 0;
     while (m < units) {

@@ -105,20 +105,21 @@ cudaError_t launch_elided(bool hs, int tp, const ScanWork& w, long long m0, long
                           uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms);
 
 // tensor3.cu -- order-3 core cells on tcgen05 (one-hot data, whole data set, one worker).
-constexpr int kT3ItemCombos = 1536;  // combinations per work item, about (32 x 96 / 2)
 // Device state of the tensor kernel for one data set: the e4m3 operand planes
 // (row 2*snp+g = "genotype of snp == g" per sample, cases then controls, each
 // class padded to a multiple of 128 samples), their TMA descriptors and the
 // work-item prefix sums.
 struct T3Plan {
     uint8_t* planes = nullptr;
+    int pack = 0;         // log2 of the control weight W when one accumulator holds both classes (else 0)
+    double item_combos = 0;  // combinations per work item, about 32 x L / 2
     int pitch = 0;        // bytes per plane row
     int k_cases = 0;      // padded case samples (= byte offset of the control region)
     long long* item_begin = nullptr;
     long long total = 0;  // work items
-    CUtensorMap map_l;    // box 128 B x 192 rows, 128-byte swizzle (l operand)
+    CUtensorMap map_l;    // box 128 B x 192 rows (256 when packed), 128-byte swizzle (l operand)
     CUtensorMap map_j;    // box 128 B x 64 rows, 128-byte swizzle (j rows of the (i,j) operand)
-    CUtensorMap map_i;    // box 128 B x 2 rows, no swizzle (i rows)
+    CUtensorMap map_i;    // box 128 B x 2 rows, 128-byte swizzle (i rows)
 };
 cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s);
 void tensor3_release(T3Plan& plan);

@@ -12,19 +12,23 @@
 // row 2*snp+g holds 0x38 (1.0) where the sample has genotype g, else 0; cases
 // then controls, each class padded to a multiple of 128 samples.  B rows are
 // plane rows 2l+z, loaded by TMA with 128-byte swizzle straight into the
-// layout tcgen05 reads (K-major, SWIZZLE_128B descriptors).  A rows are the
-// bytewise AND of the i and j plane rows (0x38 & 0x38 = 0x38), built by four
-// producer warps from TMA-staged j rows into the same swizzled layout.
+// layout tcgen05 reads (K-major, SWIZZLE_128B descriptor).  A rows are the
+// bytewise AND of the i and j plane rows (0x38 & 0x38 = 0x38): four producer
+// warps read the TMA-staged j and i rows from shared memory, AND them in
+// registers and write the result to tensor memory (tcgen05.st; one thread per
+// row, 4 e4m3 per 32-bit column), where the MMA reads A from (the [a-tmem]
+// form of tcgen05.mma): A never touches shared memory, whose bandwidth is the
+// kernel's bound.
 //
 // Warp roles (448 threads, one CTA per SM): warp 0 issues the TMA copies,
 // warp 1 issues tcgen05.mma (kind::f8f6f4, K 32 per instruction, 4 per
 // 128-sample stage) and commits, warps 2-5 build A, warps 6-13 run the
-// epilogue.  Four shared-memory stages are handed over with mbarriers.
-// Tensor memory (512 columns): case accumulators in columns 0-191, control
-// accumulators in 192-383, and a 16-bit copy of the case counts in 384-479:
-// as soon as an item's case GEMM is done the epilogue packs its counts there
-// and frees columns 0-191, so the next item's case GEMM overlaps the current
-// item's epilogue.
+// epilogue.  Four stages are handed over with mbarriers.  Tensor memory
+// (512 columns): case accumulators in columns 0-191, control accumulators in
+// 192-383, the A ring (4 stages x 32 columns) in 384-511.  As soon as an
+// item's case GEMM is done the epilogue packs its counts to 16 bits in shared
+// memory and frees columns 0-191, so the next item's case GEMM overlaps the
+// current item's epilogue.
 //
 // Epilogue.  Each thread reads the accumulators of one row (j, x, y); a
 // swizzled shared-memory transpose gives each thread the 16 core counts of one
@@ -53,21 +57,22 @@ constexpr int kT3J = 32, kT3L = 96;              // SNPs per tile
 constexpr int kT3M = 4 * kT3J, kT3N = 2 * kT3L;  // 128 x 192 GEMM tile
 constexpr int kT3KB = 128;                       // samples (= e4m3 bytes) per stage
 constexpr int kT3Stages = 4;
-constexpr int kT3SB = kT3N * kT3KB;              // 24 KB  l rows
-constexpr int kT3SA = kT3M * kT3KB;              // 16 KB  (i,j) rows
+constexpr int kT3SB = kT3N * kT3KB;              // 24 KB  l rows (1 KB multiple)
 constexpr int kT3SJ = 2 * kT3J * kT3KB;          //  8 KB  staged j rows
-constexpr int kT3Stage = kT3SB + kT3SA + kT3SJ;  // 48 KB, a multiple of 1 KB
-constexpr int kT3SI = 2 * kT3KB;                 // i rows of a stage (no swizzle)
+constexpr int kT3SI = 1024;                      // i rows of a stage (2 x 128 B, 128-byte swizzle: the two
+                                                 // rows' chunk c sit in different banks)
 constexpr int kT3EpiWarps = 8, kT3BuildWarps = 4;
 constexpr int kT3Threads = 32 * (2 + kT3BuildWarps + kT3EpiWarps);  // 448
 constexpr int kT3Ebuf = 4096;                    // per epilogue warp: 8 j x 8 l x 4 (x,y) x 16 B
-constexpr size_t kT3Smem = 1024 + (size_t)kT3Stages * (kT3Stage + kT3SI) + (size_t)kT3EpiWarps * kT3Ebuf;
-constexpr int kT3ColCtrl = kT3N, kT3ColStash = 2 * kT3N;  // tensor-memory column bases
+constexpr int kT3Stash = 32 * (kT3L / 2) * 4;    // per epilogue warp: 32 rows x 48 words (16-bit case pairs)
+constexpr size_t kT3Smem = 1024 + (size_t)kT3Stages * (kT3SB + kT3SJ + kT3SI) +
+                           (size_t)kT3EpiWarps * (kT3Ebuf + kT3Stash);
+constexpr int kT3ColCtrl = kT3N, kT3ColA = 2 * kT3N;  // tensor-memory column bases
 constexpr unsigned long long kT3LimitNs = 2000000000ull;   // 2 s per wait
 constexpr uint32_t kT3Idesc = (1u << 4) | ((uint32_t)(kT3N >> 3) << 17) | ((uint32_t)(kT3M >> 4) << 24);
 
 static_assert(kT3Smem <= 227 * 1024 - 256, "tensor kernel shared memory");
-static_assert(kT3ColStash + kT3N / 2 <= 512, "tensor memory columns");
+static_assert(kT3ColA + 32 * kT3Stages <= 512, "tensor memory columns");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -142,7 +147,8 @@ __device__ __forceinline__ float t3_lg2(float x) {
 }
 
 // Work items of one i: J-tile a starts at j0 = i+1+32a and has
-// ceil((n-1-j0)/96) L-tiles starting at l0 = j0+1+96b.
+// ceil((n-1-j0)/L) L-tiles starting at l0 = j0+1+L*b.
+template <int L>
 __device__ __forceinline__ void t3_decode(const long long* __restrict__ item_begin, int n, long long g, int& i,
                                           int& j0, int& l0) {
     int lo = 0, hi = n - 1;
@@ -155,10 +161,10 @@ __device__ __forceinline__ void t3_decode(const long long* __restrict__ item_beg
     long long q = g - item_begin[i];
     for (int a = 0;; ++a) {
         const int j = i + 1 + kT3J * a;
-        const long long nl = (n - 1 - j + kT3L - 1) / kT3L;
+        const long long nl = (n - 1 - j + L - 1) / L;
         if (q < nl) {
             j0 = j;
-            l0 = j + 1 + kT3L * (int)q;
+            l0 = j + 1 + L * (int)q;
             return;
         }
         q -= nl;
@@ -219,6 +225,113 @@ __device__ __forceinline__ void expand3f(const float* core, const uint4& pij, co
     for (int yz = 0; yz < 9; ++yz) t[18 + yz] -= t[yz] + t[9 + yz];
 }
 
+// Evaluates combination (i, j, l) whose 16 core counts (cases z0, z1, controls z0, z1 of each
+// (x, y)) sit in column group k of this warp's transpose buffer: exact 27-cell tables, the
+// bounded single-precision prefilter, the exact fixed-point key for survivors, and the
+// warp-aggregated append of candidates (warp-synchronous: every lane calls it).
+__device__ __forceinline__ void t3_eval(const ScanWork& w, const CandSink& sink, float thr_f, uint32_t* dump,
+                                        const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
+                                        const uint32_t* ebuf, int jl, int k, int i, int j, int l, bool j_ok,
+                                        const uint4& pij, const float (&si)[2][2], const float (&sj)[2][2],
+                                        int lane) {
+    const DevData& d = w.d;
+    const int n = d.snps;
+    const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
+    const float ncf[2] = {(float)d.n_cases, (float)d.n_ctrls};
+    const float tiny = 9.5367431640625e-07f;  // 2^-20: x*lg2(x + tiny) = 0 at x = 0
+    const bool valid = j_ok && l < n && l > j;
+    float core[2][8];
+#pragma unroll
+    for (int x4 = 0; x4 < 4; ++x4) {
+        const uint4 c4 = *reinterpret_cast<const uint4*>(ebuf + 4 * t3_chunk(jl, k, x4));
+        core[0][2 * x4] = u2f(c4.x);
+        core[0][2 * x4 + 1] = u2f(c4.y);
+        core[1][2 * x4] = u2f(c4.z);
+        core[1][2 * x4 + 1] = u2f(c4.w);
+    }
+    uint4 pil = make_uint4(0, 0, 0, 0), pjl = pil, sl4 = pil;
+    if (valid) {
+        pil = __ldg(pairs + pair_index(i, l, n));
+        pjl = __ldg(pairs + pair_index(j, l, n));
+        sl4 = __ldg(reinterpret_cast<const uint4*>(single) + l);
+    }
+    const float sl[2][2] = {{u2f(sl4.x), u2f(sl4.y)}, {u2f(sl4.z), u2f(sl4.w)}};
+    float t[2][27];
+#pragma unroll
+    for (int cls = 0; cls < 2; ++cls)
+        expand3f(core[cls], pij, pil, pjl, si[cls], sj[cls], sl[cls], ncf[cls], cls, t[cls]);
+    // single-precision estimate of sum over cells of T[a] + T[b] - T[a+b], in units of ln2 * 2^32
+    float kf = 0.f;
+#pragma unroll
+    for (int c = 0; c < 27; ++c) {
+        const float a = t[0][c], bb = t[1][c], s = a + bb;
+        kf = fmaf(a, t3_lg2(a + tiny), kf);
+        kf = fmaf(bb, t3_lg2(bb + tiny), kf);
+        kf = fmaf(-s, t3_lg2(s + tiny), kf);
+    }
+    const bool cand = valid && (dump != nullptr || kf >= thr_f);
+    long long key = w.base_key;
+    bool pass = false;
+    if (cand) {
+#pragma unroll
+        for (int c = 0; c < 27; ++c) {
+            const uint32_t a = min(f2u(fmaxf(t[0][c], 0.f)), ncls[0]);
+            const uint32_t bb = min(f2u(fmaxf(t[1][c], 0.f)), ncls[1]);
+            key += __ldg(d.ftab + a) + __ldg(d.ftab + bb) - __ldg(d.ftab + a + bb);
+        }
+        pass = key >= sink.thr;
+        if (dump) {
+            uint32_t* o = dump + ((size_t)pair_index(i, j, n) * n + l) * 54;
+#pragma unroll
+            for (int c = 0; c < 27; ++c) {
+                o[c] = f2u(t[0][c]);
+                o[27 + c] = f2u(t[1][c]);
+            }
+        }
+    }
+    if (sink.evaluated) {
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0 && vmask) atomicAdd(sink.evaluated, (unsigned long long)__popc(vmask));
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, pass);
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(sink.count, (unsigned)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (pass) {
+            const unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (idx < sink.cap) {
+                const int cmb[3] = {i, j, l};
+                sink.buf[idx] = Cand{key, pack_code(cmb, 3, w.bits)};
+            } else {
+                atomicOr(sink.overflow, 1u);
+            }
+        }
+    }
+}
+
+// Per-item constants of one j: the pair cores of (i, j) and the single cores of i and j as floats.
+__device__ __forceinline__ void t3_item_consts(const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
+                                               int i, int j, int n, bool j_ok, uint4& pij, float (&si)[2][2],
+                                               float (&sj)[2][2]) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4*>(single) + i);
+    uint4 b = make_uint4(0, 0, 0, 0);
+    pij = make_uint4(0, 0, 0, 0);
+    if (j_ok) {
+        b = __ldg(reinterpret_cast<const uint4*>(single) + j);
+        pij = __ldg(pairs + pair_index(i, j, n));
+    }
+    si[0][0] = u2f(a.x);
+    si[0][1] = u2f(a.y);
+    si[1][0] = u2f(a.z);
+    si[1][1] = u2f(a.w);
+    sj[0][0] = u2f(b.x);
+    sj[0][1] = u2f(b.y);
+    sj[1][0] = u2f(b.z);
+    sj[1][1] = u2f(b.w);
+}
+
 struct T3Maps {
     CUtensorMap l, j, i;
 };
@@ -232,9 +345,11 @@ __global__ void __launch_bounds__(kT3Threads, 1)
     __shared__ __align__(8) uint64_t case_full, case_empty, ctrl_full, ctrl_empty, done;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-    uint8_t* si_base = sm + kT3Stages * kT3Stage;
+    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);  // B ring
+    uint8_t* sj_base = sm + kT3Stages * kT3SB;                                 // j ring
+    uint8_t* si_base = sj_base + kT3Stages * kT3SJ;                            // i ring
     uint32_t* ebuf_all = reinterpret_cast<uint32_t*>(si_base + kT3Stages * kT3SI);
+    uint4* stash_all = reinterpret_cast<uint4*>(ebuf_all + kT3EpiWarps * (kT3Ebuf / 4));
     volatile int* abort = &abort_flag;
     const DevData& d = w.d;
     const int n = d.snps;
@@ -274,7 +389,7 @@ __global__ void __launch_bounds__(kT3Threads, 1)
             long long step = 0;
             for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
                 int i, j0, l0;
-                t3_decode(item_begin, n, g, i, j0, l0);
+                t3_decode<kT3L>(item_begin, n, g, i, j0, l0);
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const int s = (int)(step % kT3Stages);
                     const long long u = step / kT3Stages;
@@ -283,13 +398,12 @@ __global__ void __launch_bounds__(kT3Threads, 1)
                         break;
                     }
                     const int k0 = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
-                    uint8_t* st = sm + s * kT3Stage;
                     const uint32_t bar = smem_u32(&full_t[s]);
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                                 "r"((uint32_t)(kT3SB + kT3SJ + kT3SI))
+                                 "r"((uint32_t)(kT3SB + kT3SJ + 2 * kT3KB))
                                  : "memory");
-                    t3_tma(smem_u32(st), &maps.l, k0, 2 * l0, bar);
-                    t3_tma(smem_u32(st + kT3SB + kT3SA), &maps.j, k0, 2 * j0, bar);
+                    t3_tma(smem_u32(sm + s * kT3SB), &maps.l, k0, 2 * l0, bar);
+                    t3_tma(smem_u32(sj_base + s * kT3SJ), &maps.j, k0, 2 * j0, bar);
                     t3_tma(smem_u32(si_base + s * kT3SI), &maps.i, k0, 2 * i, bar);
                     ++step;
                 }
@@ -320,17 +434,18 @@ __global__ void __launch_bounds__(kT3Threads, 1)
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const uint32_t sa = smem_u32(sm + s * kT3Stage + kT3SB), sb = smem_u32(sm + s * kT3Stage);
+                    const uint32_t sb = smem_u32(sm + s * kT3SB);
+                    const uint32_t acol = tmem + (uint32_t)(kT3ColA + 32 * s);
                     const uint32_t dcol = tmem + (cls ? (uint32_t)kT3ColCtrl : 0u);
                     const bool first = ks == 0 || ks == ks_c;
 #pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) {
-                        const uint64_t ad = t3_desc(sa + 32 * kk), bd = t3_desc(sb + 32 * kk);
+                    for (int kk = 0; kk < 4; ++kk) {  // A: 8 columns (32 e4m3) per instruction
+                        const uint64_t bd = t3_desc(sb + 32 * kk);
                         const uint32_t acc = (first && kk == 0) ? 0u : 1u;
                         asm volatile(
                             "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
-                            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
-                            "l"(ad), "l"(bd), "r"(kT3Idesc), "r"(acc));
+                            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;}\n" ::"r"(dcol),
+                            "r"(acol + 8 * kk), "l"(bd), "r"(kT3Idesc), "r"(acc));
                     }
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                         smem_u32(&empty[s])));
@@ -346,8 +461,10 @@ __global__ void __launch_bounds__(kT3Threads, 1)
         }
     } else if (warp < 2 + kT3BuildWarps) {
         // ---------------------------------------------------------------- A builders
-        const int t = tid - 64;  // 0..127
-        const int c = t & 7;     // 16-byte chunk; 8 consecutive threads cover one 128-byte row
+        // thread = tensor-memory lane = A row m = (jj, x, y) of this warp's lane quarter
+        const int m = 32 * (warp & 3) + lane;
+        const int r = 2 * (m >> 2) + (m & 1), x = (m >> 1) & 1;  // staged j row (jj, y), i row x
+        const uint32_t a_lane = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)kT3ColA;
         long long step = 0;
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
             for (int ks = 0; ks < ksteps; ++ks, ++step) {
@@ -356,12 +473,288 @@ __global__ void __launch_bounds__(kT3Threads, 1)
                     ok = false;
                     break;
                 }
-                uint8_t* st = sm + s * kT3Stage;
-                const uint8_t* sJ = st + kT3SB + kT3SA;
-                const uint8_t* sI = si_base + s * kT3SI;
-                uint8_t* sA = st + kT3SB;
-                const uint4 i0 = *reinterpret_cast<const uint4*>(sI + c * 16);
-                const uint4 i1 = *reinterpret_cast<const uint4*>(sI + kT3KB + c * 16);
+                const uint8_t* sJ = sj_base + s * kT3SJ + r * 128;
+                const uint8_t* sI = si_base + s * kT3SI + x * 128;
+                uint32_t a[32];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const uint4 jv = *reinterpret_cast<const uint4*>(sJ + ((c ^ (r & 7)) << 4));
+                    const uint4 iv = *reinterpret_cast<const uint4*>(sI + ((c ^ x) << 4));
+                    a[4 * c + 0] = jv.x & iv.x;
+                    a[4 * c + 1] = jv.y & iv.y;
+                    a[4 * c + 2] = jv.z & iv.z;
+                    a[4 * c + 3] = jv.w & iv.w;
+                }
+                // slot s of the A ring is free: the TMA of this step waited for the MMAs of its last use
+                asm volatile(
+                    "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%"
+                    "16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(a_lane +
+                                                                                               (uint32_t)(32 * s)),
+                    "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]), "r"(a[8]),
+                    "r"(a[9]), "r"(a[10]), "r"(a[11]), "r"(a[12]), "r"(a[13]), "r"(a[14]), "r"(a[15]), "r"(a[16]),
+                    "r"(a[17]), "r"(a[18]), "r"(a[19]), "r"(a[20]), "r"(a[21]), "r"(a[22]), "r"(a[23]), "r"(a[24]),
+                    "r"(a[25]), "r"(a[26]), "r"(a[27]), "r"(a[28]), "r"(a[29]), "r"(a[30]), "r"(a[31]));
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_a[s])) : "memory");
+            }
+        }
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        const int e = warp - (2 + kT3BuildWarps);  // 0..7
+        const int q = warp & 3;                    // tensor-memory lane quarter this warp may access
+        const int hh = e >> 2;                     // column half: l offsets [48 hh, 48 hh + 48)
+        uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
+        uint4* stash = stash_all + e * (kT3Stash / 16);  // [word quad][lane]: conflict-free
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+        // row (writer) view: jl = lane/4, xy = lane%4; combination (reader) view: jl = lane/4, kp = lane%4
+        const int jl = lane >> 2, xy = lane & 3, kp = lane & 3;
+        long long item = 0;
+        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+            int i, j0, l0;
+            t3_decode<kT3L>(item_begin, n, g, i, j0, l0);
+            // ---- phase 1: case counts -> 16-bit stash, case columns free for the next item
+            if (!t3_wait(smem_u32(&case_full), (uint32_t)(item & 1), abort)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+            for (int cc = 0; cc < 6; ++cc) {
+                const uint32_t col = (uint32_t)(96 * hh + 16 * cc);
+                uint32_t v[16], p[8];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(lane_base + col));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    p[k] = f2u(__uint_as_float(v[2 * k])) | (f2u(__uint_as_float(v[2 * k + 1])) << 16);
+                stash[(2 * cc) * 32 + lane] = make_uint4(p[0], p[1], p[2], p[3]);
+                stash[(2 * cc + 1) * 32 + lane] = make_uint4(p[4], p[5], p[6], p[7]);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&case_empty)) : "memory");
+            // ---- per-item constants of this thread's j
+            const int j = j0 + 8 * q + jl;
+            const bool j_ok = j < n;
+            uint4 pij;
+            float si[2][2], sj[2][2];
+            t3_item_consts(single, pairs, i, j, n, j_ok, pij, si, sj);
+            // ---- phase 2: control counts + stash -> transpose -> tables -> keys
+            if (!t3_wait(smem_u32(&ctrl_full), (uint32_t)(item & 1), abort)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+            for (int cc = 0; cc < 6; ++cc) {
+                {
+                    const uint32_t col = (uint32_t)(96 * hh + 16 * cc);
+                    uint32_t vt[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
+                        "15}, [%16];"
+                        : "=r"(vt[0]), "=r"(vt[1]), "=r"(vt[2]), "=r"(vt[3]), "=r"(vt[4]), "=r"(vt[5]), "=r"(vt[6]),
+                          "=r"(vt[7]), "=r"(vt[8]), "=r"(vt[9]), "=r"(vt[10]), "=r"(vt[11]), "=r"(vt[12]),
+                          "=r"(vt[13]), "=r"(vt[14]), "=r"(vt[15])
+                        : "r"(lane_base + (uint32_t)kT3ColCtrl + col));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    const uint4 s0 = stash[(2 * cc) * 32 + lane], s1 = stash[(2 * cc + 1) * 32 + lane];
+                    const uint32_t su[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+                    if (cc == 5) {  // last read of this item's accumulators: control columns free
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ctrl_empty))
+                                         : "memory");
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        uint4 c4;
+                        c4.x = su[k] & 0xffffu;
+                        c4.y = su[k] >> 16;
+                        c4.z = f2u(__uint_as_float(vt[2 * k]));
+                        c4.w = f2u(__uint_as_float(vt[2 * k + 1]));
+                        *reinterpret_cast<uint4*>(ebuf + 4 * t3_chunk(jl, k, xy)) = c4;
+                    }
+                }
+                __syncwarp();
+#pragma unroll 1
+                for (int b = 0; b < 2; ++b)
+                    t3_eval(w, sink, thr_f, dump, single, pairs, ebuf, jl, 2 * kp + b, i, j,
+                            l0 + 48 * hh + 8 * cc + 2 * kp + b, j_ok, pij, si, sj, lane);
+                __syncwarp();
+            }
+        }
+    }
+    if (!ok) *abort = 1;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 0 && abort_flag) atomicOr(status, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+// ---------------------------------------------------------------------------
+// Packed-class kernel.  When both classes fit one FP32 accumulator -- control
+// samples weighted by W = 4^h: the operand planes hold 2^h instead of 1.0 in
+// the control region, every control product is 2^h * 2^h = W, and an
+// accumulator holds cases + W * controls, exact while n_cases < W and
+// n_cases + W * n_ctrls < 2^24 -- an item needs one tensor-memory region of
+// N columns instead of two.  N = 256 (128 l per item; the M 128 x K 32 MMA
+// costs the same for every N up to 256) and two regions alternate between
+// items, so the next item's GEMM runs while the epilogue reads the last one.
+// A is built in shared memory (tensor memory is full), 3 stages.
+constexpr int kPL = 128, kPN = 2 * kPL;                  // 128 l, N 256
+constexpr int kPStages = 3;
+constexpr int kPSB = kPN * kT3KB;                         // 32 KB  l rows
+constexpr int kPSA = kT3M * kT3KB;                        // 16 KB  (i,j) rows, 128-byte swizzle
+constexpr int kPStage = kPSB + kPSA + kT3SJ + kT3SI;      // 57 KB, a multiple of 1 KB
+constexpr size_t kPSmem = 1024 + (size_t)kPStages * kPStage + (size_t)kT3EpiWarps * kT3Ebuf;
+constexpr uint32_t kPIdesc = (1u << 4) | ((uint32_t)(kPN >> 3) << 17) | ((uint32_t)(kT3M >> 4) << 24);
+static_assert(kPSmem <= 227 * 1024 - 256, "packed tensor kernel shared memory");
+static_assert(2 * kPN <= 512, "packed tensor kernel tensor memory");
+
+__global__ void __launch_bounds__(kT3Threads, 1)
+    tensor3p_kernel(const __grid_constant__ T3Maps maps, ScanWork w, const long long* __restrict__ item_begin,
+                    long long g0, long long g1, int k_cases, int pack, CandSink sink, float thr_f, uint32_t* dump,
+                    const uint32_t* __restrict__ single, const uint4* __restrict__ pairs, int* status) {
+    extern __shared__ uint8_t smraw[];
+    __shared__ __align__(8) uint64_t full_t[kPStages], full_a[kPStages], empty[kPStages];
+    __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);  // stages: B | A | j rows | i rows
+    uint32_t* ebuf_all = reinterpret_cast<uint32_t*>(sm + kPStages * kPStage);
+    volatile int* abort = &abort_flag;
+    const DevData& d = w.d;
+    const int n = d.snps;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ks_c = k_cases / kT3KB;
+    const int ksteps = ks_c + (d.tw + 1) / 2;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kPStages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_t[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_a[s])), "r"(kT3BuildWarps));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[b])), "r"(kT3EpiWarps));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        abort_flag = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+
+    if (warp == 0) {
+        // ---------------------------------------------------------------- TMA producer
+        if (lane == 0) {
+            long long step = 0;
+            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+                int i, j0, l0;
+                t3_decode<kPL>(item_begin, n, g, i, j0, l0);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const int s = (int)(step % kPStages);
+                    const long long u = step / kPStages;
+                    if (u > 0 && !t3_wait(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    const int k0 = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
+                    uint8_t* st = sm + s * kPStage;
+                    const uint32_t bar = smem_u32(&full_t[s]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                                 "r"((uint32_t)(kPSB + kT3SJ + 2 * kT3KB))
+                                 : "memory");
+                    t3_tma(smem_u32(st), &maps.l, k0, 2 * l0, bar);
+                    t3_tma(smem_u32(st + kPSB + kPSA), &maps.j, k0, 2 * j0, bar);
+                    t3_tma(smem_u32(st + kPSB + kPSA + kT3SJ), &maps.i, k0, 2 * i, bar);
+                    ++step;
+                }
+            }
+            for (int s = 0; s < kPStages; ++s) {
+                if (step <= s) continue;
+                const long long last = s + ((step - 1 - s) / kPStages) * kPStages;
+                if (!t3_drain(smem_u32(&full_t[s]), (uint32_t)((last / kPStages) & 1))) ok = false;
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            long long step = 0, item = 0;
+            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+                const int buf = (int)(item & 1);
+                if (item >= 2 && !t3_wait(smem_u32(&acc_empty[buf]), (uint32_t)(((item >> 1) - 1) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t dcol = tmem + (uint32_t)(kPN * buf);
+                for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                    const int s = (int)(step % kPStages);
+                    if (!t3_wait(smem_u32(&full_a[s]), (uint32_t)((step / kPStages) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t sb = smem_u32(sm + s * kPStage), sa = sb + kPSB;
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint64_t ad = t3_desc(sa + 32 * kk), bd = t3_desc(sb + 32 * kk);
+                        const uint32_t acc = (ks == 0 && kk == 0) ? 0u : 1u;
+                        asm volatile(
+                            "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
+                            "l"(ad), "l"(bd), "r"(kPIdesc), "r"(acc));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                        smem_u32(&empty[s])));
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(&acc_full[buf])));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&done)));
+            if (!t3_drain(smem_u32(&done), 0)) ok = false;
+        }
+    } else if (warp < 2 + kT3BuildWarps) {
+        // ---------------------------------------------------------------- A builders (shared memory)
+        const int t = tid - 64;  // 0..127
+        const int c = t & 7;     // 16-byte chunk; 8 consecutive threads cover one 128-byte row
+        long long step = 0;
+        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+            for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                const int s = (int)(step % kPStages);
+                if (!t3_wait(smem_u32(&full_t[s]), (uint32_t)((step / kPStages) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t* st = sm + s * kPStage;
+                uint8_t* sA = st + kPSB;
+                const uint8_t* sJ = sA + kPSA;
+                const uint8_t* sI = sJ + kT3SJ;
+                const uint4 i0 = *reinterpret_cast<const uint4*>(sI + (c << 4));
+                const uint4 i1 = *reinterpret_cast<const uint4*>(sI + 128 + ((c ^ 1) << 4));
 #pragma unroll
                 for (int r = t >> 3; r < 2 * kT3J; r += 16) {  // j row r = (jj, y)
                     const uint4 jv = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((c ^ (r & 7)) << 4));
@@ -388,186 +781,59 @@ __global__ void __launch_bounds__(kT3Threads, 1)
         // ---------------------------------------------------------------- epilogue
         const int e = warp - (2 + kT3BuildWarps);  // 0..7
         const int q = warp & 3;                    // tensor-memory lane quarter this warp may access
-        const int hh = e >> 2;                     // column half: l offsets [48 hh, 48 hh + 48)
+        const int hh = e >> 2;                     // column half: l offsets [64 hh, 64 hh + 64)
         uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-        const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
-        const float ncf[2] = {(float)d.n_cases, (float)d.n_ctrls};
-        const float tiny = 9.5367431640625e-07f;  // 2^-20: x*lg2(x + tiny) = 0 at x = 0
-        // row (writer) view: jl = lane/4, xy = lane%4; combination (reader) view: jl = lane/4, kp = lane%4
+        const uint32_t wmask = (1u << pack) - 1u;
         const int jl = lane >> 2, xy = lane & 3, kp = lane & 3;
         long long item = 0;
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
             int i, j0, l0;
-            t3_decode(item_begin, n, g, i, j0, l0);
-            // ---- phase 1: case counts -> 16-bit stash, case columns free for the next item
-            if (!t3_wait(smem_u32(&case_full), (uint32_t)(item & 1), abort)) {
-                ok = false;
-                break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;");
-#pragma unroll 1
-            for (int cc = 0; cc < 6; ++cc) {
-                const uint32_t col = (uint32_t)(96 * hh + 16 * cc);
-                uint32_t v[16], p[8];
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
-                    : "r"(lane_base + col));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                for (int k = 0; k < 8; ++k)
-                    p[k] = f2u(__uint_as_float(v[2 * k])) | (f2u(__uint_as_float(v[2 * k + 1])) << 16);
-                asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(
-                                 lane_base + (uint32_t)kT3ColStash + (uint32_t)(48 * hh + 8 * cc)),
-                             "r"(p[0]), "r"(p[1]), "r"(p[2]), "r"(p[3]), "r"(p[4]), "r"(p[5]), "r"(p[6]), "r"(p[7]));
-            }
-            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            __syncwarp();
-            if (lane == 0)
-                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&case_empty)) : "memory");
-            // ---- per-item constants of this thread's j
+            t3_decode<kPL>(item_begin, n, g, i, j0, l0);
+            const int buf = (int)(item & 1);
             const int j = j0 + 8 * q + jl;
             const bool j_ok = j < n;
-            uint4 pij = make_uint4(0, 0, 0, 0);
+            uint4 pij;
             float si[2][2], sj[2][2];
-            {
-                const uint4 a = __ldg(reinterpret_cast<const uint4*>(single) + i);
-                uint4 b = make_uint4(0, 0, 0, 0);
-                if (j_ok) {
-                    b = __ldg(reinterpret_cast<const uint4*>(single) + j);
-                    pij = __ldg(pairs + pair_index(i, j, n));
-                }
-                si[0][0] = u2f(a.x);
-                si[0][1] = u2f(a.y);
-                si[1][0] = u2f(a.z);
-                si[1][1] = u2f(a.w);
-                sj[0][0] = u2f(b.x);
-                sj[0][1] = u2f(b.y);
-                sj[1][0] = u2f(b.z);
-                sj[1][1] = u2f(b.w);
-            }
-            // ---- phase 2: control counts + stash -> transpose -> tables -> keys
-            if (!t3_wait(smem_u32(&ctrl_full), (uint32_t)(item & 1), abort)) {
+            t3_item_consts(single, pairs, i, j, n, j_ok, pij, si, sj);
+            if (!t3_wait(smem_u32(&acc_full[buf]), (uint32_t)((item >> 1) & 1), abort)) {
                 ok = false;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
-            for (int cc = 0; cc < 6; ++cc) {
+            for (int cc = 0; cc < 8; ++cc) {
                 {
-                    const uint32_t col = (uint32_t)(96 * hh + 16 * cc);
-                    uint32_t vt[16], su[8];
+                    const uint32_t col = (uint32_t)(kPN * buf + 128 * hh + 16 * cc);
+                    uint32_t v[16];
                     asm volatile(
                         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
                         "15}, [%16];"
-                        : "=r"(vt[0]), "=r"(vt[1]), "=r"(vt[2]), "=r"(vt[3]), "=r"(vt[4]), "=r"(vt[5]), "=r"(vt[6]),
-                          "=r"(vt[7]), "=r"(vt[8]), "=r"(vt[9]), "=r"(vt[10]), "=r"(vt[11]), "=r"(vt[12]),
-                          "=r"(vt[13]), "=r"(vt[14]), "=r"(vt[15])
-                        : "r"(lane_base + (uint32_t)kT3ColCtrl + col));
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                        : "=r"(su[0]), "=r"(su[1]), "=r"(su[2]), "=r"(su[3]), "=r"(su[4]), "=r"(su[5]), "=r"(su[6]),
-                          "=r"(su[7])
-                        : "r"(lane_base + (uint32_t)kT3ColStash + (uint32_t)(48 * hh + 8 * cc)));
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(lane_base + col));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    if (cc == 5) {  // last read of this item's accumulators: control columns free
+                    if (cc == 7) {  // last read of this item's accumulators: the region is free
                         asm volatile("tcgen05.fence::before_thread_sync;");
                         __syncwarp();
                         if (lane == 0)
-                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ctrl_empty))
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
                                          : "memory");
                     }
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
-                        uint4 c4;
-                        c4.x = su[k] & 0xffffu;
-                        c4.y = su[k] >> 16;
-                        c4.z = f2u(__uint_as_float(vt[2 * k]));
-                        c4.w = f2u(__uint_as_float(vt[2 * k + 1]));
-                        *reinterpret_cast<uint4*>(ebuf + 4 * t3_chunk(jl, k, xy)) = c4;
+                        const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * k]));
+                        const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * k + 1]));
+                        *reinterpret_cast<uint4*>(ebuf + 4 * t3_chunk(jl, k, xy)) =
+                            make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
                     }
                 }
                 __syncwarp();
 #pragma unroll 1
-                for (int b = 0; b < 2; ++b) {
-                    const int k = 2 * kp + b;
-                    const int l = l0 + 48 * hh + 8 * cc + k;
-                    const bool valid = j_ok && l < n && l > j;
-                    float core[2][8];
-#pragma unroll
-                    for (int x4 = 0; x4 < 4; ++x4) {
-                        const uint4 c4 = *reinterpret_cast<const uint4*>(ebuf + 4 * t3_chunk(jl, k, x4));
-                        core[0][2 * x4] = u2f(c4.x);
-                        core[0][2 * x4 + 1] = u2f(c4.y);
-                        core[1][2 * x4] = u2f(c4.z);
-                        core[1][2 * x4 + 1] = u2f(c4.w);
-                    }
-                    uint4 pil = make_uint4(0, 0, 0, 0), pjl = pil, sl4 = pil;
-                    if (valid) {
-                        pil = __ldg(pairs + pair_index(i, l, n));
-                        pjl = __ldg(pairs + pair_index(j, l, n));
-                        sl4 = __ldg(reinterpret_cast<const uint4*>(single) + l);
-                    }
-                    const float sl[2][2] = {{u2f(sl4.x), u2f(sl4.y)}, {u2f(sl4.z), u2f(sl4.w)}};
-                    float t[2][27];
-#pragma unroll
-                    for (int cls = 0; cls < 2; ++cls)
-                        expand3f(core[cls], pij, pil, pjl, si[cls], sj[cls], sl[cls], ncf[cls], cls, t[cls]);
-                    // single-precision estimate of sum over cells of T[a] + T[b] - T[a+b], in units of ln2 * 2^32
-                    float kf = 0.f;
-#pragma unroll
-                    for (int c = 0; c < 27; ++c) {
-                        const float a = t[0][c], bb = t[1][c], s = a + bb;
-                        kf = fmaf(a, t3_lg2(a + tiny), kf);
-                        kf = fmaf(bb, t3_lg2(bb + tiny), kf);
-                        kf = fmaf(-s, t3_lg2(s + tiny), kf);
-                    }
-                    const bool cand = valid && (dump != nullptr || kf >= thr_f);
-                    long long key = w.base_key;
-                    bool pass = false;
-                    if (cand) {
-#pragma unroll
-                        for (int c = 0; c < 27; ++c) {
-                            const uint32_t a = min(f2u(fmaxf(t[0][c], 0.f)), ncls[0]);
-                            const uint32_t bb = min(f2u(fmaxf(t[1][c], 0.f)), ncls[1]);
-                            key += __ldg(d.ftab + a) + __ldg(d.ftab + bb) - __ldg(d.ftab + a + bb);
-                        }
-                        pass = key >= sink.thr;
-                        if (dump) {
-                            uint32_t* o = dump + ((size_t)pair_index(i, j, n) * n + l) * 54;
-#pragma unroll
-                            for (int c = 0; c < 27; ++c) {
-                                o[c] = f2u(t[0][c]);
-                                o[27 + c] = f2u(t[1][c]);
-                            }
-                        }
-                    }
-                    if (sink.evaluated) {
-                        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-                        if (lane == 0 && vmask) atomicAdd(sink.evaluated, (unsigned long long)__popc(vmask));
-                    }
-                    const unsigned mask = __ballot_sync(0xffffffffu, pass);
-                    if (mask) {
-                        const int leader = __ffs(mask) - 1;
-                        unsigned base = 0;
-                        if (lane == leader) base = atomicAdd(sink.count, (unsigned)__popc(mask));
-                        base = __shfl_sync(0xffffffffu, base, leader);
-                        if (pass) {
-                            const unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
-                            if (idx < sink.cap) {
-                                const int cmb[3] = {i, j, l};
-                                sink.buf[idx] = Cand{key, pack_code(cmb, 3, w.bits)};
-                            } else {
-                                atomicOr(sink.overflow, 1u);
-                            }
-                        }
-                    }
-                }
+                for (int b = 0; b < 2; ++b)
+                    t3_eval(w, sink, thr_f, dump, single, pairs, ebuf, jl, 2 * kp + b, i, j,
+                            l0 + 64 * hh + 8 * cc + 2 * kp + b, j_ok, pij, si, sj, lane);
                 __syncwarp();
             }
         }
@@ -580,7 +846,7 @@ __global__ void __launch_bounds__(kT3Threads, 1)
 }
 
 // Operand planes: one thread per 16 output bytes (16 samples of one row).
-__global__ void t3_planes_kernel(DevData d, uint8_t* planes, int pitch, int k_cases) {
+__global__ void t3_planes_kernel(DevData d, uint8_t* planes, int pitch, int k_cases, uint32_t ctrl_byte) {
     const long long chunks = (long long)pitch / 16;
     const long long total = 2ll * d.snps * chunks;
     const size_t per_snp = 3 * (size_t)(d.cw + d.tw);
@@ -603,18 +869,19 @@ __global__ void t3_planes_kernel(DevData d, uint8_t* planes, int pitch, int k_ca
         uint4 v;
         uint32_t* pv = &v.x;
 #pragma unroll
-        for (int qd = 0; qd < 4; ++qd) pv[qd] = (((bits >> (4 * qd)) & 0xfu) * 0x00204081u & 0x01010101u) * 0x38u;
+        for (int qd = 0; qd < 4; ++qd)
+            pv[qd] = (((bits >> (4 * qd)) & 0xfu) * 0x00204081u & 0x01010101u) * (ctrl ? ctrl_byte : 0x38u);
         *reinterpret_cast<uint4*>(planes + (size_t)row * pitch + o) = v;
     }
 }
 
 // Items per i (host): prefix sums item_begin[0..n], item_begin[n] = total.
-static long long t3_items(int n, std::vector<long long>& item_begin) {
+static long long t3_items(int n, int L, std::vector<long long>& item_begin) {
     item_begin.assign((size_t)n + 1, 0);
     long long total = 0;
     for (int i = 0; i < n; ++i) {
         item_begin[i] = total;
-        for (int j = i + 1; j < n - 1; j += kT3J) total += (n - 1 - j + kT3L - 1) / kT3L;
+        for (int j = i + 1; j < n - 1; j += kT3J) total += (n - 1 - j + L - 1) / L;
     }
     item_begin[n] = total;
     return total;
@@ -648,23 +915,37 @@ static cudaError_t t3_map(CUtensorMap* m, uint8_t* base, int rows, int pitch, in
 }
 
 cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
+    // one accumulator for both classes when some W = 4^h (h <= 8, so 2^h is an e4m3 power of two) has
+    // n_cases < W and n_cases + W * n_ctrls < 2^24 (every count exact in FP32)
+    plan.pack = 0;
+    for (int h = 1; h <= 8; ++h) {
+        const long long W = 1ll << (2 * h);
+        if (W > d.n_cases && d.n_cases + W * (long long)d.n_ctrls < (1ll << 24)) {
+            plan.pack = 2 * h;
+            break;
+        }
+    }
+    const int L = plan.pack ? kPL : kT3L;
+    plan.item_combos = kT3J * L / 2.0;
     plan.k_cases = kT3KB * ((d.cw + 1) / 2);
     plan.pitch = plan.k_cases + kT3KB * ((d.tw + 1) / 2);
     std::vector<long long> ib;
-    plan.total = t3_items(d.snps, ib);
+    plan.total = t3_items(d.snps, L, ib);
     cudaError_t e = cudaMalloc((void**)&plan.item_begin, ib.size() * sizeof(long long));
     if (e == cudaSuccess) e = cudaMemcpy(plan.item_begin, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc((void**)&plan.planes, (size_t)2 * d.snps * plan.pitch);
     if (e != cudaSuccess) return e;
     const long long total = 2ll * d.snps * (plan.pitch / 16);
     const int grid = (int)std::min<long long>((total + 255) / 256, 4096);
-    t3_planes_kernel<<<grid, 256, 0, s>>>(d, plan.planes, plan.pitch, plan.k_cases);
+    const uint32_t ctrl_byte = plan.pack ? (uint32_t)((plan.pack / 2 + 7) << 3) : 0x38u;  // e4m3 2^h
+    t3_planes_kernel<<<grid, 256, 0, s>>>(d, plan.planes, plan.pitch, plan.k_cases, ctrl_byte);
     count_launch();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int rows = 2 * d.snps;
-    if ((e = t3_map(&plan.map_l, plan.planes, rows, plan.pitch, kT3N, true)) != cudaSuccess) return e;
+    if ((e = t3_map(&plan.map_l, plan.planes, rows, plan.pitch, plan.pack ? kPN : kT3N, true)) != cudaSuccess)
+        return e;
     if ((e = t3_map(&plan.map_j, plan.planes, rows, plan.pitch, 2 * kT3J, true)) != cudaSuccess) return e;
-    return t3_map(&plan.map_i, plan.planes, rows, plan.pitch, 2, false);
+    return t3_map(&plan.map_i, plan.planes, rows, plan.pitch, 2, true);
 }
 
 void tensor3_release(T3Plan& plan) {
@@ -728,6 +1009,8 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tensor3p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
@@ -738,8 +1021,12 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     const float thr_f = (float)std::max(-3.0e38, std::min(3.0e38, thr));
     T3Maps maps{plan.map_l, plan.map_j, plan.map_i};
     const unsigned grid = (unsigned)(items < sms ? items : sms);
-    tensor3_kernel<<<grid, kT3Threads, kT3Smem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, sink, thr_f, dump,
-                                                     single, pairs, status);
+    if (plan.pack)
+        tensor3p_kernel<<<grid, kT3Threads, kPSmem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, plan.pack,
+                                                          sink, thr_f, dump, single, pairs, status);
+    else
+        tensor3_kernel<<<grid, kT3Threads, kT3Smem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, sink, thr_f,
+                                                         dump, single, pairs, status);
     count_launch();
     return cudaGetLastError();
 }

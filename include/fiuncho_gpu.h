@@ -91,7 +91,7 @@ int fiu_kernel_timing(const fiu_ctx *ctx, double *count_ms, uint64_t *count_laun
 /* Measures this GPU's sustained 32-bit AND+POPC+ADD rate (word-ops per second)
  * with a short in-bounds kernel; the integer-pipe peak for roofline reports. */
 int fiu_probe_popc_rate(fiu_ctx *ctx, double *word_ops_per_s);
-/* Self-check of the tensor kernel's threshold prefilter: the largest absolute
+/* Self-check of the tensor kernels' threshold prefilter: the largest absolute
  * error, against double precision, of the single-precision log2 it uses, over
  * every input it can see (x = c + 2^-20 rounded to float, integer counts c in
  * [0, max_c]).  The prefilter's error bound assumes it stays below 2^-18. */

@@ -348,7 +348,7 @@ def test_tiles_agree(oracle, order, kernel):
 
 
 def test_lg2_prefilter_bound(gs):
-    """The tensor kernel's single-precision MI estimate assumes its log2 is within
+    """The tensor kernels' single-precision MI estimate assumes its log2 is within
     2^-18 of the exact value on every input it can see (counts up to 2^17 - 1,
     shifted by 2^-20); checked exhaustively against double precision."""
     import ctypes as C
@@ -367,10 +367,13 @@ def _one_hot_dataset(seed, snps, n_case, n_ctrl):
 
 
 @pytest.mark.parametrize("snps,n_case,n_ctrl", [(3, 1, 1), (4, 65, 63), (33, 130, 1), (34, 64, 64),
-                                                (97, 200, 129), (100, 129, 300)])
+                                                (97, 200, 129), (100, 129, 300), (130, 100, 60000),
+                                                (40, 5000, 4100), (97, 4500, 4500), (98, 1, 9000)])
 def test_tensor_tile_edges(oracle, snps, n_case, n_ctrl):
-    """tcgen05 kernel vs the full-table kernel at tile edges (SNP counts around the
-    32 x 96 work item, one-sample classes, odd word counts padded to 128 samples):
+    """tcgen05 kernels vs the full-table kernel at tile edges (SNP counts around the
+    32 x 128 and 32 x 96 work items, one-sample classes, odd word counts padded to 128
+    samples), in both forms -- one accumulator for both classes (controls weighted by
+    4^h, N 256) and one accumulator per class (N 192, classes too large to pack):
     identical tables for every combination and identical top-N lists."""
     from fiuncho_gb300 import Distribution, GpuSearch, Resident
     ds = _one_hot_dataset(snps * 7 + n_case, snps, n_case, n_ctrl)
@@ -386,6 +389,8 @@ def test_tensor_tile_edges(oracle, snps, n_case, n_ctrl):
     a = g.run(res, 3, dist, out, with_fp64=True)
     g.set_kernel(4)
     b = g.run(res, 3, dist, out, with_fp64=True)
+    packed = any(4 ** h > n_case and n_case + 4 ** h * n_ctrl < 2 ** 24 for h in range(1, 9))
+    assert g.last_tile() == (4, 256 if packed else 192)
     assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
     _check_topn(oracle, ds, 3, out, b[0], b[1])
 
