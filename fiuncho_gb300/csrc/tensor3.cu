@@ -612,8 +612,11 @@ __global__ void __launch_bounds__(kT3Threads, 1)
 // N columns instead of two.  N = 256 (128 l per item; the M 128 x K 32 MMA
 // costs the same for every N up to 256) and two regions alternate between
 // items, so the next item's GEMM runs while the epilogue reads the last one.
-// A is built in shared memory (tensor memory is full), 3 stages.
+// A is built in shared memory (tensor memory is full) by six producer warps,
+// 3 stages.
 constexpr int kPL = 128, kPN = 2 * kPL;                  // 128 l, N 256
+constexpr int kPBuildWarps = 6;                           // producer warps (the A build is on the critical path)
+constexpr int kPThreads = 32 * (2 + kPBuildWarps + kT3EpiWarps);  // 512: 128 registers fill the register file
 constexpr int kPStages = 3;
 constexpr int kPSB = kPN * kT3KB;                         // 32 KB  l rows
 constexpr int kPSA = kT3M * kT3KB;                        // 16 KB  (i,j) rows, 128-byte swizzle
@@ -623,7 +626,7 @@ constexpr uint32_t kPIdesc = (1u << 4) | ((uint32_t)(kPN >> 3) << 17) | ((uint32
 static_assert(kPSmem <= 227 * 1024 - 256, "packed tensor kernel shared memory");
 static_assert(2 * kPN <= 512, "packed tensor kernel tensor memory");
 
-__global__ void __launch_bounds__(kT3Threads, 1)
+__global__ void __launch_bounds__(kPThreads, 1)
     tensor3p_kernel(const __grid_constant__ T3Maps maps, ScanWork w, const long long* __restrict__ item_begin,
                     long long g0, long long g1, int k_cases, int pack, CandSink sink, float thr_f, uint32_t* dump,
                     const uint32_t* __restrict__ single, const uint4* __restrict__ pairs, int* status) {
@@ -649,7 +652,7 @@ __global__ void __launch_bounds__(kT3Threads, 1)
     if (tid == 0) {
         for (int s = 0; s < kPStages; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_t[s])));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_a[s])), "r"(kT3BuildWarps));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_a[s])), "r"(kPBuildWarps));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
         }
         for (int b = 0; b < 2; ++b) {
@@ -737,9 +740,9 @@ __global__ void __launch_bounds__(kT3Threads, 1)
                 smem_u32(&done)));
             if (!t3_drain(smem_u32(&done), 0)) ok = false;
         }
-    } else if (warp < 2 + kT3BuildWarps) {
+    } else if (warp < 2 + kPBuildWarps) {
         // ---------------------------------------------------------------- A builders (shared memory)
-        const int t = tid - 64;  // 0..127
+        const int t = tid - 64;  // 0 .. 32 * kPBuildWarps - 1
         const int c = t & 7;     // 16-byte chunk; 8 consecutive threads cover one 128-byte row
         long long step = 0;
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
@@ -756,7 +759,7 @@ __global__ void __launch_bounds__(kT3Threads, 1)
                 const uint4 i0 = *reinterpret_cast<const uint4*>(sI + (c << 4));
                 const uint4 i1 = *reinterpret_cast<const uint4*>(sI + 128 + ((c ^ 1) << 4));
 #pragma unroll
-                for (int r = t >> 3; r < 2 * kT3J; r += 16) {  // j row r = (jj, y)
+                for (int r = t >> 3; r < 2 * kT3J; r += 4 * kPBuildWarps) {  // j row r = (jj, y)
                     const uint4 jv = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((c ^ (r & 7)) << 4));
                     const int m0 = 4 * (r >> 1) + (r & 1), m1 = m0 + 2;  // A rows (jj, x, y), x = 0, 1
                     uint4 v;
@@ -779,7 +782,7 @@ __global__ void __launch_bounds__(kT3Threads, 1)
         }
     } else {
         // ---------------------------------------------------------------- epilogue
-        const int e = warp - (2 + kT3BuildWarps);  // 0..7
+        const int e = warp - (2 + kPBuildWarps);  // 0..7
         const int q = warp & 3;                    // tensor-memory lane quarter this warp may access
         const int hh = e >> 2;                     // column half: l offsets [64 hh, 64 hh + 64)
         uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
@@ -1022,7 +1025,7 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     T3Maps maps{plan.map_l, plan.map_j, plan.map_i};
     const unsigned grid = (unsigned)(items < sms ? items : sms);
     if (plan.pack)
-        tensor3p_kernel<<<grid, kT3Threads, kPSmem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, plan.pack,
+        tensor3p_kernel<<<grid, kPThreads, kPSmem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, plan.pack,
                                                           sink, thr_f, dump, single, pairs, status);
     else
         tensor3_kernel<<<grid, kT3Threads, kT3Smem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, sink, thr_f,
