@@ -103,8 +103,8 @@ int choose_kernel(fiu_ctx* ctx, const fiu_resident* res_c, unsigned order, int r
                            res->d.n_ctrls <= 65535 && elided_smem(order, res->d.cw, res->d.tw) <= 160 * 1024;
     kernel = requested ? requested : (elided_ok ? FIU_KERNEL_ELIDED_HS : FIU_KERNEL_FULL);
     if (kernel < FIU_KERNEL_FULL || kernel > FIU_KERNEL_TENSOR) return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
-    if (kernel == FIU_KERNEL_TENSOR && order != 3)
-        return fail(ctx, FIU_ERR_UNSUPPORTED, "the tensor-core kernel serves order 3");
+    if (kernel == FIU_KERNEL_TENSOR && order != 2 && order != 3)
+        return fail(ctx, FIU_ERR_UNSUPPORTED, "the tensor-core kernels serve orders 2 and 3");
     if (kernel == FIU_KERNEL_FULL) return FIU_OK;
     if (!elided_ok)
         return fail(ctx, FIU_ERR_UNSUPPORTED, "elided kernels need one-hot data, order 2 or 3, classes <= 65535");
@@ -152,7 +152,7 @@ static int heuristic_tp(int kernel, const ScanWork& w) {
 }
 
 static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
-    return res->one_hot && w.order == 3 && w.dist_step == 1 && w.dist_offset == 0 && w.dist_n == res->d.snps &&
+    return res->one_hot && (w.order == 2 || w.order == 3) && w.dist_step == 1 && w.dist_offset == 0 && w.dist_n == res->d.snps &&
            res->d.n_cases >= 1 && res->d.n_ctrls >= 1 && res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 &&
            res->d.snps < (1 << 21);
 }
@@ -163,8 +163,8 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
                                                    tensor_ok(res, w))) {
         if (!allow_tensor || !tensor_ok(res, w))
             return fail(ctx, FIU_ERR_UNSUPPORTED,
-                        "the tensor-core kernel needs one-hot data, order 3 and the whole data set on one worker");
-        int rc = choose_kernel(ctx, res, 3, FIU_KERNEL_ELIDED_HS, kernel);  // builds the core tables
+                        "the tensor-core kernels need one-hot data, order 2 or 3 and the whole data set on one worker");
+        int rc = choose_kernel(ctx, res, (unsigned)w.order, FIU_KERNEL_ELIDED_HS, kernel);  // builds the core tables
         if (rc) return rc;
         fiu_resident* r = const_cast<fiu_resident*>(res);
         if (!r->t3) {
@@ -180,7 +180,8 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
             r->t3 = plan;
         }
         kernel = FIU_KERNEL_TENSOR;
-        tp = r->t3->pack ? 256 : 192;  // GEMM width N: one accumulator for both classes, or one per class
+        // GEMM width N: order 3 uses 256 with one accumulator for both classes, 192 with one per class
+        tp = (w.order == 2 || r->t3->pack) ? 256 : 192;
         return FIU_OK;
     }
     int rc = choose_kernel(ctx, res, (unsigned)w.order, requested_kernel, kernel);
@@ -262,7 +263,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     ctx->last_kernel = kernel;
     ctx->last_tp = tp;
     const bool tensor = kernel == FIU_KERNEL_TENSOR;
-    const long long units = tensor ? res->t3->total : w.n_prefixes;
+    const long long units = tensor ? tensor_units(*res->t3, (int)order) : w.n_prefixes;
     int* t_status = (int*)(ctx->ctl + 16);
     if (tensor) CK(cudaMemsetAsync(t_status, 0, sizeof(int), ctx->stream), "status reset");
     const unsigned keep = outputs + std::max(32u, outputs / 8);
@@ -278,7 +279,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     long long thr = (long long)0x8000000000000000ull;
     unsigned have = 0;
     const double per_prefix = (double)binom(w.dist_n, order) / std::max<double>(1.0, (double)binom(w.dist_n, order - 1));
-    const double per_unit = tensor ? res->t3->item_combos : per_prefix;
+    const double per_unit = tensor ? tensor_item_combos(*res->t3, (int)order) : per_prefix;
     long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_unit)));
     long long m = 0;
     while (m < units) {
@@ -723,7 +724,8 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
     if (e == cudaSuccess && kernel == FIU_KERNEL_TENSOR) {
         e = cudaMemsetAsync(ctx->ctl + 16, 0, sizeof(int), s);
         if (e == cudaSuccess)
-            e = launch_tensor3(w, *res->t3, 0, res->t3->total, sink, d, res->single, res->pairs, (int*)(ctx->ctl + 16),
+            e = launch_tensor3(w, *res->t3, 0, tensor_units(*res->t3, (int)order), sink, d, res->single, res->pairs,
+                               (int*)(ctx->ctl + 16),
                                s, ctx->sms);
     } else if (e == cudaSuccess) {
         e = launch_kernel(kernel, tp, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);

@@ -104,7 +104,7 @@ size_t elided_smem(int order, int cw, int tw);
 cudaError_t launch_elided(bool hs, int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
                           uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms);
 
-// tensor3.cu -- order-3 core cells on tcgen05 (one-hot data, whole data set, one worker).
+// tensor3.cu -- order-2 and order-3 core cells on tcgen05 (one-hot data, whole data set, one worker).
 // Device state of the tensor kernel for one data set: the e4m3 operand planes
 // (row 2*snp+g = "genotype of snp == g" per sample, cases then controls, each
 // class padded to a multiple of 128 samples), their TMA descriptors and the
@@ -120,7 +120,16 @@ struct T3Plan {
     CUtensorMap map_l;    // box 128 B x 192 rows (256 when packed), 128-byte swizzle (l operand)
     CUtensorMap map_j;    // box 128 B x 64 rows, 128-byte swizzle (j rows of the (i,j) operand)
     CUtensorMap map_i;    // box 128 B x 2 rows, 128-byte swizzle (i rows)
+    // order 2: work items (64 i, 128 j) over i-tiles
+    long long* item2_begin = nullptr;
+    long long total2 = 0;
+    int n_itiles = 0;
+    double item2_combos = 0;
+    CUtensorMap map_a2;   // box 128 B x 128 rows (i rows)
+    CUtensorMap map_b2;   // box 128 B x 256 rows (j rows)
 };
+long long tensor_units(const T3Plan& plan, int order);
+double tensor_item_combos(const T3Plan& plan, int order);
 cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s);
 void tensor3_release(T3Plan& plan);
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,

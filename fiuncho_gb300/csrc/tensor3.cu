@@ -848,6 +848,338 @@ __global__ void __launch_bounds__(kPThreads, 1)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
+// ---------------------------------------------------------------------------
+// Order 2.  The 4 core cells of a pair (i, j) are plain dot products of two
+// plane rows, core[x][y] = sum_s a_ix(s) a_jy(s): a work item (64 i, 128 j)
+// is one GEMM D[(i,x), (j,y)] (M 128 x N 256) with both operands straight
+// from the operand planes by TMA -- no producer warps.  Both classes in one
+// accumulator when they pack (two alternating tensor-memory regions), else
+// cases in columns 0-255 and controls in 256-511 (the MMA then waits for the
+// epilogue between items).  4 stages of 48 KB; 8 epilogue warps.
+// Reference semantics: GenotypeTable::combine_and_popcnt for order 2
+// (src/base/gt_popcnt.cpp:4-35) over the pairs ThreadedSearch visits
+// (include/fiuncho/ThreadedSearch.h:157-180) with one worker.
+constexpr int kT2I = 64, kT2L = 128;                     // SNPs per tile
+constexpr int kT2M = 2 * kT2I, kT2N = 2 * kT2L;          // 128 x 256
+constexpr int kT2Stages = 4;
+constexpr int kT2SA = kT2M * kT3KB, kT2SB = kT2N * kT3KB;  // 16 KB, 32 KB
+constexpr int kT2Stage = kT2SA + kT2SB;                    // 48 KB
+constexpr int kT2Threads = 32 * (2 + kT3EpiWarps);         // 320
+constexpr size_t kT2Smem = 1024 + (size_t)kT2Stages * kT2Stage + (size_t)kT3EpiWarps * kT3Ebuf;
+constexpr uint32_t kT2Idesc = (1u << 4) | ((uint32_t)(kT2N >> 3) << 17) | ((uint32_t)(kT2M >> 4) << 24);
+static_assert(kT2Smem <= 227 * 1024 - 256, "order-2 tensor kernel shared memory");
+
+// Work items of i-tile a (i0 = 64 a): ceil((n-1-i0)/128) j-tiles at j0 = i0+1+128 b.
+__device__ __forceinline__ void t2_decode(const long long* __restrict__ item_begin, int n_itiles, long long g, int& i0,
+                                          int& j0) {
+    int lo = 0, hi = n_itiles - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (item_begin[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    i0 = kT2I * lo;
+    j0 = i0 + 1 + kT2L * (int)(g - item_begin[lo]);
+}
+
+// 16-byte chunk of the order-2 transpose buffer holding (cases y0, y1, controls
+// y0, y1) of row (ii, x) and column group k; conflict-free for the row-wise
+// writes (fixed k) and the pair-wise reads (fixed x, k = 4 kh + kk).
+__device__ __forceinline__ int t2_chunk(int ii, int k, int x) {
+    return (((ii * 8 + k) * 2 + x) ^ ((ii & 3) << 1) ^ ((k >> 2) & 1));
+}
+
+// Evaluates pair (i, j) from its transpose chunks: exact 9-cell tables from the
+// cores and the single cores, the bounded single-precision prefilter, the exact
+// fixed-point key for survivors, warp-aggregated append (every lane calls it).
+__device__ __forceinline__ void t2_eval(const ScanWork& w, const CandSink& sink, float thr_f, uint32_t* dump,
+                                        const uint32_t* __restrict__ single, const uint32_t* ebuf, int ii, int k,
+                                        int i, int j, bool i_ok, const float (&si)[2][2], int lane) {
+    const DevData& d = w.d;
+    const int n = d.snps;
+    const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
+    const float ncf[2] = {(float)d.n_cases, (float)d.n_ctrls};
+    const float tiny = 9.5367431640625e-07f;  // 2^-20: x*lg2(x + tiny) = 0 at x = 0
+    const bool valid = i_ok && j < n && j > i;
+    float t[2][9];
+#pragma unroll
+    for (int x = 0; x < 2; ++x) {
+        const uint4 c4 = *reinterpret_cast<const uint4*>(ebuf + 4 * t2_chunk(ii, k, x));
+        t[0][x * 3 + 0] = u2f(c4.x);
+        t[0][x * 3 + 1] = u2f(c4.y);
+        t[1][x * 3 + 0] = u2f(c4.z);
+        t[1][x * 3 + 1] = u2f(c4.w);
+    }
+    uint4 sj4 = make_uint4(0, 0, 0, 0);
+    if (valid) sj4 = __ldg(reinterpret_cast<const uint4*>(single) + j);
+    const float sj[2][2] = {{u2f(sj4.x), u2f(sj4.y)}, {u2f(sj4.z), u2f(sj4.w)}};
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+#pragma unroll
+        for (int x = 0; x < 2; ++x) t[c][x * 3 + 2] = si[c][x] - t[c][x * 3] - t[c][x * 3 + 1];
+#pragma unroll
+        for (int y = 0; y < 2; ++y) t[c][6 + y] = sj[c][y] - t[c][y] - t[c][3 + y];
+        t[c][8] = ncf[c] - si[c][0] - si[c][1] - t[c][6] - t[c][7];
+    }
+    float kf = 0.f;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+        const float a = t[0][c], bb = t[1][c], s = a + bb;
+        kf = fmaf(a, t3_lg2(a + tiny), kf);
+        kf = fmaf(bb, t3_lg2(bb + tiny), kf);
+        kf = fmaf(-s, t3_lg2(s + tiny), kf);
+    }
+    const bool cand = valid && (dump != nullptr || kf >= thr_f);
+    long long key = w.base_key;
+    bool pass = false;
+    if (cand) {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+            const uint32_t a = min(f2u(fmaxf(t[0][c], 0.f)), ncls[0]);
+            const uint32_t bb = min(f2u(fmaxf(t[1][c], 0.f)), ncls[1]);
+            key += __ldg(d.ftab + a) + __ldg(d.ftab + bb) - __ldg(d.ftab + a + bb);
+        }
+        pass = key >= sink.thr;
+        if (dump) {
+            uint32_t* o = dump + ((size_t)i * n + j) * 18;
+#pragma unroll
+            for (int c = 0; c < 9; ++c) {
+                o[c] = f2u(t[0][c]);
+                o[9 + c] = f2u(t[1][c]);
+            }
+        }
+    }
+    if (sink.evaluated) {
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0 && vmask) atomicAdd(sink.evaluated, (unsigned long long)__popc(vmask));
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, pass);
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(sink.count, (unsigned)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (pass) {
+            const unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (idx < sink.cap) {
+                const int cmb[2] = {i, j};
+                sink.buf[idx] = Cand{key, pack_code(cmb, 2, w.bits)};
+            } else {
+                atomicOr(sink.overflow, 1u);
+            }
+        }
+    }
+}
+
+struct T2Maps {
+    CUtensorMap a, b;
+};
+
+__global__ void __launch_bounds__(kT2Threads, 1)
+    tensor2_kernel(const __grid_constant__ T2Maps maps, ScanWork w, const long long* __restrict__ item_begin,
+                   int n_itiles, long long g0, long long g1, int k_cases, int pack, CandSink sink, float thr_f,
+                   uint32_t* dump, const uint32_t* __restrict__ single, int* status) {
+    extern __shared__ uint8_t smraw[];
+    __shared__ __align__(8) uint64_t full[kT2Stages], empty[kT2Stages];
+    __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);  // stages: A | B
+    uint32_t* ebuf_all = reinterpret_cast<uint32_t*>(sm + kT2Stages * kT2Stage);
+    volatile int* abort = &abort_flag;
+    const DevData& d = w.d;
+    const int n = d.snps;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ks_c = k_cases / kT3KB;
+    const int ksteps = ks_c + (d.tw + 1) / 2;
+    const int nbuf = pack ? 2 : 1;  // accumulator regions that alternate between items
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kT2Stages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[b])), "r"(kT3EpiWarps));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        abort_flag = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+
+    if (warp == 0) {
+        // ---------------------------------------------------------------- TMA producer
+        if (lane == 0) {
+            long long step = 0;
+            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+                int i0, j0;
+                t2_decode(item_begin, n_itiles, g, i0, j0);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const int s = (int)(step % kT2Stages);
+                    const long long u = step / kT2Stages;
+                    if (u > 0 && !t3_wait(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    const int k0 = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
+                    uint8_t* st = sm + s * kT2Stage;
+                    const uint32_t bar = smem_u32(&full[s]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                                 "r"((uint32_t)kT2Stage)
+                                 : "memory");
+                    t3_tma(smem_u32(st), &maps.a, k0, 2 * i0, bar);
+                    t3_tma(smem_u32(st + kT2SA), &maps.b, k0, 2 * j0, bar);
+                    ++step;
+                }
+            }
+            for (int s = 0; s < kT2Stages; ++s) {
+                if (step <= s) continue;
+                const long long last = s + ((step - 1 - s) / kT2Stages) * kT2Stages;
+                if (!t3_drain(smem_u32(&full[s]), (uint32_t)((last / kT2Stages) & 1))) ok = false;
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            long long step = 0, item = 0;
+            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+                const int buf = (int)(item % nbuf);
+                if (item >= nbuf &&
+                    !t3_wait(smem_u32(&acc_empty[buf]), (uint32_t)(((item / nbuf) - 1) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                    const int s = (int)(step % kT2Stages);
+                    if (!t3_wait(smem_u32(&full[s]), (uint32_t)((step / kT2Stages) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t sa = smem_u32(sm + s * kT2Stage), sb = sa + kT2SA;
+                    const int cls = ks >= ks_c;
+                    const uint32_t dcol = tmem + (uint32_t)(pack ? kT2N * buf : kT2N * cls);
+                    const bool first = pack ? ks == 0 : (ks == 0 || ks == ks_c);
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint64_t ad = t3_desc(sa + 32 * kk), bd = t3_desc(sb + 32 * kk);
+                        const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+                        asm volatile(
+                            "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
+                            "l"(ad), "l"(bd), "r"(kT2Idesc), "r"(acc));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                        smem_u32(&empty[s])));
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(&acc_full[buf])));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&done)));
+            if (!t3_drain(smem_u32(&done), 0)) ok = false;
+        }
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        const int e = warp - 2;     // 0..7
+        const int q = warp & 3;     // tensor-memory lane quarter this warp may access
+        const int hh = e >> 2;      // column half: j offsets [64 hh, 64 hh + 64)
+        uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+        const uint32_t wmask = pack ? (1u << pack) - 1u : 0xffffffffu;
+        const int ii = lane >> 1, x = lane & 1, kh = lane & 1;  // row (ii, x); pairs k = 4 kh + kk
+        long long item = 0;
+        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+            int i0, j0;
+            t2_decode(item_begin, n_itiles, g, i0, j0);
+            const int buf = (int)(item % nbuf);
+            const int i = i0 + 16 * q + ii;
+            const bool i_ok = i < n;
+            float si[2][2];
+            {
+                uint4 a = make_uint4(0, 0, 0, 0);
+                if (i_ok) a = __ldg(reinterpret_cast<const uint4*>(single) + i);
+                si[0][0] = u2f(a.x);
+                si[0][1] = u2f(a.y);
+                si[1][0] = u2f(a.z);
+                si[1][1] = u2f(a.w);
+            }
+            if (!t3_wait(smem_u32(&acc_full[buf]), (uint32_t)((item / nbuf) & 1), abort)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+            for (int cc = 0; cc < 8; ++cc) {
+                {
+                    const uint32_t col = (uint32_t)((pack ? kT2N * buf : 0) + 128 * hh + 16 * cc);
+                    uint32_t v[16], vt[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
+                        "15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(lane_base + col));
+                    if (!pack)
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%"
+                            "14,%15}, [%16];"
+                            : "=r"(vt[0]), "=r"(vt[1]), "=r"(vt[2]), "=r"(vt[3]), "=r"(vt[4]), "=r"(vt[5]),
+                              "=r"(vt[6]), "=r"(vt[7]), "=r"(vt[8]), "=r"(vt[9]), "=r"(vt[10]), "=r"(vt[11]),
+                              "=r"(vt[12]), "=r"(vt[13]), "=r"(vt[14]), "=r"(vt[15])
+                            : "r"(lane_base + (uint32_t)kT2N + col));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (cc == 7) {  // last read of this item's accumulators
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
+                                         : "memory");
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        uint4 c4;
+                        if (pack) {
+                            const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * k]));
+                            const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * k + 1]));
+                            c4 = make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                        } else {
+                            c4 = make_uint4(f2u(__uint_as_float(v[2 * k])), f2u(__uint_as_float(v[2 * k + 1])),
+                                            f2u(__uint_as_float(vt[2 * k])), f2u(__uint_as_float(vt[2 * k + 1])));
+                        }
+                        *reinterpret_cast<uint4*>(ebuf + 4 * t2_chunk(ii, k, x)) = c4;
+                    }
+                }
+                __syncwarp();
+#pragma unroll 1
+                for (int kk = 0; kk < 4; ++kk) {
+                    const int k = 4 * kh + kk;
+                    t2_eval(w, sink, thr_f, dump, single, ebuf, ii, k, i, j0 + 64 * hh + 8 * cc + k, i_ok, si, lane);
+                }
+                __syncwarp();
+            }
+        }
+    }
+    if (!ok) *abort = 1;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 0 && abort_flag) atomicOr(status, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
 // Operand planes: one thread per 16 output bytes (16 samples of one row).
 __global__ void t3_planes_kernel(DevData d, uint8_t* planes, int pitch, int k_cases, uint32_t ctrl_byte) {
     const long long chunks = (long long)pitch / 16;
@@ -876,6 +1208,20 @@ __global__ void t3_planes_kernel(DevData d, uint8_t* planes, int pitch, int k_ca
             pv[qd] = (((bits >> (4 * qd)) & 0xfu) * 0x00204081u & 0x01010101u) * (ctrl ? ctrl_byte : 0x38u);
         *reinterpret_cast<uint4*>(planes + (size_t)row * pitch + o) = v;
     }
+}
+
+// Order-2 items (host): prefix sums over i-tiles of their j-tiles; returns the total.
+static long long t2_items(int n, std::vector<long long>& item_begin) {
+    const int tiles = std::max(1, (n - 1 + kT2I - 1) / kT2I);
+    item_begin.assign((size_t)tiles + 1, 0);
+    long long total = 0;
+    for (int a = 0; a < tiles; ++a) {
+        item_begin[a] = total;
+        const int i0 = kT2I * a;
+        if (n - 1 - i0 > 0) total += (n - 1 - i0 + kT2L - 1) / kT2L;
+    }
+    item_begin[tiles] = total;
+    return total;
 }
 
 // Items per i (host): prefix sums item_begin[0..n], item_begin[n] = total.
@@ -948,14 +1294,30 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
     if ((e = t3_map(&plan.map_l, plan.planes, rows, plan.pitch, plan.pack ? kPN : kT3N, true)) != cudaSuccess)
         return e;
     if ((e = t3_map(&plan.map_j, plan.planes, rows, plan.pitch, 2 * kT3J, true)) != cudaSuccess) return e;
-    return t3_map(&plan.map_i, plan.planes, rows, plan.pitch, 2, true);
+    if ((e = t3_map(&plan.map_i, plan.planes, rows, plan.pitch, 2, true)) != cudaSuccess) return e;
+    // order 2
+    std::vector<long long> ib2;
+    plan.total2 = t2_items(d.snps, ib2);
+    plan.n_itiles = (int)ib2.size() - 1;
+    plan.item2_combos = kT2I * kT2L * 0.9;
+    e = cudaMalloc((void**)&plan.item2_begin, ib2.size() * sizeof(long long));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan.item2_begin, ib2.data(), ib2.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    if ((e = t3_map(&plan.map_a2, plan.planes, rows, plan.pitch, kT2M, true)) != cudaSuccess) return e;
+    return t3_map(&plan.map_b2, plan.planes, rows, plan.pitch, kT2N, true);
 }
+
+long long tensor_units(const T3Plan& plan, int order) { return order == 2 ? plan.total2 : plan.total; }
+double tensor_item_combos(const T3Plan& plan, int order) { return order == 2 ? plan.item2_combos : plan.item_combos; }
 
 void tensor3_release(T3Plan& plan) {
     cudaFree(plan.planes);
     cudaFree(plan.item_begin);
+    cudaFree(plan.item2_begin);
     plan.planes = nullptr;
     plan.item_begin = nullptr;
+    plan.item2_begin = nullptr;
 }
 
 // Bound on |single-precision estimate - exact key / (ln2 * 2^32)| over the 81
@@ -1014,6 +1376,8 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(tensor3p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tensor2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2Smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
@@ -1022,8 +1386,15 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     const double scale = 1.0 / (std::log(2.0) * 4294967296.0);
     const double thr = ((double)sink.thr - (double)w.base_key) * scale - t3_margin(w.d.n_cases + w.d.n_ctrls);
     const float thr_f = (float)std::max(-3.0e38, std::min(3.0e38, thr));
-    T3Maps maps{plan.map_l, plan.map_j, plan.map_i};
     const unsigned grid = (unsigned)(items < sms ? items : sms);
+    if (w.order == 2) {
+        T2Maps maps2{plan.map_a2, plan.map_b2};
+        tensor2_kernel<<<grid, kT2Threads, kT2Smem, s>>>(maps2, w, plan.item2_begin, plan.n_itiles, g0, g1,
+                                                         plan.k_cases, plan.pack, sink, thr_f, dump, single, status);
+        count_launch();
+        return cudaGetLastError();
+    }
+    T3Maps maps{plan.map_l, plan.map_j, plan.map_i};
     if (plan.pack)
         tensor3p_kernel<<<grid, kPThreads, kPSmem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, plan.pack,
                                                           sink, thr_f, dump, single, pairs, status);

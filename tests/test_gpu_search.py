@@ -65,7 +65,7 @@ def test_combine_and_popcnt_bit_exact(gs, oracle, golden_testdata):
     assert np.all(cc[27:] == 0) and np.all(tt[27:] == 0)
 
 
-@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 2), (3, 2), (2, 3), (3, 3), (3, 4)])
+@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 2), (3, 2), (2, 3), (3, 3), (2, 4), (3, 4)])
 def test_hot_kernel_tables_bit_exact_reference(gs, golden_testdata, order, kernel):
     """Each counting kernel's own contingency tables for EVERY combination of the
     reference's test data == the reference's combine_and_popcnt tables
@@ -249,7 +249,7 @@ def test_kernels_agree(oracle, n_case, n_ctrl, snps):
     ds = Dataset.from_genotypes(geno, is_case)
     for order in (2, 3):
         outs, tabs = [], []
-        for kernel in ((1, 2, 3) if order == 2 else (1, 2, 3, 4)):
+        for kernel in (1, 2, 3, 4):
             g = GpuSearch(0, kernel=kernel)
             res = Resident(g.ctx, ds)
             assert res.one_hot
@@ -277,11 +277,13 @@ def test_tensor_kernel_scope(gs, golden_synth):
     assert g.last_tile()[0] == 4
     g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
     assert g.last_tile()[0] in (2, 3)
+    g.run(res, 2, Distribution(ds.snps, 1), 10)
+    assert g.last_tile()[0] == 4
     g.set_kernel(4)
     with pytest.raises(FiunchoError):
         g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
     with pytest.raises(FiunchoError):
-        g.run(res, 2, Distribution(ds.snps, 1), 10)
+        g.run(res, 4, Distribution(ds.snps, 3), 10)
 
 
 def test_elided_rejects_non_one_hot(gs):
@@ -411,3 +413,51 @@ def test_tensor_prefilter_many_chunks(oracle):
     assert g.last_tile()[0] == 4
     assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
     _check_topn(oracle, ds, 3, 5, b[0], b[1], threads=16)
+
+
+@pytest.mark.parametrize("snps,n_case,n_ctrl", [(2, 1, 1), (3, 65, 63), (66, 130, 1), (129, 200, 129),
+                                                (130, 5000, 4100), (200, 100, 60000), (131, 1, 9000)])
+def test_tensor2_tile_edges(oracle, snps, n_case, n_ctrl):
+    """Order-2 tcgen05 kernel vs the full-table kernel around the 64 x 128 work item,
+    with classes that share one accumulator and classes that do not: identical tables
+    for every pair and identical top-N lists, checked against the oracle."""
+    from fiuncho_gb300 import Distribution, GpuSearch, Resident
+    ds = _one_hot_dataset(snps * 5 + n_ctrl, snps, n_case, n_ctrl)
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    dist = Distribution(snps, 1)
+    full = g.scan_tables(res, 2, dist, kernel=1)
+    tens = g.scan_tables(res, 2, dist, kernel=4)
+    mask = full != 0xFFFFFFFF
+    assert np.array_equal(tens[mask], full[mask])
+    out = min(30, math.comb(snps, 2))
+    g.set_kernel(1)
+    a = g.run(res, 2, dist, out, with_fp64=True)
+    g.set_kernel(4)
+    b = g.run(res, 2, dist, out, with_fp64=True)
+    assert g.last_tile() == (4, 256)
+    assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
+    _check_topn(oracle, ds, 2, out, b[0], b[1])
+
+
+def test_order2_40000x16000_top1000(oracle):
+    """Order 2 at full size (40 000 SNPs x 8 000/8 000 samples, 8e8 pairs, top-1 000): the
+    tcgen05 kernel and the reduced-work CUDA-core kernel give identical lists and FP64
+    values, and every returned MI equals the oracle's FP64 MI of its pair."""
+    from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident, synth
+    spec = synth.WORKLOADS["order2_40000x16000"]
+    geno, is_case, planted = synth.simulate(spec)
+    ds = Dataset.from_genotypes(geno, is_case)
+    del geno
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    dist = Distribution(ds.snps, 1)
+    g.set_kernel(4)
+    a, av = g.run(res, 2, dist, 1000, with_fp64=True)
+    g.set_kernel(3)
+    b, bv = g.run(res, 2, dist, 1000, with_fp64=True)
+    assert [x.combination for x in a] == [x.combination for x in b] and np.array_equal(av, bv)
+    ex = exact_mi(oracle, ds.data, ds.cases_words, ds.ctrls_words, ds.cases, ds.ctrls, 2,
+                  [x.combination for x in a])
+    assert np.allclose(av, ex, rtol=1e-9, atol=0)
+    assert_sorted_desc(av)
