@@ -96,26 +96,38 @@ int make_work(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_d
     return FIU_OK;
 }
 
+// Triple cores of the order-4 reduced-work kernel are kept up to this size
+// (C(n,3) x 32 bytes: about 1 150 SNPs); larger data sets use the full kernel.
+constexpr size_t kMaxTriplesBytes = 8ull << 30;
+
 // Chooses the counting kernel of a request and makes sure its tables exist.
 int choose_kernel(fiu_ctx* ctx, const fiu_resident* res_c, unsigned order, int requested, int& kernel) {
     fiu_resident* res = const_cast<fiu_resident*>(res_c);
-    const bool elided_ok = res->one_hot && (order == 2 || order == 3) && res->d.n_cases <= 65535 &&
-                           res->d.n_ctrls <= 65535 && elided_smem(order, res->d.cw, res->d.tw) <= 160 * 1024;
-    kernel = requested ? requested : (elided_ok ? FIU_KERNEL_ELIDED_HS : FIU_KERNEL_FULL);
+    const bool classes_ok = res->one_hot && res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535;
+    const bool elided_ok =
+        classes_ok && (((order == 2 || order == 3) && elided_smem(order, res->d.cw, res->d.tw) <= 160 * 1024) ||
+                       (order == 4 && res->d.snps >= 4 && elided4_smem(res->d.cw, res->d.tw) <= 160 * 1024 &&
+                        triples_bytes(res->d.snps) <= kMaxTriplesBytes));
+    // measured: Harley-Seal counting wins at orders 2-3, plain POPC at order 4
+    // (its 16 Harley-Seal counters do not fit two CTAs per SM)
+    kernel = requested ? requested
+                       : (elided_ok ? (order == 4 ? FIU_KERNEL_ELIDED_POPC : FIU_KERNEL_ELIDED_HS) : FIU_KERNEL_FULL);
     if (kernel < FIU_KERNEL_FULL || kernel > FIU_KERNEL_TENSOR) return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
     if (kernel == FIU_KERNEL_TENSOR && order != 2 && order != 3)
         return fail(ctx, FIU_ERR_UNSUPPORTED, "the tensor-core kernels serve orders 2 and 3");
     if (kernel == FIU_KERNEL_FULL) return FIU_OK;
     if (!elided_ok)
-        return fail(ctx, FIU_ERR_UNSUPPORTED, "elided kernels need one-hot data, order 2 or 3, classes <= 65535");
-    if (!res->single || (order == 3 && !res->pairs)) {
+        return fail(ctx, FIU_ERR_UNSUPPORTED,
+                    "elided kernels need one-hot data, order 2, 3 or 4 (at most 1 150 SNPs), classes <= 65535");
+    const bool need_pairs = order >= 3 && !res->pairs, need_triples = order == 4 && !res->triples;
+    if (!res->single || need_pairs || need_triples) {
         const long long np = (long long)res->d.snps * (res->d.snps - 1) / 2;
         cudaError_t e = cudaSuccess;
         if (!res->single) e = cudaMalloc((void**)&res->single, (size_t)res->d.snps * 4 * sizeof(uint32_t));
-        if (e == cudaSuccess && order == 3 && !res->pairs && np > 0)
-            e = cudaMalloc((void**)&res->pairs, (size_t)np * sizeof(uint4));
-        if (e == cudaSuccess)
-            e = build_cores(res->d, res->single, order == 3 ? res->pairs : nullptr, ctx->sms, ctx->stream);
+        if (e == cudaSuccess && need_pairs && np > 0) e = cudaMalloc((void**)&res->pairs, (size_t)np * sizeof(uint4));
+        if (e == cudaSuccess) e = build_cores(res->d, res->single, need_pairs ? res->pairs : nullptr, ctx->sms, ctx->stream);
+        if (e == cudaSuccess && need_triples) e = cudaMalloc((void**)&res->triples, triples_bytes(res->d.snps));
+        if (e == cudaSuccess && need_triples) e = build_triples(res->d, res->triples, ctx->sms, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "core tables");
     }
@@ -125,6 +137,9 @@ int choose_kernel(fiu_ctx* ctx, const fiu_resident* res_c, unsigned order, int r
 cudaError_t launch_kernel(int kernel, int tp, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
                           const CandSink& sink, uint32_t* dump, cudaStream_t s, int sms) {
     if (kernel == FIU_KERNEL_FULL) return launch_count(tp, w, m0, m1, sink, dump, s, sms);
+    if (w.order == 4)
+        return launch_elided4(kernel == FIU_KERNEL_ELIDED_HS, tp, w, m0, m1, sink, dump, res->single, res->pairs,
+                              res->triples, s, sms);
     return launch_elided(kernel == FIU_KERNEL_ELIDED_HS, tp, w, m0, m1, sink, dump, res->single, res->pairs, s, sms);
 }
 
@@ -134,7 +149,7 @@ static size_t group_smem(int kernel, const ScanWork& w) {
         for (int t = 0; t < w.order - 1; ++t) rows *= 3;
         return (size_t)(rows < 9 ? rows : 9) * 64 * sizeof(uint64_t);
     }
-    return elided_smem(w.order, w.d.cw, w.d.tw);
+    return w.order == 4 ? elided4_smem(w.d.cw, w.d.tw) : elided_smem(w.order, w.d.cw, w.d.tw);
 }
 
 static bool tile_ok(int kernel, int tp, const ScanWork& w) {
@@ -530,6 +545,7 @@ void fiu_dataset_free(fiu_ctx* ctx, fiu_resident* r) {
     cudaFree(r->ftab);
     cudaFree(r->single);
     cudaFree(r->pairs);
+    cudaFree(r->triples);
     if (r->t3) {
         tensor3_release(*r->t3);
         delete r->t3;

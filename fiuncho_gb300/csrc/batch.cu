@@ -11,7 +11,7 @@
 // Reference semantics per scan are those of the single-scan path
 // (ThreadedSearch::run, include/fiuncho/ThreadedSearch.h:207-246; MaxArray,
 // include/fiuncho/utils/MaxArray.h:31-46), with the same total order.
-#include "elided_prefix.cuh"
+#include "elided4_prefix.cuh"
 #include "full_prefix.cuh"
 #include "topn_dev.cuh"
 
@@ -23,7 +23,8 @@ static_assert(kRoundThreads == kThreads && kRoundThreads == kEThreads, "one bloc
 // Round kernels are specialised per family and per l-tile width TP so that
 // each keeps the registers of its own prefix bodies: family 0 = reduced-work
 // kernels (orders 2-3, Harley-Seal counting), family 1 = full-table kernel
-// (orders 2-4; higher orders take the single-scan path).  A CTA holds
+// (orders 2-4; higher orders take the single-scan path), family 2 = the
+// order-4 reduced-work kernel (POPC counting).  A CTA holds
 // 256 / TP groups, each working on its own prefix.
 template <int FAMILY, int TP>
 __device__ __forceinline__ void run_prefix(const ScanDesc& sd, long long m, const CandSink& sink, uint64_t* sm,
@@ -31,6 +32,8 @@ __device__ __forceinline__ void run_prefix(const ScanDesc& sd, long long m, cons
     if (FAMILY == 0) {
         if (sd.w.order == 2) elided_prefix<2, true, TP>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sm, grp);
         else elided_prefix<3, true, TP>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sm, grp);
+    } else if (FAMILY == 2) {
+        elided4_prefix<false, TP>(sd.w, m, sink, nullptr, sd.single, sd.pairs, sd.triples, sm, grp);
     } else {
         switch (sd.w.order) {
             case 2: full_prefix<2, TP>(sd.w, m, sink, nullptr, sm, grp); break;
@@ -44,6 +47,7 @@ __device__ __forceinline__ void run_prefix(const ScanDesc& sd, long long m, cons
 // Shared-memory words of one group for a scan.
 __host__ __device__ inline size_t group_words(const ScanDesc& sd) {
     if (sd.kind == FIU_KERNEL_FULL_ID) return (size_t)full_group_words(sd.w.order);
+    if (sd.w.order == 4) return elided4_words(sd.w.d.cw, sd.w.d.tw);
     return (size_t)(1 << (sd.w.order - 1)) * (sd.w.d.cw + sd.w.d.tw);
 }
 
@@ -76,8 +80,8 @@ __global__ void __launch_bounds__(kRoundThreads, 2) round_kernel(const ScanDesc*
     }
 }
 
-static size_t g_round_attr[2][4] = {};
-static int g_round_per_sm[2][4] = {};
+static size_t g_round_attr[3][4] = {};
+static int g_round_per_sm[3][4] = {};
 static bool g_select_attr = false, g_finish_attr = false;
 
 __global__ void select_scans_kernel(const ScanDesc* __restrict__ scans, ScanState* states, int final_pass);
@@ -86,11 +90,13 @@ __global__ void finish_scans_kernel(const ScanDesc* __restrict__ scans, ScanStat
 static int tp_index(int tp) { return tp == 32 ? 0 : tp == 64 ? 1 : tp == 128 ? 2 : 3; }
 
 static const void* round_fn(int family, int ti) {
-    static const void* fns[2][4] = {
+    static const void* fns[3][4] = {
         {(const void*)round_kernel<0, 32>, (const void*)round_kernel<0, 64>, (const void*)round_kernel<0, 128>,
          (const void*)round_kernel<0, 256>},
         {(const void*)round_kernel<1, 32>, (const void*)round_kernel<1, 64>, (const void*)round_kernel<1, 128>,
-         (const void*)round_kernel<1, 256>}};
+         (const void*)round_kernel<1, 256>},
+        {(const void*)round_kernel<2, 32>, (const void*)round_kernel<2, 64>, (const void*)round_kernel<2, 128>,
+         (const void*)round_kernel<2, 256>}};
     return fns[family][ti];
 }
 
@@ -98,7 +104,7 @@ static const void* round_fn(int family, int ti) {
 // inside a stream capture) and caches the round kernels' occupancy.
 cudaError_t prepare_round_kernels(size_t smem) {
     cudaError_t e = cudaSuccess;
-    for (int f = 0; f < 2; ++f)
+    for (int f = 0; f < 3; ++f)
         for (int t = 0; t < 4; ++t) {
             if (smem > g_round_attr[f][t] || !g_round_per_sm[f][t]) {
                 const size_t want = smem > g_round_attr[f][t] ? smem : g_round_attr[f][t];
@@ -137,13 +143,20 @@ cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* s
                          int n_ents, long long total, size_t smem, int sms, cudaStream_t s) {
     if (total <= 0 || n_ents <= 0) return cudaSuccess;
     const int ti = tp_index(tp);
-    if (family < 0 || family > 1 || smem > g_round_attr[family][ti] || !g_round_per_sm[family][ti])
+    if (family < 0 || family > 2 || smem > g_round_attr[family][ti] || !g_round_per_sm[family][ti])
         return cudaErrorInvalidConfiguration;  // prepare_round_kernels first
     const long long G = kRoundThreads / tp;
     const long long ctas = (total + G - 1) / G, cap = (long long)sms * g_round_per_sm[family][ti];
     const unsigned grid = (unsigned)(ctas < cap ? ctas : cap);
     const size_t sm = g_round_attr[family][ti];
-    if (family == 0) {
+    if (family == 2) {
+        switch (ti) {
+            case 0: launch_round_t<2, 32>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 1: launch_round_t<2, 64>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 2: launch_round_t<2, 128>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            default: launch_round_t<2, 256>(grid, sm, scans, states, ents, n_ents, total, s); break;
+        }
+    } else if (family == 0) {
         switch (ti) {
             case 0: launch_round_t<0, 32>(grid, sm, scans, states, ents, n_ents, total, s); break;
             case 1: launch_round_t<0, 64>(grid, sm, scans, states, ents, n_ents, total, s); break;

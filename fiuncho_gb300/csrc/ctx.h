@@ -51,7 +51,8 @@ struct fiu_resident {
     int one_hot = 0;
     int device = 0;
     uint32_t* single = nullptr;  // single-SNP cores (elided kernels)
-    uint4* pairs = nullptr;      // pair cores (elided order-3 kernel)
+    uint4* pairs = nullptr;      // pair cores (elided order-3 and order-4 kernels)
+    uint4* triples = nullptr;    // triple cores (elided order-4 kernel)
     fiu::T3Plan* t3 = nullptr;  // operand planes and work items of the tensor order-3 kernel
 };
 

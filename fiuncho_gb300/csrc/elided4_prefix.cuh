@@ -1,0 +1,268 @@
+// Per-prefix body of the order-4 reduced-work counting kernel, shared by
+// elided4.cu (single scan) and batch.cu (round kernel).
+//
+// For one-hot data a combination (i, j, k, l) is counted on its 16 core cells
+// per class -- genotypes x, y, z, w in {0, 1} -- from the 8 prefix rows
+// (x, y, z) of (i, j, k), staged in shared memory, and the last SNP's rows 0
+// and 1; the other 65 cells follow exactly (the genotype-2 slice of an axis is
+// the marginal minus its 0 and 1 slices).  Slice w in {0, 1} of the 81-cell
+// table is an order-3 derivation whose pair-like marginals are the cores of
+// the triples (i,j,l), (i,k,l), (j,k,l) at w, whose single-like marginals are
+// the cores of the pairs (i,l), (j,l), (k,l) at w and whose size is l's core
+// w; slice w = 2 is the full table of the prefix triple (i, j, k) minus slices
+// 0 and 1.  The MI key is accumulated in three streaming passes over the 81
+// cells -- cases, controls, totals -- (the derivation is linear, so the totals
+// table is the derivation of the summed cores) with at most two slices live
+// in registers.  The tables are identical to combine_and_popcnt's
+// (src/base/gt_popcnt.cpp:4-35) for one-hot data.
+#pragma once
+
+#include "elided_prefix.cuh"
+
+namespace fiu {
+
+// Lexicographic rank of the triple i < j < k among the triples of n SNPs:
+// C(n,3) - C(n-i,3) triples start below i, then the pair (j, k) among the
+// n-i-1 SNPs after i.
+__host__ __device__ __forceinline__ long long triple_index(int i, int j, int k, int n) {
+    auto c3 = [](long long m) { return m < 3 ? 0ll : m * (m - 1) * (m - 2) / 6; };
+    const long long m = n - i - 1, a = j - i - 1, b = k - i - 1;
+    return c3(n) - c3(n - i) + a * (2 * m - a - 1) / 2 + (b - a - 1);
+}
+
+// Shared-memory words of one group: 8 prefix rows of cw + tw words, then the
+// prefix triple's full table for cases, controls and totals (81 uint32).
+__host__ __device__ inline size_t elided4_words(int cw, int tw) { return 8 * (size_t)(cw + tw) + 41; }
+
+// The star table of three SNPs holds at (a, b, c), a, b, c in {0, 1, 2}
+// ((a*3+b)*3+c; 2 = any genotype), the core count of the SNPs not at "any".
+// Subtracting the 0 and 1 slices from the "any" slice, axis by axis, turns it
+// in place into the contingency table t[(x*3+y)*3+z].
+__device__ __forceinline__ void star_to_table(uint32_t* t) {
+#pragma unroll
+    for (int xy = 0; xy < 9; ++xy) t[xy * 3 + 2] -= t[xy * 3 + 0] + t[xy * 3 + 1];
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int z = 0; z < 3; ++z) t[(x * 3 + 2) * 3 + z] -= t[(x * 3 + 0) * 3 + z] + t[(x * 3 + 1) * 3 + z];
+#pragma unroll
+    for (int yz = 0; yz < 9; ++yz) t[18 + yz] -= t[yz] + t[9 + yz];
+}
+
+// Cell (x, y, z) of one class's triple word (8 uint16: [x][y][z]).
+__device__ __forceinline__ uint32_t tcell(const uint4& v, int x, int y, int z) {
+    const int q = x * 4 + y * 2 + z;
+    const uint32_t wv = (&v.x)[q >> 1];
+    return (q & 1) ? (wv >> 16) : (wv & 0xffffu);
+}
+
+// Value of pass PC (0 cases, 1 controls, 2 both classes summed) from a
+// per-class pair of values.
+template <int PC>
+__device__ __forceinline__ uint32_t by_pass(uint32_t a, uint32_t b) {
+    return PC == 0 ? a : PC == 1 ? b : a + b;
+}
+
+// Locations of the sub-combination cores of one combination (i, j, k, l).
+struct E4Src {
+    const uint4* tij;  // triple (i,j,l): two words, cases then controls
+    const uint4* tik;  // triple (i,k,l)
+    const uint4* tjk;  // triple (j,k,l)
+    uint4 pil, pjl, pkl;  // pairs (i,l), (j,l), (k,l): [class][x][y] uint16
+    uint4 sl;             // single l: [class][x]
+};
+
+// One pass of the MI key over the 81 cells: the slices l = 0, 1, 2, each an
+// order-3 derivation from its star table (slice 2's is the prefix's star
+// table minus slices 0 and 1: the derivation is linear).  Returns the sum of T[cell] over
+// the pass's 81 cells; writes the cells to o[((x*3+y)*3+z)*3 + w] if o.
+// The counted cores arrive packed: cp[cls][r] = core (r, w=0) | core (r, w=1) << 16.
+template <int PC>
+__device__ __forceinline__ long long e4_pass(const uint32_t (&cp)[2][8], const E4Src& src,
+                                             const uint32_t* __restrict__ pstar, const long long* __restrict__ ftab,
+                                             uint32_t nc, uint32_t* o) {
+    uint4 ta[3], tb[3];  // triple words of the pass's class(es)
+    {
+        const uint4* tp[3] = {src.tij, src.tik, src.tjk};
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+            ta[u] = __ldg(tp[u] + (PC == 1 ? 1 : 0));
+            tb[u] = PC == 2 ? __ldg(tp[u] + 1) : make_uint4(0, 0, 0, 0);
+        }
+    }
+    // ta holds the pass's class (controls for PC 1), tb the controls for PC 2
+    auto tri = [&](int u, int x, int y, int z) {
+        return PC == 2 ? tcell(ta[u], x, y, z) + tcell(tb[u], x, y, z) : tcell(ta[u], x, y, z);
+    };
+    auto pr = [&](const uint4& v, int x, int y) { return by_pass<PC>(pcore(v, 0, x, y), pcore(v, 1, x, y)); };
+    auto star = [&](int w, int q) -> uint32_t {
+        const int a = q / 9, b = (q / 3) % 3, z = q % 3;
+        if (a < 2 && b < 2 && z < 2) {
+            const int r = (a * 2 + b) * 2 + z;
+            return by_pass<PC>(w ? cp[0][r] >> 16 : cp[0][r] & 0xffffu, w ? cp[1][r] >> 16 : cp[1][r] & 0xffffu);
+        }
+        if (a < 2 && b < 2) return tri(0, a, b, w);
+        if (a < 2 && z < 2) return tri(1, a, z, w);
+        if (b < 2 && z < 2) return tri(2, b, z, w);
+        if (a < 2) return pr(src.pil, a, w);
+        if (b < 2) return pr(src.pjl, b, w);
+        if (z < 2) return pr(src.pkl, z, w);
+        return by_pass<PC>(w ? src.sl.y : src.sl.x, w ? src.sl.w : src.sl.z);
+    };
+    long long part = 0;
+#pragma unroll
+    for (int sw = 0; sw < 3; ++sw) {
+        uint32_t t[27];
+#pragma unroll
+        for (int q = 0; q < 27; ++q) t[q] = sw < 2 ? star(sw, q) : pstar[q] - star(0, q) - star(1, q);
+        star_to_table(t);
+        // derived cells of consistent one-hot data never exceed the class
+        // size; the clamp keeps any inconsistency inside the table
+#pragma unroll
+        for (int q = 0; q < 27; ++q) part += __ldg(ftab + min(t[q], nc));
+        if (PC < 2 && o) {
+#pragma unroll
+            for (int q = 0; q < 27; ++q) o[PC * 81 + q * 3 + sw] = t[q];
+        }
+    }
+    return part;
+}
+
+// One prefix (owned ordinal m): the TP threads of group grp, one last SNP per
+// thread; sp holds elided4_words(cw, tw) words.  Synchronises the group only.
+template <bool HS, int TP>
+__device__ __forceinline__ void elided4_prefix(const ScanWork& w, long long m, const CandSink& sink, uint32_t* dump,
+                                               const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
+                                               const uint4* __restrict__ triples, uint64_t* sp, int grp) {
+    const DevData& d = w.d;
+    const int S = d.snps, WT = d.cw + d.tw;
+    const size_t per_snp = 3 * (size_t)WT;
+    const int lane = threadIdx.x & 31;
+    const int gt = threadIdx.x % TP;
+    const uint4* single4 = reinterpret_cast<const uint4*>(single);
+    uint32_t* ptab = reinterpret_cast<uint32_t*>(sp + 8 * (size_t)WT);
+    int c[4];
+    unrank((long long)w.dist_offset + m * (long long)w.dist_step, w.dist_n, 3, c);
+    const int last = c[2];
+    if (last + 1 >= S) return;  // uniform across the group
+    if (sink.evaluated && gt == 0) atomicAdd(sink.evaluated, (unsigned long long)(S - 1 - last));
+    group_sync<TP>(grp);
+    for (int e = gt; e < 8 * WT; e += TP) {
+        const int r = e / WT, ww = e - r * WT;
+        const bool cls = ww >= d.cw;
+        const int W = cls ? d.tw : d.cw, wd = cls ? ww - d.cw : ww;
+        const size_t off = (cls ? 3 * (size_t)d.cw : 0) + (size_t)wd;
+        sp[e] = __ldg(d.ref + (size_t)c[0] * per_snp + off + (size_t)(r >> 2) * W) &
+                __ldg(d.ref + (size_t)c[1] * per_snp + off + (size_t)((r >> 1) & 1) * W) &
+                __ldg(d.ref + (size_t)c[2] * per_snp + off + (size_t)(r & 1) * W);
+    }
+    if (gt == 0) {  // star table of the prefix triple, per pass
+        const long long ti = triple_index(c[0], c[1], c[2], S);
+        const uint4 tc[2] = {__ldg(triples + 2 * ti), __ldg(triples + 2 * ti + 1)};
+        const uint4 p01 = __ldg(pairs + pair_index(c[0], c[1], S)), p02 = __ldg(pairs + pair_index(c[0], c[2], S)),
+                    p12 = __ldg(pairs + pair_index(c[1], c[2], S));
+        const uint4 sv[3] = {__ldg(single4 + c[0]), __ldg(single4 + c[1]), __ldg(single4 + c[2])};
+        const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
+#pragma unroll
+        for (int cls = 0; cls < 2; ++cls)
+#pragma unroll
+            for (int q = 0; q < 27; ++q) {
+                const int a = q / 9, b = (q / 3) % 3, z = q % 3;
+                uint32_t v;
+                if (a < 2 && b < 2 && z < 2) v = tcell(tc[cls], a, b, z);
+                else if (a < 2 && b < 2) v = pcore(p01, cls, a, b);
+                else if (a < 2 && z < 2) v = pcore(p02, cls, a, z);
+                else if (b < 2 && z < 2) v = pcore(p12, cls, b, z);
+                else if (a < 2) v = (&sv[0].x)[cls * 2 + a];
+                else if (b < 2) v = (&sv[1].x)[cls * 2 + b];
+                else if (z < 2) v = (&sv[2].x)[cls * 2 + z];
+                else v = ncls[cls];
+                ptab[27 * cls + q] = v;
+            }
+#pragma unroll 1
+        for (int q = 0; q < 27; ++q) ptab[54 + q] = ptab[q] + ptab[27 + q];
+    }
+    group_sync<TP>(grp);
+
+    for (int l0 = last + 1; l0 < S; l0 += TP) {
+        const int l = l0 + gt;
+        const bool valid = l < S;
+        long long key = w.base_key;
+        if (valid) {
+            uint32_t cnt[2][16];
+#pragma unroll
+            for (int cls = 0; cls < 2; ++cls) {
+                const int W = cls ? d.tw : d.cw;
+                const uint64_t* L = d.tr + (size_t)(cls ? 3 * d.cw : 0) * S + l;
+                const uint64_t* pr = sp + (cls ? d.cw : 0);
+                int wq = 0;
+                if (HS) {
+                    HSCounter hc[16];
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) hc[q].zero();
+                    for (; wq + 8 <= W; wq += 8) {
+#pragma unroll
+                        for (int z = 0; z < 2; ++z) {
+                            uint64_t lz[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) lz[k] = __ldg(L + (size_t)(z * W + wq + k) * S);
+#pragma unroll
+                            for (int r = 0; r < 8; ++r) hc[r * 2 + z].add8(pr + r * WT + wq, lz);
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) cnt[cls][q] = hc[q].value();
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) cnt[cls][q] = 0;
+                }
+                for (; wq < W; ++wq) {
+                    const uint64_t l0v = __ldg(L + (size_t)wq * S), l1v = __ldg(L + (size_t)(W + wq) * S);
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) {
+                        const uint64_t p = pr[r * WT + wq];
+                        cnt[cls][r * 2 + 0] += __popcll(p & l0v);
+                        cnt[cls][r * 2 + 1] += __popcll(p & l1v);
+                    }
+                }
+            }
+            uint32_t cp[2][8];  // cores <= class size <= 65535
+#pragma unroll
+            for (int cls = 0; cls < 2; ++cls)
+#pragma unroll
+                for (int r = 0; r < 8; ++r) cp[cls][r] = cnt[cls][r * 2] | (cnt[cls][r * 2 + 1] << 16);
+            E4Src src;
+            src.tij = triples + 2 * triple_index(c[0], c[1], l, S);
+            src.tik = triples + 2 * triple_index(c[0], c[2], l, S);
+            src.tjk = triples + 2 * triple_index(c[1], c[2], l, S);
+            src.pil = __ldg(pairs + pair_index(c[0], l, S));
+            src.pjl = __ldg(pairs + pair_index(c[1], l, S));
+            src.pkl = __ldg(pairs + pair_index(c[2], l, S));
+            src.sl = __ldg(single4 + l);
+            uint32_t* o = dump ? dump + ((size_t)m * S + l) * 2 * 81 : nullptr;
+            // key = base + sum over the 81 cells of T[case] + T[control] - T[total]
+            key += e4_pass<0>(cp, src, ptab, d.ftab, d.n_cases, o);
+            key += e4_pass<1>(cp, src, ptab + 27, d.ftab, d.n_ctrls, o);
+            key -= e4_pass<2>(cp, src, ptab + 54, d.ftab, d.n_cases + d.n_ctrls, o);
+        }
+        const bool pass = valid && key >= sink.thr;
+        const unsigned mask = __ballot_sync(0xffffffffu, pass);
+        if (mask) {
+            const int leader = __ffs(mask) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(sink.count, (unsigned)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (pass) {
+                const unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+                if (idx < sink.cap) {
+                    c[3] = l;
+                    sink.buf[idx] = Cand{key, pack_code(c, 4, w.bits)};
+                } else {
+                    atomicOr(sink.overflow, 1u);
+                }
+            }
+        }
+    }
+}
+
+}  // namespace fiu

@@ -4,6 +4,9 @@
 // scan gets a threshold early and later rounds admit few candidates.  A scan
 // whose candidate buffer overflowed is re-run alone on the single-scan path
 // (whose chunking adapts on the host), so results never depend on batching.
+// Scans served by the tensor-core kernels (one-hot order 2 or 3 over the whole
+// data set) are not split into rounds: they run alone, one after the other,
+// as they would in a loop of single calls.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -54,11 +57,12 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
         }
         if (sc.outputs == 0 || w.n_prefixes == 0) continue;
         int kind = 0, tp = 256;
-        if ((rc = choose_tile(ctx, sc.res, w, ctx->kernel, kind, tp))) {
+        if ((rc = choose_tile(ctx, sc.res, w, ctx->kernel, kind, tp, true))) {
             sc.status = rc;
             continue;
         }
-        if (kind == FIU_KERNEL_FULL && sc.order > 4) {
+        // tensor-core scans and full-table scans above order 4 run alone
+        if (kind == FIU_KERNEL_TENSOR || (kind == FIU_KERNEL_FULL && sc.order > 4)) {
             single_path.push_back(i);
             continue;
         }
@@ -85,8 +89,8 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
     }
     const int n = (int)plans.size();
     if (n > 0) {
-        // ---- round schedule: per round, the entries of family 0 (reduced-work
-        // kernels) then family 1 (full-table kernel), each with its own item space
+        // ---- round schedule: per round, the entries of each kernel family
+        // (round_family) and l-tile width, each group with its own item space
         std::vector<RoundEntry> ents;
         std::vector<size_t> grp_first;      // entries of group g = [grp_first[g], grp_first[g+1])
         std::vector<long long> grp_total;   // items of group g
@@ -105,12 +109,12 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
                 const long long left = plans[s].w.n_prefixes - cursor[s];
                 if (left > 0) take[s] = std::min(left, chunk[s]);
             }
-            for (int fam = 0; fam < 2; ++fam)
+            for (int fam = 0; fam < kRoundFamilies; ++fam)
                 for (int tp : {32, 64, 128, 256}) {
                     long long total = 0;
                     grp_first.push_back(ents.size());
                     for (int s = 0; s < n; ++s) {
-                        if (!take[s] || (plans[s].kind == FIU_KERNEL_FULL) != (fam == 1) || plans[s].tp != tp)
+                        if (!take[s] || round_family(plans[s].kind, plans[s].w.order) != fam || plans[s].tp != tp)
                             continue;
                         ents.push_back(RoundEntry{s, 0, cursor[s], total});
                         total += take[s];
@@ -151,6 +155,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             d.outputs = p.outputs;
             d.single = p.res->single;
             d.pairs = p.res->pairs;
+            d.triples = p.res->triples;
             d.cand = (Cand*)(base + off_bufs + p.off_cand);
             d.scored = (ScoredRec*)(base + off_bufs + p.off_scored);
             d.out_comb = (int*)(base + off_bufs + p.off_comb);

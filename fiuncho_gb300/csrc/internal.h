@@ -37,6 +37,7 @@ struct ScanDesc {  // per scan, read-only on the device
     unsigned outputs;
     const uint32_t* single;
     const uint4* pairs;
+    const uint4* triples;  // order-4 reduced-work kernel only
     Cand* cand;        // [cap]
     ScoredRec* scored; // [keep]
     int* out_comb;     // [outputs * order]
@@ -62,7 +63,10 @@ struct RoundEntry {  // owned prefix ordinals [m0, m0 + n) of scan `scan`, items
 
 // batch.cu
 size_t round_smem(const ScanDesc& sd);
-// family: 0 reduced-work kernels (orders 2-3), 1 full table (orders 2-4); tp as in ScanDesc.
+// family: 0 reduced-work kernels (orders 2-3), 1 full table (orders 2-4), 2 reduced-work
+// kernel at order 4; tp as in ScanDesc.
+constexpr int kRoundFamilies = 3;
+inline int round_family(int kind, int order) { return kind == FIU_KERNEL_FULL_ID ? 1 : order == 4 ? 2 : 0; }
 cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* states, const RoundEntry* ents,
                          int n_ents, long long total, size_t smem, int sms, cudaStream_t s);
 cudaError_t launch_select_scans(const ScanDesc* scans, ScanState* states, int n_scans, int final_pass,
@@ -103,6 +107,14 @@ cudaError_t build_cores(const DevData& d, uint32_t* single, uint4* pairs, int sm
 size_t elided_smem(int order, int cw, int tw);
 cudaError_t launch_elided(bool hs, int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
                           uint32_t* dump, const uint32_t* single, const uint4* pairs, cudaStream_t s, int sms);
+
+// elided4.cu -- reduced-work kernel for one-hot data, order 4 (reads triple cores).
+size_t triples_bytes(int snps);
+cudaError_t build_triples(const DevData& d, uint4* triples, int sms, cudaStream_t s);
+size_t elided4_smem(int cw, int tw);
+cudaError_t launch_elided4(bool hs, int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
+                           uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
+                           cudaStream_t s, int sms);
 
 // tensor3.cu -- order-2 and order-3 core cells on tcgen05 (one-hot data, whole data set, one worker).
 // Device state of the tensor kernel for one data set: the e4m3 operand planes

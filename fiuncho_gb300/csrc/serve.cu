@@ -10,7 +10,9 @@
 // large scan does not hold small ones back), then one selection CTA per slot
 // raises thresholds on the device.  Scans whose last chunk ran are finalised
 // (FP64 re-score + top-N), copied out, and release their memory and slot;
-// scans that arrived meanwhile are admitted before the next round.
+// scans that arrived meanwhile are admitted before the next round.  A scan
+// served by the tensor-core kernels (one-hot order 2 or 3 over the whole data
+// set) runs alone on admission, between two rounds.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -148,11 +150,11 @@ bool admit(fiu_server* sv, ServeScan* s) {
         finish(sv, s, FIU_OK);
         return false;
     }
-    if ((rc = choose_tile(ctx, s->res, s->w, ctx->kernel, s->kind, s->tp))) {
+    if ((rc = choose_tile(ctx, s->res, s->w, ctx->kernel, s->kind, s->tp, true))) {
         finish(sv, s, rc);
         return false;
     }
-    if ((s->kind == FIU_KERNEL_FULL && s->order > 4) || sv->free_slots.empty()) {
+    if (s->kind == FIU_KERNEL_TENSOR || (s->kind == FIU_KERNEL_FULL && s->order > 4) || sv->free_slots.empty()) {
         // outside the round kernels: the single-scan path, right now
         rc = search_impl(ctx, s->res, s->order, &dist, s->outputs, s->comb.data(), s->vals.data(), s->vals64.data(),
                          &s->count, 0);
@@ -185,6 +187,7 @@ bool admit(fiu_server* sv, ServeScan* s) {
     d.outputs = s->outputs;
     d.single = s->res->single;
     d.pairs = s->res->pairs;
+    d.triples = s->res->triples;
     d.cand = (Cand*)s->buf;
     d.scored = (ScoredRec*)(s->buf + s->off_scored);
     d.out_comb = (int*)(s->buf + s->off_comb);
@@ -223,13 +226,13 @@ int run_round(fiu_server* sv) {
         take[i] = std::min({s->w.n_prefixes - s->cursor, s->chunk, s->max_chunk});
     }
     std::vector<std::pair<int, int>> gkey;  // (family, tp) of each group
-    for (int fam = 0; fam < 2; ++fam)
+    for (int fam = 0; fam < kRoundFamilies; ++fam)
         for (int tp : {32, 64, 128, 256}) {
             const size_t first = ents.size();
             long long total = 0;
             for (size_t i = 0; i < sv->active.size(); ++i) {
                 ServeScan* s = sv->active[i];
-                if (!take[i] || (s->kind == FIU_KERNEL_FULL) != (fam == 1) || s->tp != tp) continue;
+                if (!take[i] || round_family(s->kind, s->order) != fam || s->tp != tp) continue;
                 ents.push_back(RoundEntry{s->slot, 0, s->cursor, total});
                 total += take[i];
             }

@@ -18,6 +18,8 @@ Named workloads (``WORKLOADS``):
 * ``order2_40000x16000`` -- 40 000 SNPs, 8 000 / 8 000, order 2, MAF ~
   Beta(0.5, 0.5) truncated to [0.01, 0.5] by rejection; five planted pairs
   with penetrance 0.6.  Top-1 000.
+* ``order4_300x8000``   -- 300 SNPs, 4 000 / 4 000, order 4, MAF ~ U(0.05,
+  0.5); one planted quadruple: all four carry a minor allele -> 0.7.  Top-100.
 * ``batch_specs()``      -- 64 independent scans, seeds 1000+i: SNPs
   log-uniform in [500, 20 000], samples log-uniform in [1 000, 32 000], case
   fraction U(0.3, 0.7), order uniform in {2, 3, 4} (order-4 scans capped at
@@ -58,6 +60,7 @@ WORKLOADS = {
     "order3_2000x8000": ScanSpec(2000, 4000, 4000, 3, 100, seed=2, planted=(3,), penetrance=0.65),
     "order2_40000x16000": ScanSpec(40000, 8000, 8000, 2, 1000, seed=3, maf="beta", planted=(2, 2, 2, 2, 2),
                                    penetrance=0.6),
+    "order4_300x8000": ScanSpec(300, 4000, 4000, 4, 100, seed=4, planted=(4,), penetrance=0.7),
 }
 
 

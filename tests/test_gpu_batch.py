@@ -28,6 +28,8 @@ SCANS = [  # seed, snps, cases, ctrls, order, outputs, one_hot, (step, offset)
     (6, 700, 1500, 1500, 2, 7, True, (1, 0)),
     (7, 25, 4000, 4100, 3, 2000, True, (1, 0)),  # fewer combinations than outputs
     (8, 12, 64, 64, 5, 10, True, (1, 0)),        # order 5: single-scan path inside the batch
+    (9, 34, 1200, 800, 4, 40, True, (2, 1)),     # order 4, reduced-work kernel, a Distribution layer
+    (10, 30, 500, 520, 4, 25, False, (1, 0)),    # order 4, full kernel
 ]
 
 
@@ -73,7 +75,7 @@ def test_batch_against_oracle(batch_setup, oracle):
     from helpers import assert_topn_equivalent, exact_mi
     gs, reqs, _ = batch_setup
     got = gs.run_batch(reqs)
-    for i in (1, 4):
+    for i in (1, 2, 4, 8):
         seed, snps, nc, nt, order, outputs, one_hot, (step, off) = SCANS[i]
         ds = _scan_data(seed, snps, nc, nt, one_hot)
         c, _, o64, _ = oracle.search(ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words, order,

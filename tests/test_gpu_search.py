@@ -65,12 +65,13 @@ def test_combine_and_popcnt_bit_exact(gs, oracle, golden_testdata):
     assert np.all(cc[27:] == 0) and np.all(tt[27:] == 0)
 
 
-@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 2), (3, 2), (2, 3), (3, 3), (2, 4), (3, 4)])
+@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 2), (3, 2), (4, 2), (2, 3), (3, 3), (4, 3),
+                                          (2, 4), (3, 4)])
 def test_hot_kernel_tables_bit_exact_reference(gs, golden_testdata, order, kernel):
     """Each counting kernel's own contingency tables for EVERY combination of the
     reference's test data == the reference's combine_and_popcnt tables
-    (kernel 1: full table; 2, 3: core cells + exact marginals, POPC / Harley-Seal;
-    4: core cells on the tcgen05 tensor cores)."""
+    (kernel 1: full table; 2, 3: core cells + exact marginals, POPC / Harley-Seal,
+    at order 4 from triple cores; 4: core cells on the tcgen05 tensor cores)."""
     from fiuncho_gb300 import Distribution, Resident
     ds = _ds_from_golden(golden_testdata)
     res = Resident(gs.ctx, ds)
@@ -265,6 +266,55 @@ def test_kernels_agree(oracle, n_case, n_ctrl, snps):
         _check_topn(oracle, ds, order, 40, r, outs[0][1])
 
 
+@pytest.mark.parametrize("n_case,n_ctrl,snps", [(1000, 777, 30), (65, 63, 26), (1, 513, 20), (4000, 4000, 28),
+                                                 (130, 1, 23), (511, 1537, 33)])
+def test_order4_kernels_agree(oracle, n_case, n_ctrl, snps):
+    """Order 4: the reduced-work kernels (16 core cells counted, 65 derived from
+    triple, pair and single cores; POPC and Harley-Seal counting) give the full
+    kernel's tables for every combination and the same top-N, which matches the
+    oracle."""
+    from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident
+    rng = np.random.default_rng(n_case * 3 + n_ctrl + snps)
+    maf = rng.uniform(0.05, 0.5, snps)[:, None]
+    u = rng.random((snps, n_case + n_ctrl))
+    geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
+    ds = Dataset.from_genotypes(geno, np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)])
+    dist = Distribution(snps, 3)
+    outs, tabs = [], []
+    for kernel in (1, 2, 3):
+        g = GpuSearch(0, kernel=kernel)
+        res = Resident(g.ctx, ds)
+        tabs.append(g.scan_tables(res, 4, dist, kernel=kernel))
+        r, v64 = g.run(res, 4, dist, 40, with_fp64=True)
+        assert g.last_tile()[0] == kernel
+        outs.append(([x.combination for x in r], v64))
+    mask = tabs[0] != 0xFFFFFFFF
+    assert mask.sum() == math.comb(snps, 4) * 2 * 81
+    for t in tabs[1:]:
+        assert np.array_equal(t[mask], tabs[0][mask])
+    for o in outs[1:]:
+        assert o[0] == outs[0][0] and np.array_equal(o[1], outs[0][1])
+    r = [type("R", (), {"combination": c, "val": v})() for c, v in zip(outs[0][0], outs[0][1])]
+    _check_topn(oracle, ds, 4, 40, r, outs[0][1])
+
+
+def test_order4_reduced_work_is_automatic(gs, golden_synth):
+    """One-hot order-4 searches pick a reduced-work kernel by themselves, also for a
+    Distribution layer (step > 1) of the prefixes; non-one-hot data keeps the full kernel."""
+    from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident
+    ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    g.run(res, 4, Distribution(ds.snps, 3), 10)
+    assert g.last_tile()[0] in (2, 3)
+    g.run(res, 4, Distribution(ds.snps, 3, 3, 2), 10)
+    assert g.last_tile()[0] in (2, 3)
+    rng = np.random.default_rng(5)
+    bad = Dataset(100, 70, 9, 2, 2, rng.integers(0, 2 ** 63, 9 * 3 * 4, dtype=np.uint64))
+    g.run(bad, 4, Distribution(9, 3), 5)
+    assert g.last_tile()[0] == 1
+
+
 def test_tensor_kernel_scope(gs, golden_synth):
     """The tcgen05 kernel serves one-hot order-3 searches of the whole data set by one
     worker; a step > 1 distribution falls back to the reduced-work kernel automatically
@@ -322,7 +372,7 @@ def test_order3_300x8000_top100(gs, oracle):
     _check_topn(oracle, ds, 3, 100, res, v64, threads=16)
 
 
-@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 3), (3, 3), (3, 2)])
+@pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 3), (3, 3), (3, 2), (4, 3), (4, 2)])
 def test_tiles_agree(oracle, order, kernel):
     """Every l-tile width (threads per prefix 32/64/128/256) of each kernel gives
     the same tables, and searches with autotuning on/off give identical lists."""
