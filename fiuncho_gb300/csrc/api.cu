@@ -166,6 +166,33 @@ static int heuristic_tp(int kernel, const ScanWork& w) {
     return tp;
 }
 
+static bool whole_data_set(const fiu_resident* res, const ScanWork& w) {
+    return w.dist_step == 1 && w.dist_offset == 0 && w.dist_n == res->d.snps;
+}
+
+// A whole-data-set order-4 scan on the reduced-work POPC kernel runs pair-major
+// (work items of (k, l) runs per pair (i, j), see elided4.cu).
+bool e4_pair_major(int kernel, const fiu_resident* res, const ScanWork& w) {
+    return kernel == FIU_KERNEL_ELIDED_POPC && w.order == 4 && whole_data_set(res, w);
+}
+
+// Work-item table of the pair-major order-4 schedule, built once per data set.
+static int ensure_e4_items(fiu_ctx* ctx, const fiu_resident* res_c) {
+    fiu_resident* res = const_cast<fiu_resident*>(res_c);
+    if (res->e4_begin) return FIU_OK;
+    const std::vector<long long> b = e4p_item_begin(res->d.snps);
+    long long* d = nullptr;
+    CK(cudaMalloc((void**)&d, b.size() * sizeof(long long)), "work-item table");
+    cudaError_t e = cudaMemcpy(d, b.data(), b.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(ctx, e, "work-item table");
+    }
+    res->e4_begin = d;
+    res->e4_items = b.back();
+    return FIU_OK;
+}
+
 static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
     return res->one_hot && (w.order == 2 || w.order == 3) && w.dist_step == 1 && w.dist_offset == 0 && w.dist_n == res->d.snps &&
            res->d.n_cases >= 1 && res->d.n_ctrls >= 1 && res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 &&
@@ -201,6 +228,10 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
     }
     int rc = choose_kernel(ctx, res, (unsigned)w.order, requested_kernel, kernel);
     if (rc) return rc;
+    if (e4_pair_major(kernel, res, w)) {  // one warp per work item: no l-tile to choose
+        tp = 32;
+        return ensure_e4_items(ctx, res);
+    }
     tp = heuristic_tp(kernel, w);
     const double work = (double)binom(w.dist_n, w.order) / std::max(1, w.dist_step) * (w.d.n_cases + w.d.n_ctrls);
     if (!ctx->autotune || work < 2e11 || w.n_prefixes < 64) return FIU_OK;
@@ -278,7 +309,8 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     ctx->last_kernel = kernel;
     ctx->last_tp = tp;
     const bool tensor = kernel == FIU_KERNEL_TENSOR;
-    const long long units = tensor ? tensor_units(*res->t3, (int)order) : w.n_prefixes;
+    const bool pair_major = e4_pair_major(kernel, res, w);
+    const long long units = tensor ? tensor_units(*res->t3, (int)order) : pair_major ? res->e4_items : w.n_prefixes;
     int* t_status = (int*)(ctx->ctl + 16);
     if (tensor) CK(cudaMemsetAsync(t_status, 0, sizeof(int), ctx->stream), "status reset");
     const unsigned keep = outputs + std::max(32u, outputs / 8);
@@ -294,7 +326,9 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     long long thr = (long long)0x8000000000000000ull;
     unsigned have = 0;
     const double per_prefix = (double)binom(w.dist_n, order) / std::max<double>(1.0, (double)binom(w.dist_n, order - 1));
-    const double per_unit = tensor ? tensor_item_combos(*res->t3, (int)order) : per_prefix;
+    const double per_unit = tensor       ? tensor_item_combos(*res->t3, (int)order)
+                            : pair_major ? (double)binom(w.dist_n, 4) / std::max(1ll, res->e4_items)
+                                         : per_prefix;
     long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_unit)));
     long long m = 0;
     while (m < units) {
@@ -307,6 +341,10 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
         if (tensor)
             CK(launch_tensor3(w, *res->t3, m, m1, sink, nullptr, res->single, res->pairs, t_status, s, ctx->sms),
                "tensor kernel launch");
+        else if (pair_major)
+            CK(launch_elided4p(w, res->e4_begin, m, m1, sink, nullptr, res->single, res->pairs, res->triples, s,
+                               ctx->sms),
+               "count kernel launch");
         else
             CK(launch_kernel(kernel, tp, res, w, m, m1, sink, nullptr, s, ctx->sms), "count kernel launch");
         if (ctx->timing) CK(cudaEventRecord(ctx->ev1, s), "event");
@@ -546,6 +584,7 @@ void fiu_dataset_free(fiu_ctx* ctx, fiu_resident* r) {
     cudaFree(r->single);
     cudaFree(r->pairs);
     cudaFree(r->triples);
+    cudaFree(r->e4_begin);
     if (r->t3) {
         tensor3_release(*r->t3);
         delete r->t3;
@@ -743,6 +782,13 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
             e = launch_tensor3(w, *res->t3, 0, tensor_units(*res->t3, (int)order), sink, d, res->single, res->pairs,
                                (int*)(ctx->ctl + 16),
                                s, ctx->sms);
+    } else if (e == cudaSuccess && e4_pair_major(kernel, res, w)) {
+        if ((rc = ensure_e4_items(ctx, res))) {
+            cudaFreeAsync(d, s);
+            return rc;
+        }
+        e = launch_elided4p(w, res->e4_begin, 0, res->e4_items, sink, d, res->single, res->pairs, res->triples, s,
+                            ctx->sms);
     } else if (e == cudaSuccess) {
         e = launch_kernel(kernel, tp, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
     }

@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(kRoundThreads, 2) round_kernel(const ScanDesc*
 static size_t g_round_attr[3][4] = {};
 static int g_round_per_sm[3][4] = {};
 static bool g_select_attr = false, g_finish_attr = false;
+static std::mutex g_round_mu;  // the tables above are shared by every host thread
 
 __global__ void select_scans_kernel(const ScanDesc* __restrict__ scans, ScanState* states, int final_pass);
 __global__ void finish_scans_kernel(const ScanDesc* __restrict__ scans, ScanState* states);
@@ -103,6 +104,7 @@ static const void* round_fn(int family, int ti) {
 // Sets the dynamic shared-memory limits of the multi-scan kernels (never
 // inside a stream capture) and caches the round kernels' occupancy.
 cudaError_t prepare_round_kernels(size_t smem) {
+    std::lock_guard<std::mutex> g(g_round_mu);
     cudaError_t e = cudaSuccess;
     for (int f = 0; f < 3; ++f)
         for (int t = 0; t < 4; ++t) {
@@ -143,12 +145,18 @@ cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* s
                          int n_ents, long long total, size_t smem, int sms, cudaStream_t s) {
     if (total <= 0 || n_ents <= 0) return cudaSuccess;
     const int ti = tp_index(tp);
-    if (family < 0 || family > 2 || smem > g_round_attr[family][ti] || !g_round_per_sm[family][ti])
-        return cudaErrorInvalidConfiguration;  // prepare_round_kernels first
+    if (family < 0 || family > 2) return cudaErrorInvalidValue;
+    size_t sm = 0;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> g(g_round_mu);
+        sm = g_round_attr[family][ti];
+        per_sm = g_round_per_sm[family][ti];
+    }
+    if (smem > sm || !per_sm) return cudaErrorInvalidConfiguration;  // prepare_round_kernels first
     const long long G = kRoundThreads / tp;
-    const long long ctas = (total + G - 1) / G, cap = (long long)sms * g_round_per_sm[family][ti];
+    const long long ctas = (total + G - 1) / G, cap = (long long)sms * per_sm;
     const unsigned grid = (unsigned)(ctas < cap ? ctas : cap);
-    const size_t sm = g_round_attr[family][ti];
     if (family == 2) {
         switch (ti) {
             case 0: launch_round_t<2, 32>(grid, sm, scans, states, ents, n_ents, total, s); break;

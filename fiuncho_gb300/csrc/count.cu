@@ -33,14 +33,10 @@ static cudaError_t launch_full(const ScanWork& w, long long m0, long long m1, co
                                cudaStream_t s, int sms) {
     constexpr int G = kThreads / TP;
     const size_t smem = (size_t)G * full_group_words(K) * sizeof(uint64_t);
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(count_full<K, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, count_full<K, TP>, kThreads, smem);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
-    }
+    static LaunchCache cache;
+    int per_sm = 1;
+    const cudaError_t e = blocks_per_sm(cache, count_full<K, TP>, kThreads, smem, per_sm);
+    if (e != cudaSuccess) return e;
     const long long ctas = (m1 - m0 + G - 1) / G;
     if (ctas <= 0) return cudaSuccess;
     const long long grid = ctas < (long long)sms * per_sm ? ctas : (long long)sms * per_sm;

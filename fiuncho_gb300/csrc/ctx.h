@@ -53,6 +53,8 @@ struct fiu_resident {
     uint32_t* single = nullptr;  // single-SNP cores (elided kernels)
     uint4* pairs = nullptr;      // pair cores (elided order-3 and order-4 kernels)
     uint4* triples = nullptr;    // triple cores (elided order-4 kernel)
+    long long* e4_begin = nullptr;  // pair-major order-4 work items: first item per second SNP j
+    long long e4_items = 0;
     fiu::T3Plan* t3 = nullptr;  // operand planes and work items of the tensor order-3 kernel
 };
 
@@ -81,6 +83,7 @@ int choose_kernel(fiu_ctx* ctx, const fiu_resident* res, unsigned order, int req
 // bucket) when autotuning is on and the request is large, else a heuristic.
 int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp,
                 bool allow_tensor = false);
+bool e4_pair_major(int kernel, const fiu_resident* res, const ScanWork& w);
 cudaError_t launch_kernel(int kernel, int tp, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
                           const CandSink& sink, uint32_t* dump, cudaStream_t s, int sms);
 int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,

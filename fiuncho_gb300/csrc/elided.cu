@@ -92,7 +92,9 @@ cudaError_t build_cores(const DevData& d, uint32_t* single, uint4* pairs, int sm
     if (e != cudaSuccess || !pairs) return e;
     const size_t smem = 2 * (size_t)(d.cw + d.tw) * sizeof(uint64_t);
     if (smem > 200 * 1024) return cudaErrorInvalidValue;
-    e = cudaFuncSetAttribute(pair_cores_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static LaunchCache cache;
+    int per_sm = 1;
+    e = blocks_per_sm(cache, pair_cores_kernel, kEThreads, smem, per_sm);
     if (e != cudaSuccess) return e;
     const int grid = d.snps - 1 < sms * 8 ? (d.snps - 1 > 0 ? d.snps - 1 : 1) : sms * 8;
     pair_cores_kernel<<<grid, kEThreads, smem, s>>>(d, pairs);
@@ -120,17 +122,10 @@ static cudaError_t launch_el(const ScanWork& w, long long m0, long long m1, cons
     constexpr int G = kEThreads / TP;
     const size_t smem = G * elided_smem(K, w.d.cw, w.d.tw);
     if (smem > kMaxGroupSmem) return cudaErrorInvalidConfiguration;
-    static int per_sm = 0;
-    static size_t per_sm_smem = 0;
-    if (!per_sm || per_sm_smem != smem) {
-        cudaError_t e = cudaFuncSetAttribute(count_elided<K, HS, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, count_elided<K, HS, TP>, kEThreads, smem);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
-        per_sm_smem = smem;
-    }
+    static LaunchCache cache;
+    int per_sm = 1;
+    const cudaError_t e = blocks_per_sm(cache, count_elided<K, HS, TP>, kEThreads, smem, per_sm);
+    if (e != cudaSuccess) return e;
     const long long ctas = (m1 - m0 + G - 1) / G;
     if (ctas <= 0) return cudaSuccess;
     const long long grid = ctas < (long long)sms * per_sm ? ctas : (long long)sms * per_sm;

@@ -64,23 +64,30 @@ __device__ __forceinline__ uint32_t by_pass(uint32_t a, uint32_t b) {
 }
 
 // Locations of the sub-combination cores of one combination (i, j, k, l).
+// Each pass loads what it reads itself, after a compiler memory barrier, so
+// that the loads of a pass are not hoisted above the previous one (fewer
+// registers held across the passes; the reloads hit L1).
 struct E4Src {
     const uint4* tij;  // triple (i,j,l): two words, cases then controls
     const uint4* tik;  // triple (i,k,l)
     const uint4* tjk;  // triple (j,k,l)
-    uint4 pil, pjl, pkl;  // pairs (i,l), (j,l), (k,l): [class][x][y] uint16
-    uint4 sl;             // single l: [class][x]
+    const uint4* pil;  // pairs (i,l), (j,l), (k,l): [class][x][y] uint16
+    const uint4* pjl;
+    const uint4* pkl;
+    const uint4* sl;   // single l: [class][x]
 };
 
 // One pass of the MI key over the 81 cells: the slices l = 0, 1, 2, each an
 // order-3 derivation from its star table (slice 2's is the prefix's star
-// table minus slices 0 and 1: the derivation is linear).  Returns the sum of T[cell] over
-// the pass's 81 cells; writes the cells to o[((x*3+y)*3+z)*3 + w] if o.
-// The counted cores arrive packed: cp[cls][r] = core (r, w=0) | core (r, w=1) << 16.
-template <int PC>
-__device__ __forceinline__ long long e4_pass(const uint32_t (&cp)[2][8], const E4Src& src,
-                                             const uint32_t* __restrict__ pstar, const long long* __restrict__ ftab,
-                                             uint32_t nc, uint32_t* o) {
+// table, pstar(q), minus slices 0 and 1: the derivation is linear).  Returns
+// the sum of T[cell] over the pass's 81 cells; writes the cells to
+// o[((x*3+y)*3+z)*3 + w] if o.  The counted cores arrive packed:
+// cp[cls][r] = core (r, w=0) | core (r, w=1) << 16.
+template <int PC, class PStar>
+__device__ __forceinline__ long long e4_pass(const uint32_t (&cp)[2][8], const E4Src& src, const PStar& pstar,
+                                             const long long* __restrict__ ftab, uint32_t nc, uint32_t* o) {
+    asm volatile("" ::: "memory");
+    const uint4 pil = __ldg(src.pil), pjl = __ldg(src.pjl), pkl = __ldg(src.pkl), sl = __ldg(src.sl);
     uint4 ta[3], tb[3];  // triple words of the pass's class(es)
     {
         const uint4* tp[3] = {src.tij, src.tik, src.tjk};
@@ -104,17 +111,17 @@ __device__ __forceinline__ long long e4_pass(const uint32_t (&cp)[2][8], const E
         if (a < 2 && b < 2) return tri(0, a, b, w);
         if (a < 2 && z < 2) return tri(1, a, z, w);
         if (b < 2 && z < 2) return tri(2, b, z, w);
-        if (a < 2) return pr(src.pil, a, w);
-        if (b < 2) return pr(src.pjl, b, w);
-        if (z < 2) return pr(src.pkl, z, w);
-        return by_pass<PC>(w ? src.sl.y : src.sl.x, w ? src.sl.w : src.sl.z);
+        if (a < 2) return pr(pil, a, w);
+        if (b < 2) return pr(pjl, b, w);
+        if (z < 2) return pr(pkl, z, w);
+        return by_pass<PC>(w ? sl.y : sl.x, w ? sl.w : sl.z);
     };
     long long part = 0;
 #pragma unroll
     for (int sw = 0; sw < 3; ++sw) {
         uint32_t t[27];
 #pragma unroll
-        for (int q = 0; q < 27; ++q) t[q] = sw < 2 ? star(sw, q) : pstar[q] - star(0, q) - star(1, q);
+        for (int q = 0; q < 27; ++q) t[q] = sw < 2 ? star(sw, q) : pstar(q) - star(0, q) - star(1, q);
         star_to_table(t);
         // derived cells of consistent one-hot data never exceed the class
         // size; the clamp keeps any inconsistency inside the table
@@ -235,15 +242,15 @@ __device__ __forceinline__ void elided4_prefix(const ScanWork& w, long long m, c
             src.tij = triples + 2 * triple_index(c[0], c[1], l, S);
             src.tik = triples + 2 * triple_index(c[0], c[2], l, S);
             src.tjk = triples + 2 * triple_index(c[1], c[2], l, S);
-            src.pil = __ldg(pairs + pair_index(c[0], l, S));
-            src.pjl = __ldg(pairs + pair_index(c[1], l, S));
-            src.pkl = __ldg(pairs + pair_index(c[2], l, S));
-            src.sl = __ldg(single4 + l);
+            src.pil = pairs + pair_index(c[0], l, S);
+            src.pjl = pairs + pair_index(c[1], l, S);
+            src.pkl = pairs + pair_index(c[2], l, S);
+            src.sl = single4 + l;
             uint32_t* o = dump ? dump + ((size_t)m * S + l) * 2 * 81 : nullptr;
             // key = base + sum over the 81 cells of T[case] + T[control] - T[total]
-            key += e4_pass<0>(cp, src, ptab, d.ftab, d.n_cases, o);
-            key += e4_pass<1>(cp, src, ptab + 27, d.ftab, d.n_ctrls, o);
-            key -= e4_pass<2>(cp, src, ptab + 54, d.ftab, d.n_cases + d.n_ctrls, o);
+            key += e4_pass<0>(cp, src, [&](int q) { return ptab[q]; }, d.ftab, d.n_cases, o);
+            key += e4_pass<1>(cp, src, [&](int q) { return ptab[27 + q]; }, d.ftab, d.n_ctrls, o);
+            key -= e4_pass<2>(cp, src, [&](int q) { return ptab[54 + q]; }, d.ftab, d.n_cases + d.n_ctrls, o);
         }
         const bool pass = valid && key >= sink.thr;
         const unsigned mask = __ballot_sync(0xffffffffu, pass);

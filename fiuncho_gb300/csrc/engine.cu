@@ -5,8 +5,9 @@
 // whose candidate buffer overflowed is re-run alone on the single-scan path
 // (whose chunking adapts on the host), so results never depend on batching.
 // Scans served by the tensor-core kernels (one-hot order 2 or 3 over the whole
-// data set) are not split into rounds: they run alone, one after the other,
-// as they would in a loop of single calls.
+// data set) or by the pair-major order-4 kernel (one-hot, whole data set) are
+// not split into rounds: they run alone, one after the other, as they would in
+// a loop of single calls.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -61,8 +62,8 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             sc.status = rc;
             continue;
         }
-        // tensor-core scans and full-table scans above order 4 run alone
-        if (kind == FIU_KERNEL_TENSOR || (kind == FIU_KERNEL_FULL && sc.order > 4)) {
+        // tensor-core and pair-major order-4 scans and full-table scans above order 4 run alone
+        if (kind == FIU_KERNEL_TENSOR || e4_pair_major(kind, sc.res, w) || (kind == FIU_KERNEL_FULL && sc.order > 4)) {
             single_path.push_back(i);
             continue;
         }

@@ -3,6 +3,7 @@
 
 #include <cuda.h>
 
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -96,6 +97,34 @@ inline void count_launch(unsigned n = 1) {
 // Largest dynamic shared memory a counting kernel may use (all groups).
 constexpr size_t kMaxGroupSmem = 200 * 1024;
 
+// Launch configuration of one kernel, cached and safe to share between host
+// threads (the served form runs two): the dynamic shared-memory limit only
+// grows, so a launch prepared by one thread is never invalidated by another;
+// resident blocks per SM are looked up again when the size changes.
+struct LaunchCache {
+    std::mutex mu;
+    size_t attr = 0;
+    size_t occ_smem = ~(size_t)0;
+    int occ = 0;
+};
+template <class F>
+cudaError_t blocks_per_sm(LaunchCache& c, F* fn, int threads, size_t smem, int& out) {
+    std::lock_guard<std::mutex> g(c.mu);
+    if (smem > c.attr) {
+        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        c.attr = smem;
+    }
+    if (c.occ_smem != smem) {
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.occ, fn, threads, smem);
+        if (e != cudaSuccess) return e;
+        if (c.occ < 1) c.occ = 1;
+        c.occ_smem = smem;
+    }
+    out = c.occ;
+    return cudaSuccess;
+}
+
 // count.cu -- generic full 3^k table kernel (any data, orders 2..8) with the
 // fused fixed-point MI and the candidate filter; tp = threads per prefix
 // (32, 64, 128 or 256; orders above 5 always use 256).
@@ -115,6 +144,13 @@ size_t elided4_smem(int cw, int tw);
 cudaError_t launch_elided4(bool hs, int tp, const ScanWork& w, long long m0, long long m1, const CandSink& sink,
                            uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
                            cudaStream_t s, int sms);
+// Pair-major schedule of a whole-data-set order-4 scan: work items g in [g0, g1)
+// of the table begin[0..snps] (e4p_item_begin).
+std::vector<long long> e4p_item_begin(int snps);
+size_t e4p_smem(int cw, int tw);
+cudaError_t launch_elided4p(const ScanWork& w, const long long* begin, long long g0, long long g1,
+                            const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
+                            const uint4* triples, cudaStream_t s, int sms);
 
 // tensor3.cu -- order-2 and order-3 core cells on tcgen05 (one-hot data, whole data set, one worker).
 // Device state of the tensor kernel for one data set: the e4m3 operand planes

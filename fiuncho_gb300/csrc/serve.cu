@@ -10,9 +10,14 @@
 // large scan does not hold small ones back), then one selection CTA per slot
 // raises thresholds on the device.  Scans whose last chunk ran are finalised
 // (FP64 re-score + top-N), copied out, and release their memory and slot;
-// scans that arrived meanwhile are admitted before the next round.  A scan
-// served by the tensor-core kernels (one-hot order 2 or 3 over the whole data
-// set) runs alone on admission, between two rounds.
+// scans that arrived meanwhile are admitted before the next round.
+//
+// Scans that run best alone -- those served by the tensor-core kernels
+// (one-hot order 2 or 3) or the pair-major order-4 kernel, full-table scans
+// above order 4, and any scan admitted while every slot is taken -- go to a
+// second lane: a solo worker thread with its own context and stream runs them
+// one at a time through the single-scan path, concurrently with the rounds,
+// so both lanes share the device.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -81,6 +86,11 @@ struct fiu_server {
     uint64_t next_ticket = 1;
     bool stop = false;
     std::thread worker;
+    // solo lane
+    fiu_ctx* solo_ctx = nullptr;
+    std::deque<ServeScan*> solo_queue;
+    std::condition_variable cv_solo;
+    std::thread solo_worker;
     ScanDesc* d_desc = nullptr;
     ScanState* d_state = nullptr;
     unsigned* d_zero = nullptr;
@@ -88,7 +98,7 @@ struct fiu_server {
     size_t ents_cap = 0;
     std::vector<int> free_slots;
     // statistics (under mu)
-    uint64_t submitted = 0, completed = 0, failed = 0, rounds = 0, bytes_in_use = 0;
+    uint64_t submitted = 0, completed = 0, failed = 0, rounds = 0, bytes_in_use = 0, solo = 0;
     std::vector<double> lat_ms;
     double combos_samples = 0;
     int init_status = FIU_OK;
@@ -96,7 +106,8 @@ struct fiu_server {
 
 namespace {
 
-void release(fiu_server* sv, ServeScan* s) {
+// Frees what a scan holds on the device; ctx is the context of the calling lane.
+void release(fiu_server* sv, ServeScan* s, fiu_ctx* ctx) {
     if (s->slot >= 0) {
         ScanDesc zero{};
         cudaMemcpyAsync(sv->d_desc + s->slot, &zero, sizeof(zero), cudaMemcpyHostToDevice, sv->ctx->stream);
@@ -106,15 +117,14 @@ void release(fiu_server* sv, ServeScan* s) {
     }
     if (s->buf) cudaFree(s->buf);
     s->buf = nullptr;
-    if (s->res) fiu_dataset_free(sv->ctx, s->res);
+    if (s->res) fiu_dataset_free(ctx, s->res);
     s->res = nullptr;
     std::vector<uint64_t>().swap(s->data);
 }
 
-void finish(fiu_server* sv, ServeScan* s, int status) {
-    fiu_ctx* ctx = sv->ctx;
+void finish(fiu_server* sv, ServeScan* s, int status, fiu_ctx* ctx = nullptr) {
     s->status = status;
-    release(sv, s);
+    release(sv, s, ctx ? ctx : sv->ctx);
     std::lock_guard<std::mutex> g(sv->mu);
     s->done = Clock::now();
     s->finished = true;
@@ -126,7 +136,6 @@ void finish(fiu_server* sv, ServeScan* s, int status) {
     } else {
         sv->failed++;
     }
-    (void)ctx;
     sv->cv_done.notify_all();
 }
 
@@ -154,11 +163,12 @@ bool admit(fiu_server* sv, ServeScan* s) {
         finish(sv, s, rc);
         return false;
     }
-    if (s->kind == FIU_KERNEL_TENSOR || (s->kind == FIU_KERNEL_FULL && s->order > 4) || sv->free_slots.empty()) {
-        // outside the round kernels: the single-scan path, right now
-        rc = search_impl(ctx, s->res, s->order, &dist, s->outputs, s->comb.data(), s->vals.data(), s->vals64.data(),
-                         &s->count, 0);
-        finish(sv, s, rc);
+    if (s->kind == FIU_KERNEL_TENSOR || e4_pair_major(s->kind, s->res, s->w) ||
+        (s->kind == FIU_KERNEL_FULL && s->order > 4) || sv->free_slots.empty()) {
+        // outside the round kernels: the solo lane
+        std::lock_guard<std::mutex> g(sv->mu);
+        sv->solo_queue.push_back(s);
+        sv->cv_solo.notify_one();
         return false;
     }
     s->keep = s->outputs + std::max(32u, s->outputs / 8);
@@ -297,6 +307,29 @@ int run_round(fiu_server* sv) {
     return FIU_OK;
 }
 
+// The solo lane: scans that run alone, FIFO, on the lane's own stream.
+void solo_main(fiu_server* sv) {
+    Scope scope(sv->solo_ctx);
+    for (;;) {
+        ServeScan* s = nullptr;
+        {
+            std::unique_lock<std::mutex> g(sv->mu);
+            sv->cv_solo.wait(g, [&] { return sv->stop || !sv->solo_queue.empty(); });
+            if (sv->stop) return;
+            s = sv->solo_queue.front();
+            sv->solo_queue.pop_front();
+        }
+        fiu_distribution dist{(int)s->host.snps, (int)s->order - 1, 1, 0};
+        const int rc = search_impl(sv->solo_ctx, s->res, s->order, &dist, s->outputs, s->comb.data(),
+                                   s->vals.data(), s->vals64.data(), &s->count, 0);
+        {
+            std::lock_guard<std::mutex> g(sv->mu);
+            sv->solo++;
+        }
+        finish(sv, s, rc, sv->solo_ctx);
+    }
+}
+
 void worker_main(fiu_server* sv) {
     Scope scope(sv->ctx);
     for (;;) {
@@ -343,6 +376,11 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
         return rc;
     }
     sv->budget = budget_bytes ? budget_bytes : 120ull * 1000 * 1000 * 1000;
+    if ((rc = fiu_create(device, &sv->solo_ctx))) {
+        fiu_destroy(sv->ctx);
+        delete sv;
+        return rc;
+    }
     cudaSetDevice(device);
     if (cudaMalloc((void**)&sv->d_desc, kSlots * sizeof(ScanDesc)) != cudaSuccess ||
         cudaMalloc((void**)&sv->d_state, kSlots * sizeof(ScanState)) != cudaSuccess ||
@@ -353,6 +391,7 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
         cudaFree(sv->d_desc);
         cudaFree(sv->d_state);
         cudaFree(sv->d_zero);
+        fiu_destroy(sv->solo_ctx);
         fiu_destroy(sv->ctx);
         delete sv;
         return FIU_ERR_CUDA;
@@ -361,6 +400,10 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
     sv->worker = std::thread([sv] {
         cudaSetDevice(sv->ctx->device);
         worker_main(sv);
+    });
+    sv->solo_worker = std::thread([sv] {
+        cudaSetDevice(sv->ctx->device);
+        solo_main(sv);
     });
     *out = sv;
     return FIU_OK;
@@ -426,6 +469,7 @@ int fiu_server_stats(fiu_server* sv, fiu_serve_stats* out) {
     out->queued = sv->queue.size();
     out->active = sv->submitted - sv->completed - sv->failed - sv->queue.size();
     out->rounds = sv->rounds;
+    out->solo = sv->solo;
     out->bytes_in_use = sv->bytes_in_use;
     out->combos_samples = sv->combos_samples;
     if (!sv->lat_ms.empty()) {
@@ -449,17 +493,20 @@ void fiu_server_destroy(fiu_server* sv) {
         sv->stop = true;
     }
     sv->cv_work.notify_all();
+    sv->cv_solo.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
+    if (sv->solo_worker.joinable()) sv->solo_worker.join();
     cudaSetDevice(sv->ctx->device);
-    for (ServeScan* s : sv->active) release(sv, s);
+    for (ServeScan* s : sv->active) release(sv, s, sv->ctx);
     for (auto& kv : sv->tickets) {
-        if (kv.second->res || kv.second->buf) release(sv, kv.second);
+        if (kv.second->res || kv.second->buf) release(sv, kv.second, sv->ctx);
         delete kv.second;
     }
     cudaFree(sv->d_desc);
     cudaFree(sv->d_state);
     cudaFree(sv->d_zero);
     cudaFree(sv->d_ents);
+    fiu_destroy(sv->solo_ctx);
     fiu_destroy(sv->ctx);
     delete sv;
 }

@@ -296,6 +296,14 @@ def test_order4_kernels_agree(oracle, n_case, n_ctrl, snps):
         assert o[0] == outs[0][0] and np.array_equal(o[1], outs[0][1])
     r = [type("R", (), {"combination": c, "val": v})() for c, v in zip(outs[0][0], outs[0][1])]
     _check_topn(oracle, ds, 4, 40, r, outs[0][1])
+    # a Distribution layer (per-prefix schedule) against the full kernel
+    layer = Distribution(snps, 3, 3, 1)
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    full = g.scan_tables(res, 4, layer, kernel=1)
+    mask = full != 0xFFFFFFFF
+    for kernel in (2, 3):
+        assert np.array_equal(g.scan_tables(res, 4, layer, kernel=kernel)[mask], full[mask])
 
 
 def test_order4_reduced_work_is_automatic(gs, golden_synth):

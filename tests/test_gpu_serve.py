@@ -10,17 +10,23 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _ds(seed, snps, n_case, n_ctrl):
+def _ds(seed, snps, n_case, n_ctrl, one_hot=True):
     from fiuncho_gb300 import Dataset
     rng = np.random.default_rng(seed)
+    if not one_hot:  # random bits: the full-table kernel in the rounds
+        cw, tw = (n_case + 63) // 64, (n_ctrl + 63) // 64
+        return Dataset(n_case, n_ctrl, snps, cw, tw, rng.integers(0, 2 ** 63, snps * 3 * (cw + tw), dtype=np.uint64))
     maf = rng.uniform(0.05, 0.5, snps)[:, None]
     u = rng.random((snps, n_case + n_ctrl))
     geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
     return Dataset.from_genotypes(geno, np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)])
 
 
+# seed, snps, cases, controls, order, outputs[, one-hot]: one-hot scans take the solo lane
+# (tensor-core / pair-major kernels), the others the rounds
 MIX = [(11, 400, 1200, 1300, 2, 50), (12, 150, 3000, 2500, 3, 50), (13, 60, 900, 700, 4, 25),
-       (14, 900, 800, 800, 2, 20), (15, 220, 2000, 2000, 3, 100), (16, 35, 5000, 4000, 3, 10)]
+       (14, 900, 800, 800, 2, 20), (15, 220, 2000, 2000, 3, 100), (16, 35, 5000, 4000, 3, 10),
+       (17, 70, 600, 500, 3, 30, False), (18, 40, 700, 650, 4, 20, False), (19, 300, 900, 900, 2, 15, False)]
 
 
 def _same(a, b):
@@ -32,7 +38,7 @@ def _same(a, b):
 def test_server_alone_and_in_mix_identical():
     from fiuncho_gb300 import Distribution, GpuSearch, Server
     gs = GpuSearch(0)
-    data = [_ds(*m[:4]) for m in MIX]
+    data = [_ds(*m[:4], *m[6:]) for m in MIX]
     ref = [gs.run(ds, m[4], Distribution(ds.snps, m[4] - 1), m[5], with_fp64=True) for ds, m in zip(data, MIX)]
     srv = Server(0)
     try:
@@ -54,6 +60,7 @@ def test_server_alone_and_in_mix_identical():
         assert st["completed"] == 2 * len(MIX) + 3 and st["failed"] == 0
         assert st["p50_ms"] > 0 and st["p99_ms"] >= st["p50_ms"]
         assert st["rounds"] > 0 and st["bytes_in_use"] == 0
+        assert st["solo"] == 2 * 6 + 3  # the one-hot scans, twice, and the three repeats
     finally:
         srv.close()
 
