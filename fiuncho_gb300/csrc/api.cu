@@ -113,8 +113,8 @@ int choose_kernel(fiu_ctx* ctx, const fiu_resident* res_c, unsigned order, int r
     kernel = requested ? requested
                        : (elided_ok ? (order == 4 ? FIU_KERNEL_ELIDED_POPC : FIU_KERNEL_ELIDED_HS) : FIU_KERNEL_FULL);
     if (kernel < FIU_KERNEL_FULL || kernel > FIU_KERNEL_TENSOR) return fail(ctx, FIU_ERR_INVALID, "unknown kernel id");
-    if (kernel == FIU_KERNEL_TENSOR && order != 2 && order != 3)
-        return fail(ctx, FIU_ERR_UNSUPPORTED, "the tensor-core kernels serve orders 2 and 3");
+    if (kernel == FIU_KERNEL_TENSOR && (order < 2 || order > 4))
+        return fail(ctx, FIU_ERR_UNSUPPORTED, "the tensor-core kernels serve orders 2, 3 and 4");
     if (kernel == FIU_KERNEL_FULL) return FIU_OK;
     if (!elided_ok)
         return fail(ctx, FIU_ERR_UNSUPPORTED,
@@ -194,9 +194,12 @@ static int ensure_e4_items(fiu_ctx* ctx, const fiu_resident* res_c) {
 }
 
 static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
-    return res->one_hot && (w.order == 2 || w.order == 3) && w.dist_step == 1 && w.dist_offset == 0 && w.dist_n == res->d.snps &&
-           res->d.n_cases >= 1 && res->d.n_ctrls >= 1 && res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 &&
-           res->d.snps < (1 << 21);
+    const bool base = res->one_hot && whole_data_set(res, w) && res->d.n_cases >= 1 && res->d.n_ctrls >= 1 &&
+                      res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 && res->d.snps < (1 << 21);
+    if (w.order == 2 || w.order == 3) return base;
+    // order 4: both classes in one accumulator, triple cores within their limit
+    return base && w.order == 4 && res->d.snps >= 4 && tensor_pack(res->d.n_cases, res->d.n_ctrls) &&
+           triples_bytes(res->d.snps) <= kMaxTriplesBytes;
 }
 
 int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp,
@@ -205,7 +208,8 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
                                                    tensor_ok(res, w))) {
         if (!allow_tensor || !tensor_ok(res, w))
             return fail(ctx, FIU_ERR_UNSUPPORTED,
-                        "the tensor-core kernels need one-hot data, order 2 or 3 and the whole data set on one worker");
+                        "the tensor-core kernels need one-hot data, order 2, 3 or 4 (order 4: classes that share "
+                        "one accumulator) and the whole data set on one worker");
         int rc = choose_kernel(ctx, res, (unsigned)w.order, FIU_KERNEL_ELIDED_HS, kernel);  // builds the core tables
         if (rc) return rc;
         fiu_resident* r = const_cast<fiu_resident*>(res);
@@ -223,7 +227,7 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
         }
         kernel = FIU_KERNEL_TENSOR;
         // GEMM width N: order 3 uses 256 with one accumulator for both classes, 192 with one per class
-        tp = (w.order == 2 || r->t3->pack) ? 256 : 192;
+        tp = (w.order != 3 || r->t3->pack) ? 256 : 192;
         return FIU_OK;
     }
     int rc = choose_kernel(ctx, res, (unsigned)w.order, requested_kernel, kernel);
@@ -339,7 +343,8 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
         CandSink sink{ctx->cand, count, overflow, (unsigned)cap, thr, ctx->timing ? ctx->evaluated : nullptr};
         if (ctx->timing) CK(cudaEventRecord(ctx->ev0, s), "event");
         if (tensor)
-            CK(launch_tensor3(w, *res->t3, m, m1, sink, nullptr, res->single, res->pairs, t_status, s, ctx->sms),
+            CK(launch_tensor3(w, *res->t3, m, m1, sink, nullptr, res->single, res->pairs, res->triples, t_status, s,
+                              ctx->sms),
                "tensor kernel launch");
         else if (pair_major)
             CK(launch_elided4p(w, res->e4_begin, m, m1, sink, nullptr, res->single, res->pairs, res->triples, s,
@@ -780,8 +785,7 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
         e = cudaMemsetAsync(ctx->ctl + 16, 0, sizeof(int), s);
         if (e == cudaSuccess)
             e = launch_tensor3(w, *res->t3, 0, tensor_units(*res->t3, (int)order), sink, d, res->single, res->pairs,
-                               (int*)(ctx->ctl + 16),
-                               s, ctx->sms);
+                               res->triples, (int*)(ctx->ctl + 16), s, ctx->sms);
     } else if (e == cudaSuccess && e4_pair_major(kernel, res, w)) {
         if ((rc = ensure_e4_items(ctx, res))) {
             cudaFreeAsync(d, s);

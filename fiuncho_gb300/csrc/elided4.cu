@@ -151,38 +151,6 @@ std::vector<long long> e4p_item_begin(int snps) {
 
 size_t e4p_smem(int cw, int tw) { return (size_t)(kEThreads / 32) * 4 * (cw + tw) * sizeof(uint64_t); }
 
-// Locations of the sub-combination cores of the prefix triple (i, j, k) of one lane.
-struct E4Prefix {
-    const uint4* tijk;             // triple (i,j,k): cases word, controls word
-    const uint4 *pij, *pik, *pjk;  // pairs
-    const uint4 *si, *sj, *sk;     // singles
-};
-
-template <int PC>
-__device__ __forceinline__ long long e4p_pass(const uint32_t (&cp)[2][8], const E4Src& src, const E4Prefix& pre,
-                                              const long long* __restrict__ ftab, uint32_t nc, uint32_t* o) {
-    asm volatile("" ::: "memory");
-    const uint4 ta = __ldg(pre.tijk + (PC == 1 ? 1 : 0));
-    const uint4 tb = PC == 2 ? __ldg(pre.tijk + 1) : make_uint4(0, 0, 0, 0);
-    const uint4 pij = __ldg(pre.pij), pik = __ldg(pre.pik), pjk = __ldg(pre.pjk);
-    const uint4 si = __ldg(pre.si), sj = __ldg(pre.sj), sk = __ldg(pre.sk);
-    auto pr = [&](const uint4& v, int x, int y) { return by_pass<PC>(pcore(v, 0, x, y), pcore(v, 1, x, y)); };
-    auto sg = [&](const uint4& v, int x) { return by_pass<PC>(x ? v.y : v.x, x ? v.w : v.z); };
-    // star table of (i, j, k) for the pass
-    auto ps = [&](int q) -> uint32_t {
-        const int a = q / 9, b = (q / 3) % 3, z = q % 3;
-        if (a < 2 && b < 2 && z < 2) return PC == 2 ? tcell(ta, a, b, z) + tcell(tb, a, b, z) : tcell(ta, a, b, z);
-        if (a < 2 && b < 2) return pr(pij, a, b);
-        if (a < 2 && z < 2) return pr(pik, a, z);
-        if (b < 2 && z < 2) return pr(pjk, b, z);
-        if (a < 2) return sg(si, a);
-        if (b < 2) return sg(sj, b);
-        if (z < 2) return sg(sk, z);
-        return nc;
-    };
-    return e4_pass<PC>(cp, src, ps, ftab, nc, o);
-}
-
 __global__ void __launch_bounds__(kEThreads, 2)
     count_elided4p(ScanWork w, const long long* __restrict__ begin, long long g0, long long g1, CandSink sink,
                    uint32_t* dump, const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,

@@ -77,15 +77,15 @@ struct E4Src {
     const uint4* sl;   // single l: [class][x]
 };
 
-// One pass of the MI key over the 81 cells: the slices l = 0, 1, 2, each an
-// order-3 derivation from its star table (slice 2's is the prefix's star
-// table, pstar(q), minus slices 0 and 1: the derivation is linear).  Returns
-// the sum of T[cell] over the pass's 81 cells; writes the cells to
-// o[((x*3+y)*3+z)*3 + w] if o.  The counted cores arrive packed:
+// One pass over the 81 cells: the slices l = 0, 1, 2, each an order-3
+// derivation from its star table (slice 2's is the prefix's star table,
+// pstar(q), minus slices 0 and 1: the derivation is linear); use(sw, t)
+// receives each slice's 27 cells t[(x*3+y)*3+z] (cell index
+// ((x*3+y)*3+z)*3 + sw).  The counted cores arrive packed:
 // cp[cls][r] = core (r, w=0) | core (r, w=1) << 16.
-template <int PC, class PStar>
-__device__ __forceinline__ long long e4_pass(const uint32_t (&cp)[2][8], const E4Src& src, const PStar& pstar,
-                                             const long long* __restrict__ ftab, uint32_t nc, uint32_t* o) {
+template <int PC, class PStar, class Use>
+__device__ __forceinline__ void e4_slices(const uint32_t (&cp)[2][8], const E4Src& src, const PStar& pstar,
+                                          Use&& use) {
     asm volatile("" ::: "memory");
     const uint4 pil = __ldg(src.pil), pjl = __ldg(src.pjl), pkl = __ldg(src.pkl), sl = __ldg(src.sl);
     uint4 ta[3], tb[3];  // triple words of the pass's class(es)
@@ -116,13 +116,23 @@ __device__ __forceinline__ long long e4_pass(const uint32_t (&cp)[2][8], const E
         if (z < 2) return pr(pkl, z, w);
         return by_pass<PC>(w ? sl.y : sl.x, w ? sl.w : sl.z);
     };
-    long long part = 0;
 #pragma unroll
     for (int sw = 0; sw < 3; ++sw) {
         uint32_t t[27];
 #pragma unroll
         for (int q = 0; q < 27; ++q) t[q] = sw < 2 ? star(sw, q) : pstar(q) - star(0, q) - star(1, q);
         star_to_table(t);
+        use(sw, t);
+    }
+}
+
+// One pass of the exact key: the sum of T[cell] over the pass's 81 cells;
+// writes the cells to o[PC * 81 + ((x*3+y)*3+z)*3 + w] if o (cases, controls).
+template <int PC, class PStar>
+__device__ __forceinline__ long long e4_pass(const uint32_t (&cp)[2][8], const E4Src& src, const PStar& pstar,
+                                             const long long* __restrict__ ftab, uint32_t nc, uint32_t* o) {
+    long long part = 0;
+    e4_slices<PC>(cp, src, pstar, [&](int sw, const uint32_t* t) {
         // derived cells of consistent one-hot data never exceed the class
         // size; the clamp keeps any inconsistency inside the table
 #pragma unroll
@@ -131,8 +141,58 @@ __device__ __forceinline__ long long e4_pass(const uint32_t (&cp)[2][8], const E
 #pragma unroll
             for (int q = 0; q < 27; ++q) o[PC * 81 + q * 3 + sw] = t[q];
         }
-    }
+    });
     return part;
+}
+
+// Locations of the sub-combination cores of a prefix triple (i, j, k).
+struct E4Prefix {
+    const uint4* tijk;             // triple (i,j,k): cases word, controls word
+    const uint4 *pij, *pik, *pjk;  // pairs
+    const uint4 *si, *sj, *sk;     // singles
+};
+
+// Star table of the prefix triple for pass PC, entry q; nc = the pass's class size.
+template <int PC>
+struct E4PrefixStar {
+    uint4 ta, tb, pij, pik, pjk, si, sj, sk;
+    uint32_t nc;
+    __device__ __forceinline__ E4PrefixStar(const E4Prefix& pre, uint32_t n) : nc(n) {
+        asm volatile("" ::: "memory");
+        ta = __ldg(pre.tijk + (PC == 1 ? 1 : 0));
+        tb = PC == 2 ? __ldg(pre.tijk + 1) : make_uint4(0, 0, 0, 0);
+        pij = __ldg(pre.pij);
+        pik = __ldg(pre.pik);
+        pjk = __ldg(pre.pjk);
+        si = __ldg(pre.si);
+        sj = __ldg(pre.sj);
+        sk = __ldg(pre.sk);
+    }
+    __device__ __forceinline__ uint32_t pr(const uint4& v, int x, int y) const {
+        return by_pass<PC>(pcore(v, 0, x, y), pcore(v, 1, x, y));
+    }
+    __device__ __forceinline__ uint32_t sg(const uint4& v, int x) const {
+        return by_pass<PC>(x ? v.y : v.x, x ? v.w : v.z);
+    }
+    __device__ __forceinline__ uint32_t operator()(int q) const {
+        const int a = q / 9, b = (q / 3) % 3, z = q % 3;
+        if (a < 2 && b < 2 && z < 2) return PC == 2 ? tcell(ta, a, b, z) + tcell(tb, a, b, z) : tcell(ta, a, b, z);
+        if (a < 2 && b < 2) return pr(pij, a, b);
+        if (a < 2 && z < 2) return pr(pik, a, z);
+        if (b < 2 && z < 2) return pr(pjk, b, z);
+        if (a < 2) return sg(si, a);
+        if (b < 2) return sg(sj, b);
+        if (z < 2) return sg(sk, z);
+        return nc;
+    }
+};
+
+// Exact pass with the prefix star table computed from the prefix's cores.
+template <int PC>
+__device__ __forceinline__ long long e4p_pass(const uint32_t (&cp)[2][8], const E4Src& src, const E4Prefix& pre,
+                                              const long long* __restrict__ ftab, uint32_t nc, uint32_t* o) {
+    const E4PrefixStar<PC> ps(pre, nc);
+    return e4_pass<PC>(cp, src, ps, ftab, nc, o);
 }
 
 // One prefix (owned ordinal m): the TP threads of group grp, one last SNP per

@@ -175,14 +175,31 @@ struct T3Plan {
     double item2_combos = 0;
     CUtensorMap map_a2;   // box 128 B x 128 rows (i rows)
     CUtensorMap map_b2;   // box 128 B x 256 rows (j rows)
+    // order 4 (packed classes only): work items (i, j, 16 k, 128 l); item4_begin[j]
+    // = first item of the pairs with second SNP j, item4_per[j] = items per such pair
+    long long* item4_begin = nullptr;
+    long long* item4_per = nullptr;
+    long long total4 = 0;
+    double item4_combos = 0;
+    CUtensorMap map_k4;   // box 128 B x 32 rows (k rows)
 };
+// log2 of the control weight W = 4^h when both classes fit one FP32 accumulator
+// (n_cases < W, n_cases + W * n_ctrls < 2^24), else 0.
+int tensor_pack(int n_cases, int n_ctrls);
 long long tensor_units(const T3Plan& plan, int order);
 double tensor_item_combos(const T3Plan& plan, int order);
 cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s);
 void tensor3_release(T3Plan& plan);
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
-                           uint32_t* dump, const uint32_t* single, const uint4* pairs, int* status, cudaStream_t s,
-                           int sms);
+                           uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
+                           int* status, cudaStream_t s, int sms);
+// tensor4.cu -- order 4 on tcgen05 (one-hot data, packed classes, whole data set, one worker).
+std::vector<long long> t4_item_table(int n, std::vector<long long>& per);
+cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l, const CUtensorMap& map_k,
+                           const CUtensorMap& map_i, const long long* begin, const long long* per, int k_cases,
+                           int pack, long long g0, long long g1, const CandSink& sink, uint32_t* dump,
+                           const uint32_t* single, const uint4* pairs, const uint4* triples, int* status,
+                           cudaStream_t s, int sms);
 // Largest absolute error of the kernel's single-precision log2 over all its inputs (counts <= max_c).
 cudaError_t probe_lg2_error(unsigned max_c, double* max_abs_err, cudaStream_t s);
 

@@ -49,13 +49,12 @@
 #include <cmath>
 #include <cstring>
 
-#include "elided_prefix.cuh"
+#include "tensor_common.cuh"
 
 namespace fiu {
 
 constexpr int kT3J = 32, kT3L = 96;              // SNPs per tile
 constexpr int kT3M = 4 * kT3J, kT3N = 2 * kT3L;  // 128 x 192 GEMM tile
-constexpr int kT3KB = 128;                       // samples (= e4m3 bytes) per stage
 constexpr int kT3Stages = 4;
 constexpr int kT3SB = kT3N * kT3KB;              // 24 KB  l rows (1 KB multiple)
 constexpr int kT3SJ = 2 * kT3J * kT3KB;          //  8 KB  staged j rows
@@ -68,83 +67,10 @@ constexpr int kT3Stash = 32 * (kT3L / 2) * 4;    // per epilogue warp: 32 rows x
 constexpr size_t kT3Smem = 1024 + (size_t)kT3Stages * (kT3SB + kT3SJ + kT3SI) +
                            (size_t)kT3EpiWarps * (kT3Ebuf + kT3Stash);
 constexpr int kT3ColCtrl = kT3N, kT3ColA = 2 * kT3N;  // tensor-memory column bases
-constexpr unsigned long long kT3LimitNs = 2000000000ull;   // 2 s per wait
 constexpr uint32_t kT3Idesc = (1u << 4) | ((uint32_t)(kT3N >> 3) << 17) | ((uint32_t)(kT3M >> 4) << 24);
 
 static_assert(kT3Smem <= 227 * 1024 - 256, "tensor kernel shared memory");
 static_assert(kT3ColA + 32 * kT3Stages <= 512, "tensor memory columns");
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ unsigned long long t3_now() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ bool t3_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile("{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p;}"
-                 : "=r"(ok)
-                 : "r"(bar), "r"(parity)
-                 : "memory");
-    return ok != 0;
-}
-
-// Bounded wait on an mbarrier phase.  A wait that runs past the limit raises
-// the CTA's abort flag; every other waiter then gives up at once.
-__device__ __forceinline__ bool t3_wait(uint32_t bar, uint32_t parity, volatile int* abort) {
-    const unsigned long long t0 = t3_now();
-    for (;;) {
-        if (t3_try(bar, parity)) return true;
-        if (*abort) return false;
-        if (t3_now() - t0 > kT3LimitNs) {
-            *abort = 1;
-            return false;
-        }
-    }
-}
-
-// Bounded wait that ignores the abort flag (draining copies and MMAs in flight).
-__device__ __forceinline__ bool t3_drain(uint32_t bar, uint32_t parity) {
-    const unsigned long long t0 = t3_now();
-    for (;;) {
-        if (t3_try(bar, parity)) return true;
-        if (t3_now() - t0 > kT3LimitNs) return false;
-    }
-}
-
-__device__ __forceinline__ void t3_tma(uint32_t dst, const CUtensorMap* m, int x, int y, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-        "[%4];" ::"r"(dst),
-        "l"((uint64_t)m), "r"(x), "r"(y), "r"(bar)
-        : "memory");
-}
-
-// tcgen05 shared-memory descriptor, K-major with 128-byte swizzle: start >> 4,
-// leading byte offset 16 (unused for swizzled K-major), stride byte offset
-// 1024 (8 rows of 128 bytes), version 1 at bit 46, layout SWIZZLE_128B (2) at
-// bits 61-63.  Within the 128-byte swizzle atom the K offset is added to the
-// start address (tiles are 1024-byte aligned).
-__device__ __forceinline__ uint64_t t3_desc(uint32_t saddr) {
-    return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-
-__device__ __forceinline__ float u2f(uint32_t v) {  // exact for v < 2^23
-    return __uint_as_float(0x4B000000u | v) - 8388608.0f;
-}
-
-__device__ __forceinline__ uint32_t f2u(float f) {  // f an exact integer in [0, 2^23)
-    return __float_as_uint(f + 8388608.0f) & 0x7FFFFFu;
-}
-
-__device__ __forceinline__ float t3_lg2(float x) {
-    float r;
-    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
 
 // Work items of one i: J-tile a starts at j0 = i+1+32a and has
 // ceil((n-1-j0)/L) L-tiles starting at l0 = j0+1+L*b.
@@ -1263,17 +1189,19 @@ static cudaError_t t3_map(CUtensorMap* m, uint8_t* base, int rows, int pitch, in
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
-    // one accumulator for both classes when some W = 4^h (h <= 8, so 2^h is an e4m3 power of two) has
-    // n_cases < W and n_cases + W * n_ctrls < 2^24 (every count exact in FP32)
-    plan.pack = 0;
+// One accumulator for both classes when some W = 4^h (h <= 8, so 2^h is an
+// e4m3 power of two) has n_cases < W and n_cases + W * n_ctrls < 2^24 (every
+// count exact in FP32).
+int tensor_pack(int n_cases, int n_ctrls) {
     for (int h = 1; h <= 8; ++h) {
         const long long W = 1ll << (2 * h);
-        if (W > d.n_cases && d.n_cases + W * (long long)d.n_ctrls < (1ll << 24)) {
-            plan.pack = 2 * h;
-            break;
-        }
+        if (W > n_cases && n_cases + W * (long long)n_ctrls < (1ll << 24)) return 2 * h;
     }
+    return 0;
+}
+
+cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
+    plan.pack = tensor_pack(d.n_cases, d.n_ctrls);
     const int L = plan.pack ? kPL : kT3L;
     plan.item_combos = kT3J * L / 2.0;
     plan.k_cases = kT3KB * ((d.cw + 1) / 2);
@@ -1305,19 +1233,42 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
         e = cudaMemcpy(plan.item2_begin, ib2.data(), ib2.size() * sizeof(long long), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
     if ((e = t3_map(&plan.map_a2, plan.planes, rows, plan.pitch, kT2M, true)) != cudaSuccess) return e;
-    return t3_map(&plan.map_b2, plan.planes, rows, plan.pitch, kT2N, true);
+    if ((e = t3_map(&plan.map_b2, plan.planes, rows, plan.pitch, kT2N, true)) != cudaSuccess) return e;
+    // order 4 (packed classes)
+    if (!plan.pack || d.snps < 4) return cudaSuccess;
+    std::vector<long long> per4;
+    const std::vector<long long> ib4 = t4_item_table(d.snps, per4);
+    plan.total4 = ib4.back();
+    const double n = d.snps;
+    plan.item4_combos = n * (n - 1) * (n - 2) * (n - 3) / 24.0 / std::max(1ll, plan.total4);
+    e = cudaMalloc((void**)&plan.item4_begin, ib4.size() * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&plan.item4_per, per4.size() * sizeof(long long));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan.item4_begin, ib4.data(), ib4.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan.item4_per, per4.data(), per4.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    return t3_map(&plan.map_k4, plan.planes, rows, plan.pitch, 32, true);
 }
 
-long long tensor_units(const T3Plan& plan, int order) { return order == 2 ? plan.total2 : plan.total; }
-double tensor_item_combos(const T3Plan& plan, int order) { return order == 2 ? plan.item2_combos : plan.item_combos; }
+long long tensor_units(const T3Plan& plan, int order) {
+    return order == 2 ? plan.total2 : order == 4 ? plan.total4 : plan.total;
+}
+double tensor_item_combos(const T3Plan& plan, int order) {
+    return order == 2 ? plan.item2_combos : order == 4 ? plan.item4_combos : plan.item_combos;
+}
 
 void tensor3_release(T3Plan& plan) {
     cudaFree(plan.planes);
     cudaFree(plan.item_begin);
     cudaFree(plan.item2_begin);
+    cudaFree(plan.item4_begin);
+    cudaFree(plan.item4_per);
     plan.planes = nullptr;
     plan.item_begin = nullptr;
     plan.item2_begin = nullptr;
+    plan.item4_begin = nullptr;
+    plan.item4_per = nullptr;
 }
 
 // Bound on |single-precision estimate - exact key / (ln2 * 2^32)| over the 81
@@ -1369,8 +1320,11 @@ cudaError_t probe_lg2_error(unsigned max_c, double* max_abs_err, cudaStream_t s)
 }
 
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
-                           uint32_t* dump, const uint32_t* single, const uint4* pairs, int* status, cudaStream_t s,
-                           int sms) {
+                           uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
+                           int* status, cudaStream_t s, int sms) {
+    if (w.order == 4)
+        return launch_tensor4(w, plan.map_l, plan.map_k4, plan.map_i, plan.item4_begin, plan.item4_per, plan.k_cases,
+                              plan.pack, g0, g1, sink, dump, single, pairs, triples, status, s, sms);
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);

@@ -1,0 +1,487 @@
+// Order-4 contingency tables on the 5th-generation tensor cores (tcgen05).
+//
+// For one-hot data the 16 core cells of a combination (i, j, k, l) --
+// genotypes x, y, z, w in {0, 1} -- are dot products over the samples:
+//     core[x][y][z][w] = sum_s a_ix(s) a_jy(s) a_kz(s) a_lw(s).
+// A work item is (i, j, 16 consecutive k, 128 consecutive l); it is one GEMM
+//     D[(k,x,y,z), (l,w)] = sum_s A[(k,x,y,z), s] B[(l,w), s]   (M 128, N 256)
+// over the e4m3 operand planes of tensor3.cu, both classes in one FP32
+// accumulator (control samples weighted by W = 4^h, exact while
+// n_cases < W and n_cases + W * n_ctrls < 2^24; data sets whose classes do
+// not pack use the CUDA-core pair-major kernel).  B rows are plane rows 2l+w
+// by TMA; A rows are the bytewise AND of the i, j and k plane rows, built in
+// shared memory by six producer warps from the TMA-staged rows (i AND j once
+// per stage, then AND each k row).  Two accumulator regions alternate between
+// items so the next item's GEMM overlaps the epilogue.
+//
+// Epilogue.  Each thread reads the accumulators of one row (k, x, y, z); a
+// swizzled shared-memory transpose gives each lane the 16 core counts of one
+// combination.  The 81-cell tables follow exactly (slice by slice, from the
+// triple, pair and single cores, as in the CUDA-core order-4 kernels).  A
+// bounded estimate of the MI key -- single-precision c*lg2(c) terms summed
+// pairwise per 27-cell slice, slices summed in 64-bit fixed point -- rejects
+// the combinations that cannot reach the threshold; the others get the exact
+// 64-bit fixed-point key from the integer c*ln(c) table.
+//
+// Reference semantics: GenotypeTable::combine_and_popcnt for order 4
+// (src/base/gt_popcnt.cpp:4-35) and MutualInformation::compute
+// (src/base/mutual_information.cpp:8-39) over the combinations
+// ThreadedSearch visits (include/fiuncho/ThreadedSearch.h:157-180) with one
+// worker.
+#include <algorithm>
+#include <cmath>
+
+#include "elided4_prefix.cuh"
+#include "tensor_common.cuh"
+
+namespace fiu {
+
+constexpr int kT4K = 16, kT4L = 128;                // k and l SNPs per work item
+constexpr int kT4M = 8 * kT4K, kT4N = 2 * kT4L;     // 128 x 256 GEMM tile
+constexpr int kT4BuildWarps = 6, kT4EpiWarps = 8;
+constexpr int kT4Threads = 32 * (2 + kT4BuildWarps + kT4EpiWarps);  // 512
+constexpr int kT4Stages = 3;
+constexpr int kT4SB = kT4N * kT3KB;                 // 32 KB  l rows
+constexpr int kT4SA = kT4M * kT3KB;                 // 16 KB  A (k, x, y, z)
+constexpr int kT4SK = 2 * kT4K * kT3KB;             //  4 KB  k rows
+constexpr int kT4SI = 1024;                         // i rows (2 x 128 B) in a 1 KB slot
+constexpr int kT4SJ = 1024;                         // j rows
+constexpr int kT4Stage = kT4SB + kT4SA + kT4SK + kT4SI + kT4SJ;  // 54 KB, a multiple of 1 KB
+constexpr int kT4Ebuf = 4096;                       // per epilogue warp: 32 combinations x 8 (x,y,z) x 16 B
+constexpr size_t kT4Smem = 1024 + (size_t)kT4Stages * kT4Stage + (size_t)kT4EpiWarps * kT4Ebuf;
+constexpr uint32_t kT4Idesc = (1u << 4) | ((uint32_t)(kT4N >> 3) << 17) | ((uint32_t)(kT4M >> 4) << 24);
+constexpr uint32_t kT4Tx = kT4SB + kT4SK + 2 * 2 * kT3KB;  // bytes the TMA brings per stage
+static_assert(kT4Smem <= 227 * 1024 - 256, "order-4 tensor kernel shared memory");
+static_assert(2 * kT4N <= 512, "order-4 tensor kernel tensor memory");
+
+struct T4Maps {
+    CUtensorMap l, k, i;  // boxes of 256, 32 and 2 plane rows
+};
+
+// Items of one pair (i, j): for k-tiles k0 = j + 1 + 16 a (k0 <= n - 2),
+// ceil((n - 1 - k0) / 128) l-tiles l0 = k0 + 1 + 128 b.
+__host__ __device__ inline long long t4_items_per_pair(int n, int j) {
+    long long c = 0;
+    for (int k0 = j + 1; k0 <= n - 2; k0 += kT4K) c += (n - 1 - k0 + kT4L - 1) / kT4L;
+    return c;
+}
+
+// Item g -> (i, j, k0, l0).  begin[j]: first item of the pairs with second
+// element j (j pairs of per[j] items each).
+__device__ __forceinline__ void t4_decode(const long long* __restrict__ begin, const long long* __restrict__ per,
+                                          int n, long long g, int& i, int& j, int& k0, int& l0) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(begin + mid) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    j = lo;
+    const long long pj = __ldg(per + j);
+    const long long rel = g - __ldg(begin + j);
+    i = (int)(rel / pj);
+    long long q = rel - (long long)i * pj;
+    for (int k = j + 1;; k += kT4K) {
+        const long long nl = (n - 1 - k + kT4L - 1) / kT4L;
+        if (q < nl) {
+            k0 = k;
+            l0 = k + 1 + kT4L * (int)q;
+            return;
+        }
+        q -= nl;
+    }
+}
+
+// 16-byte chunk of the epilogue transpose buffer holding (cases w0, w1,
+// controls w0, w1) of row (kk, xyz) for the column group ll; conflict-free for
+// the row-wise writes (fixed ll) and the combination-wise reads (fixed xyz).
+__device__ __forceinline__ int t4_chunk(int kk, int ll, int xyz) { return (kk * 8 + ll) * 8 + (xyz ^ ll); }
+
+// Sum of 27 floats, pairwise (every term takes part in at most 5 roundings).
+__device__ __forceinline__ float t4_sum27(const float* f) {
+    float a[14];
+#pragma unroll
+    for (int q = 0; q < 13; ++q) a[q] = f[2 * q] + f[2 * q + 1];
+    a[13] = f[26];
+    float b[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) b[q] = a[2 * q] + a[2 * q + 1];
+    const float c0 = b[0] + b[1], c1 = b[2] + b[3], c2 = b[4] + b[5], c3 = b[6];
+    return (c0 + c1) + (c2 + c3);
+}
+
+// Estimate of one pass of the key in units of 2^-16 bits: per slice the
+// single-precision sum of c*lg2(c) over its 27 cells, rounded to 2^-16.
+template <int PC>
+__device__ __forceinline__ long long t4_estimate_pass(const uint32_t (&cp)[2][8], const E4Src& src,
+                                                      const E4Prefix& pre, uint32_t nc) {
+    const float tiny = 9.5367431640625e-07f;  // 2^-20: c*lg2(c + tiny) = 0 at c = 0
+    const E4PrefixStar<PC> ps(pre, nc);
+    long long acc = 0;
+    e4_slices<PC>(cp, src, ps, [&](int, const uint32_t* t) {
+        float f[27];
+#pragma unroll
+        for (int q = 0; q < 27; ++q) {
+            const float c = u2f(min(t[q], nc));
+            f[q] = c * t3_lg2(c + tiny);
+        }
+        acc += __float2ll_rn(t4_sum27(f) * 65536.0f);
+    });
+    return acc;
+}
+
+// Exact key of one combination (and its tables when o): the rare path, kept
+// out of line so that its registers do not weigh on the estimate.
+__device__ __noinline__ long long t4_exact(const DevData& d, const uint32_t (&cp)[2][8], const E4Src& src,
+                                           const E4Prefix& pre, uint32_t* o) {
+    long long key = e4p_pass<0>(cp, src, pre, d.ftab, d.n_cases, o);
+    key += e4p_pass<1>(cp, src, pre, d.ftab, d.n_ctrls, o);
+    key -= e4p_pass<2>(cp, src, pre, d.ftab, d.n_cases + d.n_ctrls, o);
+    return key;
+}
+
+__device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink, long long thr_q, uint32_t* dump,
+                                        const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
+                                        const uint4* __restrict__ triples, const uint32_t (&cp)[2][8], int i, int j,
+                                        int k, int l, bool valid, int lane) {
+    const DevData& d = w.d;
+    const int n = d.snps;
+    long long key = w.base_key;
+    bool pass = false;
+    if (valid) {
+        const uint4* single4 = reinterpret_cast<const uint4*>(single);
+        E4Src src;
+        src.tij = triples + 2 * triple_index(i, j, l, n);
+        src.tik = triples + 2 * triple_index(i, k, l, n);
+        src.tjk = triples + 2 * triple_index(j, k, l, n);
+        src.pil = pairs + pair_index(i, l, n);
+        src.pjl = pairs + pair_index(j, l, n);
+        src.pkl = pairs + pair_index(k, l, n);
+        src.sl = single4 + l;
+        E4Prefix pre;
+        pre.tijk = triples + 2 * triple_index(i, j, k, n);
+        pre.pij = pairs + pair_index(i, j, n);
+        pre.pik = pairs + pair_index(i, k, n);
+        pre.pjk = pairs + pair_index(j, k, n);
+        pre.si = single4 + i;
+        pre.sj = single4 + j;
+        pre.sk = single4 + k;
+        bool cand = dump != nullptr;
+        if (!cand) {
+            const long long est = t4_estimate_pass<0>(cp, src, pre, d.n_cases) +
+                                  t4_estimate_pass<1>(cp, src, pre, d.n_ctrls) -
+                                  t4_estimate_pass<2>(cp, src, pre, d.n_cases + d.n_ctrls);
+            cand = est >= thr_q;
+        }
+        if (cand) {
+            uint32_t* o = dump ? dump + ((size_t)triple_index(i, j, k, n) * n + l) * 2 * 81 : nullptr;
+            key += t4_exact(d, cp, src, pre, o);
+            pass = key >= sink.thr;
+        }
+    }
+    if (sink.evaluated) {
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0 && vm) atomicAdd(sink.evaluated, (unsigned long long)__popc(vm));
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, pass);
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(sink.count, (unsigned)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (pass) {
+            const unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (idx < sink.cap) {
+                const int c[4] = {i, j, k, l};
+                sink.buf[idx] = Cand{key, pack_code(c, 4, w.bits)};
+            } else {
+                atomicOr(sink.overflow, 1u);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kT4Threads, 1)
+    tensor4p_kernel(const __grid_constant__ T4Maps maps, ScanWork w, const long long* __restrict__ begin,
+                    const long long* __restrict__ per, long long g0, long long g1, int k_cases, int pack,
+                    CandSink sink, long long thr_q, uint32_t* dump, const uint32_t* __restrict__ single,
+                    const uint4* __restrict__ pairs, const uint4* __restrict__ triples, int* status) {
+    extern __shared__ uint8_t smraw[];
+    __shared__ __align__(8) uint64_t full_t[kT4Stages], full_a[kT4Stages], empty[kT4Stages];
+    __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);  // stages: B | A | k | i | j
+    uint32_t* ebuf_all = reinterpret_cast<uint32_t*>(sm + kT4Stages * kT4Stage);
+    volatile int* abort = &abort_flag;
+    const DevData& d = w.d;
+    const int n = d.snps;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ks_c = k_cases / kT3KB;
+    const int ksteps = ks_c + (d.tw + 1) / 2;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kT4Stages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_t[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_a[s])), "r"(kT4BuildWarps));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[b])), "r"(kT4EpiWarps));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        abort_flag = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+
+    if (warp == 0) {
+        // ---------------------------------------------------------------- TMA producer
+        if (lane == 0) {
+            long long step = 0;
+            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+                int i, j, k0, l0;
+                t4_decode(begin, per, n, g, i, j, k0, l0);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const int s = (int)(step % kT4Stages);
+                    const long long u = step / kT4Stages;
+                    if (u > 0 && !t3_wait(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    const int kb = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
+                    uint8_t* st = sm + s * kT4Stage;
+                    const uint32_t bar = smem_u32(&full_t[s]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kT4Tx)
+                                 : "memory");
+                    t3_tma(smem_u32(st), &maps.l, kb, 2 * l0, bar);
+                    t3_tma(smem_u32(st + kT4SB + kT4SA), &maps.k, kb, 2 * k0, bar);
+                    t3_tma(smem_u32(st + kT4SB + kT4SA + kT4SK), &maps.i, kb, 2 * i, bar);
+                    t3_tma(smem_u32(st + kT4SB + kT4SA + kT4SK + kT4SI), &maps.i, kb, 2 * j, bar);
+                    ++step;
+                }
+            }
+            for (int s = 0; s < kT4Stages; ++s) {
+                if (step <= s) continue;
+                const long long last = s + ((step - 1 - s) / kT4Stages) * kT4Stages;
+                if (!t3_drain(smem_u32(&full_t[s]), (uint32_t)((last / kT4Stages) & 1))) ok = false;
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            long long step = 0, item = 0;
+            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+                const int buf = (int)(item & 1);
+                if (item >= 2 && !t3_wait(smem_u32(&acc_empty[buf]), (uint32_t)(((item >> 1) - 1) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t dcol = tmem + (uint32_t)(kT4N * buf);
+                for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                    const int s = (int)(step % kT4Stages);
+                    if (!t3_wait(smem_u32(&full_a[s]), (uint32_t)((step / kT4Stages) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t sb = smem_u32(sm + s * kT4Stage), sa = sb + kT4SB;
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint64_t ad = t3_desc(sa + 32 * kk), bd = t3_desc(sb + 32 * kk);
+                        const uint32_t acc = (ks == 0 && kk == 0) ? 0u : 1u;
+                        asm volatile(
+                            "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
+                            "l"(ad), "l"(bd), "r"(kT4Idesc), "r"(acc));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                        smem_u32(&empty[s])));
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(&acc_full[buf])));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&done)));
+            if (!t3_drain(smem_u32(&done), 0)) ok = false;
+        }
+    } else if (warp < 2 + kT4BuildWarps) {
+        // ---------------------------------------------------------------- A builders (shared memory)
+        const int t = tid - 64;  // 0 .. 32 * kT4BuildWarps - 1
+        const int c = t & 7;     // 16-byte chunk; 8 consecutive threads cover one 128-byte row
+        long long step = 0;
+        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+            for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                const int s = (int)(step % kT4Stages);
+                if (!t3_wait(smem_u32(&full_t[s]), (uint32_t)((step / kT4Stages) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t* st = sm + s * kT4Stage;
+                uint8_t* sA = st + kT4SB;
+                const uint8_t* sK = sA + kT4SA;
+                const uint8_t* sI = sK + kT4SK;
+                const uint8_t* sJ = sI + kT4SI;
+                // 128-byte swizzle: chunk c of box row r sits at chunk c ^ (r & 7)
+                const uint4 i0 = *reinterpret_cast<const uint4*>(sI + (c << 4));
+                const uint4 i1 = *reinterpret_cast<const uint4*>(sI + 128 + ((c ^ 1) << 4));
+                const uint4 j0 = *reinterpret_cast<const uint4*>(sJ + (c << 4));
+                const uint4 j1 = *reinterpret_cast<const uint4*>(sJ + 128 + ((c ^ 1) << 4));
+                uint4 ij[4];  // (x, y) = (0,0), (0,1), (1,0), (1,1)
+                ij[0] = make_uint4(i0.x & j0.x, i0.y & j0.y, i0.z & j0.z, i0.w & j0.w);
+                ij[1] = make_uint4(i0.x & j1.x, i0.y & j1.y, i0.z & j1.z, i0.w & j1.w);
+                ij[2] = make_uint4(i1.x & j0.x, i1.y & j0.y, i1.z & j0.z, i1.w & j0.w);
+                ij[3] = make_uint4(i1.x & j1.x, i1.y & j1.y, i1.z & j1.z, i1.w & j1.w);
+                for (int r = t >> 3; r < 2 * kT4K; r += 4 * kT4BuildWarps) {  // k row r = (kk, z)
+                    const uint4 kv = *reinterpret_cast<const uint4*>(sK + r * 128 + ((c ^ (r & 7)) << 4));
+                    const int kk = r >> 1, z = r & 1;
+#pragma unroll
+                    for (int xy = 0; xy < 4; ++xy) {
+                        const int m = kk * 8 + xy * 2 + z;  // A row (kk, x, y, z)
+                        const uint4 v = make_uint4(ij[xy].x & kv.x, ij[xy].y & kv.y, ij[xy].z & kv.z, ij[xy].w & kv.w);
+                        *reinterpret_cast<uint4*>(sA + m * 128 + ((c ^ (m & 7)) << 4)) = v;
+                    }
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_a[s])) : "memory");
+            }
+        }
+    } else {
+        // ---------------------------------------------------------------- epilogue
+        const int e = warp - (2 + kT4BuildWarps);  // 0..7
+        const int q = warp & 3;                     // tensor-memory lane quarter this warp may access
+        const int hh = e >> 2;                      // column half: l offsets [64 hh, 64 hh + 64)
+        uint32_t* ebuf = ebuf_all + e * (kT4Ebuf / 4);
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+        const uint32_t wmask = (1u << pack) - 1u;
+        const int kkw = lane >> 3, xyz = lane & 7;  // this thread's accumulator row (4 q + kkw, xyz)
+        const int kkc = lane >> 3, llc = lane & 7;  // this lane's combination in a column group
+        long long item = 0;
+        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+            int i, j, k0, l0;
+            t4_decode(begin, per, n, g, i, j, k0, l0);
+            const int buf = (int)(item & 1);
+            const int k = k0 + 4 * q + kkc;
+            if (!t3_wait(smem_u32(&acc_full[buf]), (uint32_t)((item >> 1) & 1), abort)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+            for (int cc = 0; cc < 8; ++cc) {
+                {
+                    const uint32_t col = (uint32_t)(kT4N * buf + 128 * hh + 16 * cc);
+                    uint32_t v[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
+                        "15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(lane_base + col));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (cc == 7) {  // last read of this item's accumulators: the region is free
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
+                                         : "memory");
+                    }
+#pragma unroll
+                    for (int ll = 0; ll < 8; ++ll) {
+                        const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * ll]));
+                        const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * ll + 1]));
+                        *reinterpret_cast<uint4*>(ebuf + 4 * t4_chunk(kkw, ll, xyz)) =
+                            make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                    }
+                }
+                __syncwarp();
+                uint32_t cp[2][8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const uint4 c4 = *reinterpret_cast<const uint4*>(ebuf + 4 * t4_chunk(kkc, llc, r));
+                    cp[0][r] = c4.x | (c4.y << 16);
+                    cp[1][r] = c4.z | (c4.w << 16);
+                }
+                __syncwarp();
+                const int l = l0 + 64 * hh + 8 * cc + llc;
+                const bool valid = k < n && l < n && l > k;
+                t4_eval(w, sink, thr_q, dump, single, pairs, triples, cp, i, j, valid ? k : 2, valid ? l : 3, valid,
+                        lane);
+            }
+        }
+    }
+    if (!ok) *abort = 1;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 0 && abort_flag) atomicOr(status, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+// Bound (in bits) on |estimate - exact key / (ln2 * 2^32)| over the 243 terms
+// of one combination (81 cells x cases, controls, totals), N samples:
+// the products c*lg2 and the pairwise sums of a 27-term slice round every
+// term at most 6 times (2^-24 each) and sum |c*lg2(c)| over all terms is at
+// most B = 2 N lg2 N; lg2.approx is within 2^-18 of log2 on every input the
+// kernel can see (checked exhaustively by fiu_probe_lg2_error) and sum c over
+// all terms is 2 N; the c + 2^-20 shift moves each term by at most
+// 2^-20 / ln 2, its rounding each count's logarithm by at most 2^-24 / ln 2;
+// each of the 9 slice sums rounds by 2^-17 in fixed point; the integer table
+// rounds each term by 1/2 of 2^-32 nats.  Doubled.
+double t4_margin(int n_samples) {
+    const double N = n_samples, lgN = std::log2(std::max(2.0, N)), B = 2 * N * lgN;
+    const double u = std::ldexp(1.0, -24), e20 = std::ldexp(1.0, -20), e_lg2 = std::ldexp(1.0, -18);
+    const double T = 243;
+    const double err = 6 * u * B + 2 * N * e_lg2 + T * e20 / std::log(2.0) + 2 * N * u / std::log(2.0) +
+                       9 * std::ldexp(1.0, -17) + T * 0.5 / (std::log(2.0) * 4294967296.0);
+    return 2 * err + 1e-3;
+}
+
+std::vector<long long> t4_item_table(int n, std::vector<long long>& per) {
+    std::vector<long long> begin((size_t)n + 1, 0);
+    per.assign((size_t)std::max(n, 1), 0);
+    for (int j = 0; j < n; ++j) {
+        per[j] = t4_items_per_pair(n, j);
+        begin[j + 1] = begin[j] + (long long)j * per[j];
+    }
+    return begin;
+}
+
+cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l, const CUtensorMap& map_k,
+                           const CUtensorMap& map_i, const long long* begin, const long long* per, int k_cases,
+                           int pack, long long g0, long long g1, const CandSink& sink, uint32_t* dump,
+                           const uint32_t* single, const uint4* pairs, const uint4* triples, int* status,
+                           cudaStream_t s, int sms) {
+    if (!pack || !triples || !pairs || !single) return cudaErrorInvalidValue;
+    static LaunchCache cache;
+    int per_sm = 1;
+    cudaError_t e = blocks_per_sm(cache, tensor4p_kernel, kT4Threads, kT4Smem, per_sm);
+    if (e != cudaSuccess) return e;
+    const long long items = g1 - g0;
+    if (items <= 0) return cudaSuccess;
+    // threshold of the estimate in units of 2^-16 bits
+    const double scale = 65536.0 / (std::log(2.0) * 4294967296.0);
+    const double thr = ((double)sink.thr - (double)w.base_key) * scale - t4_margin(w.d.n_cases + w.d.n_ctrls) * 65536.0;
+    const long long thr_q = (long long)std::floor(std::max(-9.0e18, std::min(9.0e18, thr)));
+    T4Maps maps{map_l, map_k, map_i};
+    const unsigned grid = (unsigned)(items < sms ? items : sms);
+    tensor4p_kernel<<<grid, kT4Threads, kT4Smem, s>>>(maps, w, begin, per, g0, g1, k_cases, pack, sink, thr_q, dump,
+                                                      single, pairs, triples, status);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace fiu

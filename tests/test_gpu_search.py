@@ -71,7 +71,10 @@ def test_hot_kernel_tables_bit_exact_reference(gs, golden_testdata, order, kerne
     """Each counting kernel's own contingency tables for EVERY combination of the
     reference's test data == the reference's combine_and_popcnt tables
     (kernel 1: full table; 2, 3: core cells + exact marginals, POPC / Harley-Seal,
-    at order 4 from triple cores; 4: core cells on the tcgen05 tensor cores)."""
+    at order 4 from triple cores; 4: core cells on the tcgen05 tensor cores -- not at
+    order 4, whose tcgen05 form needs classes that share one accumulator, which the
+    9 000 / 9 800 samples here do not; it is checked against kernel 1 at tile edges and
+    against the reference's own order-4 top-50 on the synthetic fixture)."""
     from fiuncho_gb300 import Distribution, Resident
     ds = _ds_from_golden(golden_testdata)
     res = Resident(gs.ctx, ds)
@@ -157,6 +160,7 @@ def test_search_synth_vs_reference(gs, oracle, golden_synth, order):
     from fiuncho_gb300 import Dataset, Distribution
     ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
     res, v64 = gs.run(ds, order, Distribution(ds.snps, order - 1), 50, with_fp64=True)
+    assert gs.last_tile()[0] == 4  # one-hot, whole data set, classes that pack: tcgen05 at every order
     got = _check_topn(oracle, ds, order, 50, res, v64)
     rc = golden_synth["o%d_top50_combos" % order]
     rv = golden_synth["o%d_top50_vals" % order].astype(np.float64)
@@ -270,9 +274,9 @@ def test_kernels_agree(oracle, n_case, n_ctrl, snps):
                                                  (130, 1, 23), (511, 1537, 33)])
 def test_order4_kernels_agree(oracle, n_case, n_ctrl, snps):
     """Order 4: the reduced-work kernels (16 core cells counted, 65 derived from
-    triple, pair and single cores; POPC and Harley-Seal counting) give the full
-    kernel's tables for every combination and the same top-N, which matches the
-    oracle."""
+    triple, pair and single cores; POPC and Harley-Seal counting) and the tcgen05
+    kernel give the full kernel's tables for every combination and the same top-N,
+    which matches the oracle."""
     from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident
     rng = np.random.default_rng(n_case * 3 + n_ctrl + snps)
     maf = rng.uniform(0.05, 0.5, snps)[:, None]
@@ -281,7 +285,7 @@ def test_order4_kernels_agree(oracle, n_case, n_ctrl, snps):
     ds = Dataset.from_genotypes(geno, np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)])
     dist = Distribution(snps, 3)
     outs, tabs = [], []
-    for kernel in (1, 2, 3):
+    for kernel in (1, 2, 3, 4):  # every class pair here shares one tensor accumulator
         g = GpuSearch(0, kernel=kernel)
         res = Resident(g.ctx, ds)
         tabs.append(g.scan_tables(res, 4, dist, kernel=kernel))
@@ -306,6 +310,51 @@ def test_order4_kernels_agree(oracle, n_case, n_ctrl, snps):
         assert np.array_equal(g.scan_tables(res, 4, layer, kernel=kernel)[mask], full[mask])
 
 
+@pytest.mark.parametrize("snps,n_case,n_ctrl", [(4, 1, 1), (5, 65, 63), (18, 130, 1), (20, 64, 64),
+                                                (33, 4000, 4000), (40, 700, 2500)])
+def test_tensor4_tile_edges(oracle, snps, n_case, n_ctrl):
+    """Order-4 tcgen05 kernel vs the full-table kernel around the 16-k work item (one
+    accumulator for both classes): identical tables for every combination and identical
+    top-N lists, checked against the oracle."""
+    from fiuncho_gb300 import Distribution, GpuSearch, Resident
+    ds = _one_hot_dataset(snps * 3 + n_case, snps, n_case, n_ctrl)
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    dist = Distribution(snps, 3)
+    full = g.scan_tables(res, 4, dist, kernel=1)
+    tens = g.scan_tables(res, 4, dist, kernel=4)
+    mask = full != 0xFFFFFFFF
+    assert mask.sum() == math.comb(snps, 4) * 2 * 81
+    assert np.array_equal(tens[mask], full[mask])
+    out = min(20, math.comb(snps, 4))
+    g.set_kernel(1)
+    a = g.run(res, 4, dist, out, with_fp64=True)
+    g.set_kernel(4)
+    b = g.run(res, 4, dist, out, with_fp64=True)
+    assert g.last_tile() == (4, 256)
+    assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
+    _check_topn(oracle, ds, 4, out, b[0], b[1])
+
+
+@pytest.mark.parametrize("snps,n_case,n_ctrl,out", [(150, 300, 300, 30), (145, 1000, 900, 5)])
+def test_tensor4_search_many_tiles(oracle, snps, n_case, n_ctrl, out):
+    """Order-4 tcgen05 search over SNP counts spanning several 128-l tiles, with a
+    tight threshold where the bounded estimate rejects nearly every combination:
+    the result equals the exact pair-major kernel's and the oracle's."""
+    from fiuncho_gb300 import Distribution, GpuSearch, Resident
+    ds = _one_hot_dataset(snps + n_case, snps, n_case, n_ctrl)
+    g = GpuSearch(0)
+    res = Resident(g.ctx, ds)
+    dist = Distribution(snps, 3)
+    g.set_kernel(2)
+    a = g.run(res, 4, dist, out, with_fp64=True)
+    g.set_kernel(4)
+    b = g.run(res, 4, dist, out, with_fp64=True)
+    assert g.last_tile()[0] == 4
+    assert [x.combination for x in a[0]] == [x.combination for x in b[0]] and np.array_equal(a[1], b[1])
+    _check_topn(oracle, ds, 4, out, b[0], b[1], threads=16)
+
+
 def test_order4_reduced_work_is_automatic(gs, golden_synth):
     """One-hot order-4 searches pick a reduced-work kernel by themselves, also for a
     Distribution layer (step > 1) of the prefixes; non-one-hot data keeps the full kernel."""
@@ -314,7 +363,7 @@ def test_order4_reduced_work_is_automatic(gs, golden_synth):
     g = GpuSearch(0)
     res = Resident(g.ctx, ds)
     g.run(res, 4, Distribution(ds.snps, 3), 10)
-    assert g.last_tile()[0] in (2, 3)
+    assert g.last_tile()[0] in (2, 3, 4)
     g.run(res, 4, Distribution(ds.snps, 3, 3, 2), 10)
     assert g.last_tile()[0] in (2, 3)
     rng = np.random.default_rng(5)
@@ -341,7 +390,7 @@ def test_tensor_kernel_scope(gs, golden_synth):
     with pytest.raises(FiunchoError):
         g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
     with pytest.raises(FiunchoError):
-        g.run(res, 4, Distribution(ds.snps, 3), 10)
+        g.run(res, 5, Distribution(ds.snps, 4), 10)
 
 
 def test_elided_rejects_non_one_hot(gs):
