@@ -77,6 +77,31 @@ struct E4Src {
     const uint4* sl;   // single l: [class][x]
 };
 
+// Sub-combination cores of one combination as read by one pass PC: the triple
+// words of the pass's class (ta: cases, or controls for PC 1; tb: controls for
+// PC 2, else zero) of (i,j,l), (i,k,l), (j,k,l), and the pair / single words.
+struct E4Words {
+    uint4 ta[3], tb[3];
+    uint4 pil, pjl, pkl, sl;
+};
+
+template <int PC>
+__device__ __forceinline__ E4Words e4_load(const E4Src& src) {
+    asm volatile("" ::: "memory");
+    E4Words wd;
+    const uint4* tp[3] = {src.tij, src.tik, src.tjk};
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+        wd.ta[u] = __ldg(tp[u] + (PC == 1 ? 1 : 0));
+        wd.tb[u] = PC == 2 ? __ldg(tp[u] + 1) : make_uint4(0, 0, 0, 0);
+    }
+    wd.pil = __ldg(src.pil);
+    wd.pjl = __ldg(src.pjl);
+    wd.pkl = __ldg(src.pkl);
+    wd.sl = __ldg(src.sl);
+    return wd;
+}
+
 // One pass over the 81 cells: the slices l = 0, 1, 2, each an order-3
 // derivation from its star table (slice 2's is the prefix's star table,
 // pstar(q), minus slices 0 and 1: the derivation is linear); use(sw, t)
@@ -84,22 +109,10 @@ struct E4Src {
 // ((x*3+y)*3+z)*3 + sw).  The counted cores arrive packed:
 // cp[cls][r] = core (r, w=0) | core (r, w=1) << 16.
 template <int PC, class PStar, class Use>
-__device__ __forceinline__ void e4_slices(const uint32_t (&cp)[2][8], const E4Src& src, const PStar& pstar,
-                                          Use&& use) {
-    asm volatile("" ::: "memory");
-    const uint4 pil = __ldg(src.pil), pjl = __ldg(src.pjl), pkl = __ldg(src.pkl), sl = __ldg(src.sl);
-    uint4 ta[3], tb[3];  // triple words of the pass's class(es)
-    {
-        const uint4* tp[3] = {src.tij, src.tik, src.tjk};
-#pragma unroll
-        for (int u = 0; u < 3; ++u) {
-            ta[u] = __ldg(tp[u] + (PC == 1 ? 1 : 0));
-            tb[u] = PC == 2 ? __ldg(tp[u] + 1) : make_uint4(0, 0, 0, 0);
-        }
-    }
-    // ta holds the pass's class (controls for PC 1), tb the controls for PC 2
+__device__ __forceinline__ void e4_slices_w(const uint32_t (&cp)[2][8], const E4Words& wd, const PStar& pstar,
+                                            Use&& use) {
     auto tri = [&](int u, int x, int y, int z) {
-        return PC == 2 ? tcell(ta[u], x, y, z) + tcell(tb[u], x, y, z) : tcell(ta[u], x, y, z);
+        return PC == 2 ? tcell(wd.ta[u], x, y, z) + tcell(wd.tb[u], x, y, z) : tcell(wd.ta[u], x, y, z);
     };
     auto pr = [&](const uint4& v, int x, int y) { return by_pass<PC>(pcore(v, 0, x, y), pcore(v, 1, x, y)); };
     auto star = [&](int w, int q) -> uint32_t {
@@ -111,10 +124,10 @@ __device__ __forceinline__ void e4_slices(const uint32_t (&cp)[2][8], const E4Sr
         if (a < 2 && b < 2) return tri(0, a, b, w);
         if (a < 2 && z < 2) return tri(1, a, z, w);
         if (b < 2 && z < 2) return tri(2, b, z, w);
-        if (a < 2) return pr(pil, a, w);
-        if (b < 2) return pr(pjl, b, w);
-        if (z < 2) return pr(pkl, z, w);
-        return by_pass<PC>(w ? sl.y : sl.x, w ? sl.w : sl.z);
+        if (a < 2) return pr(wd.pil, a, w);
+        if (b < 2) return pr(wd.pjl, b, w);
+        if (z < 2) return pr(wd.pkl, z, w);
+        return by_pass<PC>(w ? wd.sl.y : wd.sl.x, w ? wd.sl.w : wd.sl.z);
     };
 #pragma unroll
     for (int sw = 0; sw < 3; ++sw) {
@@ -124,6 +137,15 @@ __device__ __forceinline__ void e4_slices(const uint32_t (&cp)[2][8], const E4Sr
         star_to_table(t);
         use(sw, t);
     }
+}
+
+// The same with the words loaded from their locations (the loads of a pass are
+// not hoisted above the previous pass: fewer registers held across passes).
+template <int PC, class PStar, class Use>
+__device__ __forceinline__ void e4_slices(const uint32_t (&cp)[2][8], const E4Src& src, const PStar& pstar,
+                                          Use&& use) {
+    const E4Words wd = e4_load<PC>(src);
+    e4_slices_w<PC>(cp, wd, pstar, use);
 }
 
 // One pass of the exact key: the sum of T[cell] over the pass's 81 cells;

@@ -48,7 +48,17 @@ constexpr int kT4SI = 1024;                         // i rows (2 x 128 B) in a 1
 constexpr int kT4SJ = 1024;                         // j rows
 constexpr int kT4Stage = kT4SB + kT4SA + kT4SK + kT4SI + kT4SJ;  // 54 KB, a multiple of 1 KB
 constexpr int kT4Ebuf = 4096;                       // per epilogue warp: 32 combinations x 8 (x,y,z) x 16 B
-constexpr size_t kT4Smem = 1024 + (size_t)kT4Stages * kT4Stage + (size_t)kT4EpiWarps * kT4Ebuf;
+
+// Sources of the epilogue that depend on one of k or l only, staged in shared
+// memory once per item by the epilogue warps: the star tables of the prefix
+// triples (i, j, k0 + kk) for cases, controls and totals, and the triple
+// (i, j, l), pair (i, l), (j, l) and single l cores of every l of the item.
+struct T4Item {
+    uint32_t pstar[kT4K][81];
+    uint4 tijl[kT4L][2];
+    uint4 pil[kT4L], pjl[kT4L], sl[kT4L];
+};
+constexpr size_t kT4Smem = 1024 + (size_t)kT4Stages * kT4Stage + (size_t)kT4EpiWarps * kT4Ebuf + sizeof(T4Item);
 constexpr uint32_t kT4Idesc = (1u << 4) | ((uint32_t)(kT4N >> 3) << 17) | ((uint32_t)(kT4M >> 4) << 24);
 constexpr uint32_t kT4Tx = kT4SB + kT4SK + 2 * 2 * kT3KB;  // bytes the TMA brings per stage
 static_assert(kT4Smem <= 227 * 1024 - 256, "order-4 tensor kernel shared memory");
@@ -110,15 +120,37 @@ __device__ __forceinline__ float t4_sum27(const float* f) {
     return (c0 + c1) + (c2 + c3);
 }
 
+// Words of pass PC for combination (k0 + kk, l0 + ll): l-only and prefix
+// sources from the item's shared-memory stage, (k, l) sources from global memory.
+template <int PC>
+__device__ __forceinline__ E4Words t4_words(const T4Item& it, int ll, const uint4* tik, const uint4* tjk,
+                                            const uint4* pkl) {
+    asm volatile("" ::: "memory");
+    E4Words wd;
+    wd.ta[0] = it.tijl[ll][PC == 1 ? 1 : 0];
+    wd.tb[0] = PC == 2 ? it.tijl[ll][1] : make_uint4(0, 0, 0, 0);
+    wd.ta[1] = __ldg(tik + (PC == 1 ? 1 : 0));
+    wd.tb[1] = PC == 2 ? __ldg(tik + 1) : make_uint4(0, 0, 0, 0);
+    wd.ta[2] = __ldg(tjk + (PC == 1 ? 1 : 0));
+    wd.tb[2] = PC == 2 ? __ldg(tjk + 1) : make_uint4(0, 0, 0, 0);
+    wd.pil = it.pil[ll];
+    wd.pjl = it.pjl[ll];
+    wd.pkl = __ldg(pkl);
+    wd.sl = it.sl[ll];
+    return wd;
+}
+
 // Estimate of one pass of the key in units of 2^-16 bits: per slice the
 // single-precision sum of c*lg2(c) over its 27 cells, rounded to 2^-16.
 template <int PC>
-__device__ __forceinline__ long long t4_estimate_pass(const uint32_t (&cp)[2][8], const E4Src& src,
-                                                      const E4Prefix& pre, uint32_t nc) {
+__device__ __forceinline__ long long t4_estimate_pass(const uint32_t (&cp)[2][8], const T4Item& it, int kk, int ll,
+                                                      const uint4* tik, const uint4* tjk, const uint4* pkl,
+                                                      uint32_t nc) {
     const float tiny = 9.5367431640625e-07f;  // 2^-20: c*lg2(c + tiny) = 0 at c = 0
-    const E4PrefixStar<PC> ps(pre, nc);
+    const E4Words wd = t4_words<PC>(it, ll, tik, tjk, pkl);
+    const uint32_t* ps = it.pstar[kk] + 27 * PC;
     long long acc = 0;
-    e4_slices<PC>(cp, src, ps, [&](int, const uint32_t* t) {
+    e4_slices_w<PC>(cp, wd, [&](int q) { return ps[q]; }, [&](int, const uint32_t* t) {
         float f[27];
 #pragma unroll
         for (int q = 0; q < 27; ++q) {
@@ -132,8 +164,28 @@ __device__ __forceinline__ long long t4_estimate_pass(const uint32_t (&cp)[2][8]
 
 // Exact key of one combination (and its tables when o): the rare path, kept
 // out of line so that its registers do not weigh on the estimate.
-__device__ __noinline__ long long t4_exact(const DevData& d, const uint32_t (&cp)[2][8], const E4Src& src,
-                                           const E4Prefix& pre, uint32_t* o) {
+__device__ __noinline__ long long t4_exact(const ScanWork& w, const uint32_t (&cp)[2][8], int i, int j, int k, int l,
+                                           const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
+                                           const uint4* __restrict__ triples, uint32_t* o) {
+    const DevData& d = w.d;
+    const int n = d.snps;
+    const uint4* single4 = reinterpret_cast<const uint4*>(single);
+    E4Src src;
+    src.tij = triples + 2 * triple_index(i, j, l, n);
+    src.tik = triples + 2 * triple_index(i, k, l, n);
+    src.tjk = triples + 2 * triple_index(j, k, l, n);
+    src.pil = pairs + pair_index(i, l, n);
+    src.pjl = pairs + pair_index(j, l, n);
+    src.pkl = pairs + pair_index(k, l, n);
+    src.sl = single4 + l;
+    E4Prefix pre;
+    pre.tijk = triples + 2 * triple_index(i, j, k, n);
+    pre.pij = pairs + pair_index(i, j, n);
+    pre.pik = pairs + pair_index(i, k, n);
+    pre.pjk = pairs + pair_index(j, k, n);
+    pre.si = single4 + i;
+    pre.sj = single4 + j;
+    pre.sk = single4 + k;
     long long key = e4p_pass<0>(cp, src, pre, d.ftab, d.n_cases, o);
     key += e4p_pass<1>(cp, src, pre, d.ftab, d.n_ctrls, o);
     key -= e4p_pass<2>(cp, src, pre, d.ftab, d.n_cases + d.n_ctrls, o);
@@ -142,40 +194,28 @@ __device__ __noinline__ long long t4_exact(const DevData& d, const uint32_t (&cp
 
 __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink, long long thr_q, uint32_t* dump,
                                         const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
-                                        const uint4* __restrict__ triples, const uint32_t (&cp)[2][8], int i, int j,
-                                        int k, int l, bool valid, int lane) {
+                                        const uint4* __restrict__ triples, const T4Item& it,
+                                        const uint32_t (&cp)[2][8], int i, int j, int k0, int l0, int k, int l,
+                                        bool valid, int lane) {
     const DevData& d = w.d;
     const int n = d.snps;
     long long key = w.base_key;
     bool pass = false;
     if (valid) {
-        const uint4* single4 = reinterpret_cast<const uint4*>(single);
-        E4Src src;
-        src.tij = triples + 2 * triple_index(i, j, l, n);
-        src.tik = triples + 2 * triple_index(i, k, l, n);
-        src.tjk = triples + 2 * triple_index(j, k, l, n);
-        src.pil = pairs + pair_index(i, l, n);
-        src.pjl = pairs + pair_index(j, l, n);
-        src.pkl = pairs + pair_index(k, l, n);
-        src.sl = single4 + l;
-        E4Prefix pre;
-        pre.tijk = triples + 2 * triple_index(i, j, k, n);
-        pre.pij = pairs + pair_index(i, j, n);
-        pre.pik = pairs + pair_index(i, k, n);
-        pre.pjk = pairs + pair_index(j, k, n);
-        pre.si = single4 + i;
-        pre.sj = single4 + j;
-        pre.sk = single4 + k;
+        const uint4* tik = triples + 2 * triple_index(i, k, l, n);
+        const uint4* tjk = triples + 2 * triple_index(j, k, l, n);
+        const uint4* pkl = pairs + pair_index(k, l, n);
         bool cand = dump != nullptr;
         if (!cand) {
-            const long long est = t4_estimate_pass<0>(cp, src, pre, d.n_cases) +
-                                  t4_estimate_pass<1>(cp, src, pre, d.n_ctrls) -
-                                  t4_estimate_pass<2>(cp, src, pre, d.n_cases + d.n_ctrls);
+            const int kk = k - k0, ll = l - l0;
+            const long long est = t4_estimate_pass<0>(cp, it, kk, ll, tik, tjk, pkl, d.n_cases) +
+                                  t4_estimate_pass<1>(cp, it, kk, ll, tik, tjk, pkl, d.n_ctrls) -
+                                  t4_estimate_pass<2>(cp, it, kk, ll, tik, tjk, pkl, d.n_cases + d.n_ctrls);
             cand = est >= thr_q;
         }
         if (cand) {
             uint32_t* o = dump ? dump + ((size_t)triple_index(i, j, k, n) * n + l) * 2 * 81 : nullptr;
-            key += t4_exact(d, cp, src, pre, o);
+            key += t4_exact(w, cp, i, j, k, l, single, pairs, triples, o);
             pass = key >= sink.thr;
         }
     }
@@ -369,12 +409,55 @@ __global__ void __launch_bounds__(kT4Threads, 1)
         const uint32_t wmask = (1u << pack) - 1u;
         const int kkw = lane >> 3, xyz = lane & 7;  // this thread's accumulator row (4 q + kkw, xyz)
         const int kkc = lane >> 3, llc = lane & 7;  // this lane's combination in a column group
+        const int et = tid - 32 * (2 + kT4BuildWarps);  // 0..255
+        T4Item& it = *reinterpret_cast<T4Item*>(ebuf_all + kT4EpiWarps * (kT4Ebuf / 4));
+        const uint4* single4 = reinterpret_cast<const uint4*>(single);
         long long item = 0;
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
             int i, j, k0, l0;
             t4_decode(begin, per, n, g, i, j, k0, l0);
             const int buf = (int)(item & 1);
             const int k = k0 + 4 * q + kkc;
+            // stage the item's k-only and l-only sources (named barrier 1: the 256 epilogue threads)
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * kT4EpiWarps) : "memory");
+            if (et < kT4L) {
+                const int l = l0 + et;
+                if (l < n) {
+                    const uint4* t = triples + 2 * triple_index(i, j, l, n);
+                    it.tijl[et][0] = __ldg(t);
+                    it.tijl[et][1] = __ldg(t + 1);
+                    it.pil[et] = __ldg(pairs + pair_index(i, l, n));
+                    it.pjl[et] = __ldg(pairs + pair_index(j, l, n));
+                    it.sl[et] = __ldg(single4 + l);
+                }
+            } else if (et < kT4L + 3 * kT4K) {
+                const int kk = (et - kT4L) / 3, pc = (et - kT4L) % 3, kp = k0 + kk;
+                if (kp < n) {
+                    E4Prefix pre;
+                    pre.tijk = triples + 2 * triple_index(i, j, kp, n);
+                    pre.pij = pairs + pair_index(i, j, n);
+                    pre.pik = pairs + pair_index(i, kp, n);
+                    pre.pjk = pairs + pair_index(j, kp, n);
+                    pre.si = single4 + i;
+                    pre.sj = single4 + j;
+                    pre.sk = single4 + kp;
+                    uint32_t* ps = it.pstar[kk] + 27 * pc;
+                    if (pc == 0) {
+                        const E4PrefixStar<0> st(pre, d.n_cases);
+#pragma unroll 1
+                        for (int qq = 0; qq < 27; ++qq) ps[qq] = st(qq);
+                    } else if (pc == 1) {
+                        const E4PrefixStar<1> st(pre, d.n_ctrls);
+#pragma unroll 1
+                        for (int qq = 0; qq < 27; ++qq) ps[qq] = st(qq);
+                    } else {
+                        const E4PrefixStar<2> st(pre, d.n_cases + d.n_ctrls);
+#pragma unroll 1
+                        for (int qq = 0; qq < 27; ++qq) ps[qq] = st(qq);
+                    }
+                }
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * kT4EpiWarps) : "memory");
             if (!t3_wait(smem_u32(&acc_full[buf]), (uint32_t)((item >> 1) & 1), abort)) {
                 ok = false;
                 break;
@@ -419,8 +502,8 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                 __syncwarp();
                 const int l = l0 + 64 * hh + 8 * cc + llc;
                 const bool valid = k < n && l < n && l > k;
-                t4_eval(w, sink, thr_q, dump, single, pairs, triples, cp, i, j, valid ? k : 2, valid ? l : 3, valid,
-                        lane);
+                t4_eval(w, sink, thr_q, dump, single, pairs, triples, it, cp, i, j, k0, l0, valid ? k : 2,
+                        valid ? l : 3, valid, lane);
             }
         }
     }
