@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
         // ---------------------------------------------------------------- epilogue
         const int e = warp - (2 + kT4BuildWarps);  // 0..7
         const int q = warp & 3;                     // tensor-memory lane quarter this warp may access
-        const int hh = e >> 2;                      // column half: l offsets [64 hh, 64 hh + 64)
+        const int hh = e >> 2;                      // column groups 2 cc + hh: l offsets 16 cc + 8 hh + [0, 8)
         uint32_t* ebuf = ebuf_all + e * (kT4Ebuf / 4);
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
         const uint32_t wmask = (1u << pack) - 1u;
@@ -465,8 +465,22 @@ __global__ void __launch_bounds__(kT4Threads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
             for (int cc = 0; cc < 8; ++cc) {
+                const int l = l0 + 16 * cc + 8 * hh + llc;  // the two warps of a quarter interleave
+                const bool valid = k < n && l < n && l > k;
+                // a column group without a valid combination in this warp is skipped
+                // (its accumulators are never read); the region is still released
+                if (!__any_sync(0xffffffffu, valid)) {
+                    if (cc == 7) {
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
+                                         : "memory");
+                    }
+                    continue;
+                }
                 {
-                    const uint32_t col = (uint32_t)(kT4N * buf + 128 * hh + 16 * cc);
+                    const uint32_t col = (uint32_t)(kT4N * buf + 32 * cc + 16 * hh);
                     uint32_t v[16];
                     asm volatile(
                         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
@@ -500,8 +514,6 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     cp[1][r] = c4.z | (c4.w << 16);
                 }
                 __syncwarp();
-                const int l = l0 + 64 * hh + 8 * cc + llc;
-                const bool valid = k < n && l < n && l > k;
                 t4_eval(w, sink, thr_q, dump, single, pairs, triples, it, cp, i, j, k0, l0, valid ? k : 2,
                         valid ? l : 3, valid, lane);
             }
