@@ -197,9 +197,8 @@ static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
     const bool base = res->one_hot && whole_data_set(res, w) && res->d.n_cases >= 1 && res->d.n_ctrls >= 1 &&
                       res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 && res->d.snps < (1 << 21);
     if (w.order == 2 || w.order == 3) return base;
-    // order 4: both classes in one accumulator, triple cores within their limit
-    return base && w.order == 4 && res->d.snps >= 4 && tensor_pack(res->d.n_cases, res->d.n_ctrls) &&
-           triples_bytes(res->d.snps) <= kMaxTriplesBytes;
+    // order 4: triple cores within their limit
+    return base && w.order == 4 && res->d.snps >= 4 && triples_bytes(res->d.snps) <= kMaxTriplesBytes;
 }
 
 int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp,
@@ -208,8 +207,8 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
                                                    tensor_ok(res, w))) {
         if (!allow_tensor || !tensor_ok(res, w))
             return fail(ctx, FIU_ERR_UNSUPPORTED,
-                        "the tensor-core kernels need one-hot data, order 2, 3 or 4 (order 4: classes that share "
-                        "one accumulator) and the whole data set on one worker");
+                        "the tensor-core kernels need one-hot data, order 2, 3 or 4 and the whole data set on one "
+                        "worker");
         int rc = choose_kernel(ctx, res, (unsigned)w.order, FIU_KERNEL_ELIDED_HS, kernel);  // builds the core tables
         if (rc) return rc;
         fiu_resident* r = const_cast<fiu_resident*>(res);

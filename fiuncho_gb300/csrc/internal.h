@@ -175,7 +175,7 @@ struct T3Plan {
     double item2_combos = 0;
     CUtensorMap map_a2;   // box 128 B x 128 rows (i rows)
     CUtensorMap map_b2;   // box 128 B x 256 rows (j rows)
-    // order 4 (packed classes only): work items (i, j, 16 k, 128 l); item4_begin[j]
+    // order 4: work items (i, j, 16 k, 128 l) (64 l when the classes do not pack); item4_begin[j]
     // = first item of the pairs with second SNP j, item4_per[j] = items per such pair
     long long* item4_begin = nullptr;
     long long* item4_per = nullptr;
@@ -193,13 +193,13 @@ void tensor3_release(T3Plan& plan);
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
                            uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
                            int* status, cudaStream_t s, int sms);
-// tensor4.cu -- order 4 on tcgen05 (one-hot data, packed classes, whole data set, one worker).
-std::vector<long long> t4_item_table(int n, std::vector<long long>& per);
-cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l, const CUtensorMap& map_k,
-                           const CUtensorMap& map_i, const long long* begin, const long long* per, int k_cases,
-                           int pack, long long g0, long long g1, const CandSink& sink, uint32_t* dump,
-                           const uint32_t* single, const uint4* pairs, const uint4* triples, int* status,
-                           cudaStream_t s, int sms);
+// tensor4.cu -- order 4 on tcgen05 (one-hot data, whole data set, one worker).
+std::vector<long long> t4_item_table(int n, bool pack, std::vector<long long>& per);
+cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l256, const CUtensorMap& map_l128,
+                           const CUtensorMap& map_k, const CUtensorMap& map_i, const long long* begin,
+                           const long long* per, int k_cases, int pack, long long g0, long long g1,
+                           const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
+                           const uint4* triples, int* status, cudaStream_t s, int sms);
 // Largest absolute error of the kernel's single-precision log2 over all its inputs (counts <= max_c).
 cudaError_t probe_lg2_error(unsigned max_c, double* max_abs_err, cudaStream_t s);
 

@@ -1234,10 +1234,10 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     if ((e = t3_map(&plan.map_a2, plan.planes, rows, plan.pitch, kT2M, true)) != cudaSuccess) return e;
     if ((e = t3_map(&plan.map_b2, plan.planes, rows, plan.pitch, kT2N, true)) != cudaSuccess) return e;
-    // order 4 (packed classes)
-    if (!plan.pack || d.snps < 4) return cudaSuccess;
+    // order 4
+    if (d.snps < 4) return cudaSuccess;
     std::vector<long long> per4;
-    const std::vector<long long> ib4 = t4_item_table(d.snps, per4);
+    const std::vector<long long> ib4 = t4_item_table(d.snps, plan.pack != 0, per4);
     plan.total4 = ib4.back();
     const double n = d.snps;
     plan.item4_combos = n * (n - 1) * (n - 2) * (n - 3) / 24.0 / std::max(1ll, plan.total4);
@@ -1323,8 +1323,8 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
                            uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
                            int* status, cudaStream_t s, int sms) {
     if (w.order == 4)
-        return launch_tensor4(w, plan.map_l, plan.map_k4, plan.map_i, plan.item4_begin, plan.item4_per, plan.k_cases,
-                              plan.pack, g0, g1, sink, dump, single, pairs, triples, status, s, sms);
+        return launch_tensor4(w, plan.map_l, plan.map_a2, plan.map_k4, plan.map_i, plan.item4_begin, plan.item4_per,
+                              plan.k_cases, plan.pack, g0, g1, sink, dump, single, pairs, triples, status, s, sms);
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);

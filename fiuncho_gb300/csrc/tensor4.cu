@@ -7,8 +7,10 @@
 //     D[(k,x,y,z), (l,w)] = sum_s A[(k,x,y,z), s] B[(l,w), s]   (M 128, N 256)
 // over the e4m3 operand planes of tensor3.cu, both classes in one FP32
 // accumulator (control samples weighted by W = 4^h, exact while
-// n_cases < W and n_cases + W * n_ctrls < 2^24; data sets whose classes do
-// not pack use the CUDA-core pair-major kernel).  B rows are plane rows 2l+w
+// n_cases < W and n_cases + W * n_ctrls < 2^24).  Classes that do not pack
+// take the split form: 64 l per item, the case samples accumulate into one
+// N 128 region and the control samples into another (the MMA instruction
+// costs the same for N 128 as for N 256).  B rows are plane rows 2l+w
 // by TMA; A rows are the bytewise AND of the i, j and k plane rows, built in
 // shared memory by six producer warps from the TMA-staged rows (i AND j once
 // per stage, then AND each k row).  Two accumulator regions alternate between
@@ -36,7 +38,7 @@
 
 namespace fiu {
 
-constexpr int kT4K = 16, kT4L = 128;                // k and l SNPs per work item
+constexpr int kT4K = 16, kT4L = 128;                // k and l SNPs per work item (64 l in the split form)
 constexpr int kT4M = 8 * kT4K, kT4N = 2 * kT4L;     // 128 x 256 GEMM tile
 constexpr int kT4BuildWarps = 6, kT4EpiWarps = 8;
 constexpr int kT4Threads = 32 * (2 + kT4BuildWarps + kT4EpiWarps);  // 512
@@ -59,25 +61,26 @@ struct T4Item {
     uint4 pil[kT4L], pjl[kT4L], sl[kT4L];
 };
 constexpr size_t kT4Smem = 1024 + (size_t)kT4Stages * kT4Stage + (size_t)kT4EpiWarps * kT4Ebuf + sizeof(T4Item);
-constexpr uint32_t kT4Idesc = (1u << 4) | ((uint32_t)(kT4N >> 3) << 17) | ((uint32_t)(kT4M >> 4) << 24);
-constexpr uint32_t kT4Tx = kT4SB + kT4SK + 2 * 2 * kT3KB;  // bytes the TMA brings per stage
+// instruction descriptor: e4m3 x e4m3 -> FP32, M 128, N 256 (packed) or 128 (split)
+constexpr uint32_t t4_idesc(int N) { return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kT4M >> 4) << 24); }
 static_assert(kT4Smem <= 227 * 1024 - 256, "order-4 tensor kernel shared memory");
 static_assert(2 * kT4N <= 512, "order-4 tensor kernel tensor memory");
 
 struct T4Maps {
-    CUtensorMap l, k, i;  // boxes of 256, 32 and 2 plane rows
+    CUtensorMap l, k, i;  // boxes of 2 L (256 or 128), 32 and 2 plane rows
 };
 
 // Items of one pair (i, j): for k-tiles k0 = j + 1 + 16 a (k0 <= n - 2),
-// ceil((n - 1 - k0) / 128) l-tiles l0 = k0 + 1 + 128 b.
-__host__ __device__ inline long long t4_items_per_pair(int n, int j) {
+// ceil((n - 1 - k0) / L) l-tiles l0 = k0 + 1 + L b.
+inline long long t4_items_per_pair(int n, int j, int L) {
     long long c = 0;
-    for (int k0 = j + 1; k0 <= n - 2; k0 += kT4K) c += (n - 1 - k0 + kT4L - 1) / kT4L;
+    for (int k0 = j + 1; k0 <= n - 2; k0 += kT4K) c += (n - 1 - k0 + L - 1) / L;
     return c;
 }
 
 // Item g -> (i, j, k0, l0).  begin[j]: first item of the pairs with second
 // element j (j pairs of per[j] items each).
+template <int L>
 __device__ __forceinline__ void t4_decode(const long long* __restrict__ begin, const long long* __restrict__ per,
                                           int n, long long g, int& i, int& j, int& k0, int& l0) {
     int lo = 0, hi = n - 1;
@@ -92,10 +95,10 @@ __device__ __forceinline__ void t4_decode(const long long* __restrict__ begin, c
     i = (int)(rel / pj);
     long long q = rel - (long long)i * pj;
     for (int k = j + 1;; k += kT4K) {
-        const long long nl = (n - 1 - k + kT4L - 1) / kT4L;
+        const long long nl = (n - 1 - k + L - 1) / L;
         if (q < nl) {
             k0 = k;
-            l0 = k + 1 + kT4L * (int)q;
+            l0 = k + 1 + L * (int)q;
             return;
         }
         q -= nl;
@@ -241,6 +244,16 @@ __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink,
     }
 }
 
+// 16 consecutive accumulator columns of this warp's 32 lanes (one per thread).
+__device__ __forceinline__ void t4_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+}
+
+template <bool PACK>
 __global__ void __launch_bounds__(kT4Threads, 1)
     tensor4p_kernel(const __grid_constant__ T4Maps maps, ScanWork w, const long long* __restrict__ begin,
                     const long long* __restrict__ per, long long g0, long long g1, int k_cases, int pack,
@@ -259,6 +272,11 @@ __global__ void __launch_bounds__(kT4Threads, 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ks_c = k_cases / kT3KB;
     const int ksteps = ks_c + (d.tw + 1) / 2;
+    constexpr int L = PACK ? kT4L : kT4L / 2;                     // l per item
+    constexpr int NR = 2 * L;                                       // N of one accumulator region
+    constexpr uint32_t kIdesc = t4_idesc(NR);
+    constexpr uint32_t kTx = NR * kT3KB + kT4SK + 2 * 2 * kT3KB;  // bytes the TMA brings per stage
+    constexpr int NCC = L / 16;                                     // column groups of 8 l per epilogue warp
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -291,7 +309,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
             long long step = 0;
             for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
                 int i, j, k0, l0;
-                t4_decode(begin, per, n, g, i, j, k0, l0);
+                t4_decode<L>(begin, per, n, g, i, j, k0, l0);
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const int s = (int)(step % kT4Stages);
                     const long long u = step / kT4Stages;
@@ -302,7 +320,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     const int kb = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
                     uint8_t* st = sm + s * kT4Stage;
                     const uint32_t bar = smem_u32(&full_t[s]);
-                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kT4Tx)
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kTx)
                                  : "memory");
                     t3_tma(smem_u32(st), &maps.l, kb, 2 * l0, bar);
                     t3_tma(smem_u32(st + kT4SB + kT4SA), &maps.k, kb, 2 * k0, bar);
@@ -327,8 +345,12 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     ok = false;
                     break;
                 }
-                const uint32_t dcol = tmem + (uint32_t)(kT4N * buf);
                 for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                    // packed: one region of N 256 per buffer; split: cases in the
+                    // buffer's first N 128 columns, controls in its second
+                    const bool ctrl = !PACK && ks >= ks_c;
+                    const uint32_t dcol = tmem + (uint32_t)(kT4N * buf + (ctrl ? NR : 0));
+                    const bool first = ks == 0 || (!PACK && ks == ks_c);
                     const int s = (int)(step % kT4Stages);
                     if (!t3_wait(smem_u32(&full_a[s]), (uint32_t)((step / kT4Stages) & 1), abort)) {
                         ok = false;
@@ -339,11 +361,11 @@ __global__ void __launch_bounds__(kT4Threads, 1)
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk) {
                         const uint64_t ad = t3_desc(sa + 32 * kk), bd = t3_desc(sb + 32 * kk);
-                        const uint32_t acc = (ks == 0 && kk == 0) ? 0u : 1u;
+                        const uint32_t acc = (first && kk == 0) ? 0u : 1u;
                         asm volatile(
                             "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
                             "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
-                            "l"(ad), "l"(bd), "r"(kT4Idesc), "r"(acc));
+                            "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc));
                     }
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                         smem_u32(&empty[s])));
@@ -406,7 +428,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
         const int hh = e >> 2;                      // column groups 2 cc + hh: l offsets 16 cc + 8 hh + [0, 8)
         uint32_t* ebuf = ebuf_all + e * (kT4Ebuf / 4);
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-        const uint32_t wmask = (1u << pack) - 1u;
+        const uint32_t wmask = PACK ? (1u << pack) - 1u : 0xffffffffu;
         const int kkw = lane >> 3, xyz = lane & 7;  // this thread's accumulator row (4 q + kkw, xyz)
         const int kkc = lane >> 3, llc = lane & 7;  // this lane's combination in a column group
         const int et = tid - 32 * (2 + kT4BuildWarps);  // 0..255
@@ -415,12 +437,12 @@ __global__ void __launch_bounds__(kT4Threads, 1)
         long long item = 0;
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
             int i, j, k0, l0;
-            t4_decode(begin, per, n, g, i, j, k0, l0);
+            t4_decode<L>(begin, per, n, g, i, j, k0, l0);
             const int buf = (int)(item & 1);
             const int k = k0 + 4 * q + kkc;
             // stage the item's k-only and l-only sources (named barrier 1: the 256 epilogue threads)
             asm volatile("bar.sync 1, %0;" ::"n"(32 * kT4EpiWarps) : "memory");
-            if (et < kT4L) {
+            if (et < L) {
                 const int l = l0 + et;
                 if (l < n) {
                     const uint4* t = triples + 2 * triple_index(i, j, l, n);
@@ -430,7 +452,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     it.pjl[et] = __ldg(pairs + pair_index(j, l, n));
                     it.sl[et] = __ldg(single4 + l);
                 }
-            } else if (et < kT4L + 3 * kT4K) {
+            } else if (et >= kT4L && et < kT4L + 3 * kT4K) {
                 const int kk = (et - kT4L) / 3, pc = (et - kT4L) % 3, kp = k0 + kk;
                 if (kp < n) {
                     E4Prefix pre;
@@ -464,13 +486,13 @@ __global__ void __launch_bounds__(kT4Threads, 1)
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
-            for (int cc = 0; cc < 8; ++cc) {
+            for (int cc = 0; cc < NCC; ++cc) {
                 const int l = l0 + 16 * cc + 8 * hh + llc;  // the two warps of a quarter interleave
                 const bool valid = k < n && l < n && l > k;
                 // a column group without a valid combination in this warp is skipped
                 // (its accumulators are never read); the region is still released
                 if (!__any_sync(0xffffffffu, valid)) {
-                    if (cc == 7) {
+                    if (cc == NCC - 1) {
                         asm volatile("tcgen05.fence::before_thread_sync;");
                         __syncwarp();
                         if (lane == 0)
@@ -481,16 +503,11 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                 }
                 {
                     const uint32_t col = (uint32_t)(kT4N * buf + 32 * cc + 16 * hh);
-                    uint32_t v[16];
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
-                        "15}, [%16];"
-                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                          "=r"(v[14]), "=r"(v[15])
-                        : "r"(lane_base + col));
+                    uint32_t v[16], vt[16];
+                    t4_ld16(lane_base + col, v);
+                    if (!PACK) t4_ld16(lane_base + col + NR, vt);  // control counts of the same rows / columns
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    if (cc == 7) {  // last read of this item's accumulators: the region is free
+                    if (cc == NCC - 1) {  // last read of this item's accumulators: the region is free
                         asm volatile("tcgen05.fence::before_thread_sync;");
                         __syncwarp();
                         if (lane == 0)
@@ -501,8 +518,14 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     for (int ll = 0; ll < 8; ++ll) {
                         const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * ll]));
                         const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * ll + 1]));
-                        *reinterpret_cast<uint4*>(ebuf + 4 * t4_chunk(kkw, ll, xyz)) =
-                            make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                        uint4 c4;
+                        if (PACK) {
+                            c4 = make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                        } else {
+                            c4 = make_uint4(u0, u1, __float2uint_rn(__uint_as_float(vt[2 * ll])),
+                                            __float2uint_rn(__uint_as_float(vt[2 * ll + 1])));
+                        }
+                        *reinterpret_cast<uint4*>(ebuf + 4 * t4_chunk(kkw, ll, xyz)) = c4;
                     }
                 }
                 __syncwarp();
@@ -545,25 +568,26 @@ double t4_margin(int n_samples) {
     return 2 * err + 1e-3;
 }
 
-std::vector<long long> t4_item_table(int n, std::vector<long long>& per) {
+std::vector<long long> t4_item_table(int n, bool pack, std::vector<long long>& per) {
     std::vector<long long> begin((size_t)n + 1, 0);
     per.assign((size_t)std::max(n, 1), 0);
     for (int j = 0; j < n; ++j) {
-        per[j] = t4_items_per_pair(n, j);
+        per[j] = t4_items_per_pair(n, j, pack ? kT4L : kT4L / 2);
         begin[j + 1] = begin[j] + (long long)j * per[j];
     }
     return begin;
 }
 
-cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l, const CUtensorMap& map_k,
-                           const CUtensorMap& map_i, const long long* begin, const long long* per, int k_cases,
-                           int pack, long long g0, long long g1, const CandSink& sink, uint32_t* dump,
-                           const uint32_t* single, const uint4* pairs, const uint4* triples, int* status,
-                           cudaStream_t s, int sms) {
-    if (!pack || !triples || !pairs || !single) return cudaErrorInvalidValue;
-    static LaunchCache cache;
+cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l256, const CUtensorMap& map_l128,
+                           const CUtensorMap& map_k, const CUtensorMap& map_i, const long long* begin,
+                           const long long* per, int k_cases, int pack, long long g0, long long g1,
+                           const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
+                           const uint4* triples, int* status, cudaStream_t s, int sms) {
+    if (!triples || !pairs || !single || !begin || !per) return cudaErrorInvalidValue;
+    static LaunchCache cache_p, cache_s;
     int per_sm = 1;
-    cudaError_t e = blocks_per_sm(cache, tensor4p_kernel, kT4Threads, kT4Smem, per_sm);
+    cudaError_t e = pack ? blocks_per_sm(cache_p, tensor4p_kernel<true>, kT4Threads, kT4Smem, per_sm)
+                         : blocks_per_sm(cache_s, tensor4p_kernel<false>, kT4Threads, kT4Smem, per_sm);
     if (e != cudaSuccess) return e;
     const long long items = g1 - g0;
     if (items <= 0) return cudaSuccess;
@@ -571,10 +595,16 @@ cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l, const CU
     const double scale = 65536.0 / (std::log(2.0) * 4294967296.0);
     const double thr = ((double)sink.thr - (double)w.base_key) * scale - t4_margin(w.d.n_cases + w.d.n_ctrls) * 65536.0;
     const long long thr_q = (long long)std::floor(std::max(-9.0e18, std::min(9.0e18, thr)));
-    T4Maps maps{map_l, map_k, map_i};
     const unsigned grid = (unsigned)(items < sms ? items : sms);
-    tensor4p_kernel<<<grid, kT4Threads, kT4Smem, s>>>(maps, w, begin, per, g0, g1, k_cases, pack, sink, thr_q, dump,
-                                                      single, pairs, triples, status);
+    if (pack) {
+        T4Maps maps{map_l256, map_k, map_i};
+        tensor4p_kernel<true><<<grid, kT4Threads, kT4Smem, s>>>(maps, w, begin, per, g0, g1, k_cases, pack, sink,
+                                                                thr_q, dump, single, pairs, triples, status);
+    } else {
+        T4Maps maps{map_l128, map_k, map_i};
+        tensor4p_kernel<false><<<grid, kT4Threads, kT4Smem, s>>>(maps, w, begin, per, g0, g1, k_cases, pack, sink,
+                                                                 thr_q, dump, single, pairs, triples, status);
+    }
     count_launch();
     return cudaGetLastError();
 }

@@ -66,15 +66,13 @@ def test_combine_and_popcnt_bit_exact(gs, oracle, golden_testdata):
 
 
 @pytest.mark.parametrize("order,kernel", [(2, 1), (3, 1), (4, 1), (2, 2), (3, 2), (4, 2), (2, 3), (3, 3), (4, 3),
-                                          (2, 4), (3, 4)])
+                                          (2, 4), (3, 4), (4, 4)])
 def test_hot_kernel_tables_bit_exact_reference(gs, golden_testdata, order, kernel):
     """Each counting kernel's own contingency tables for EVERY combination of the
     reference's test data == the reference's combine_and_popcnt tables
     (kernel 1: full table; 2, 3: core cells + exact marginals, POPC / Harley-Seal,
-    at order 4 from triple cores; 4: core cells on the tcgen05 tensor cores -- not at
-    order 4, whose tcgen05 form needs classes that share one accumulator, which the
-    9 000 / 9 800 samples here do not; it is checked against kernel 1 at tile edges and
-    against the reference's own order-4 top-50 on the synthetic fixture)."""
+    at order 4 from triple cores; 4: core cells on the tcgen05 tensor cores -- with
+    9 000 / 9 800 samples one accumulator per class at every order)."""
     from fiuncho_gb300 import Distribution, Resident
     ds = _ds_from_golden(golden_testdata)
     res = Resident(gs.ctx, ds)
@@ -311,11 +309,13 @@ def test_order4_kernels_agree(oracle, n_case, n_ctrl, snps):
 
 
 @pytest.mark.parametrize("snps,n_case,n_ctrl", [(4, 1, 1), (5, 65, 63), (18, 130, 1), (20, 64, 64),
-                                                (33, 4000, 4000), (40, 700, 2500)])
+                                                (33, 4000, 4000), (40, 700, 2500), (21, 4100, 4000),
+                                                (36, 200, 40000), (17, 9000, 9800)])
 def test_tensor4_tile_edges(oracle, snps, n_case, n_ctrl):
-    """Order-4 tcgen05 kernel vs the full-table kernel around the 16-k work item (one
-    accumulator for both classes): identical tables for every combination and identical
-    top-N lists, checked against the oracle."""
+    """Order-4 tcgen05 kernel vs the full-table kernel around the 16 k x 128 l work item
+    (classes in one accumulator) and the 16 k x 64 l one (one accumulator per class):
+    identical tables for every combination and identical top-N lists, checked against
+    the oracle."""
     from fiuncho_gb300 import Distribution, GpuSearch, Resident
     ds = _one_hot_dataset(snps * 3 + n_case, snps, n_case, n_ctrl)
     g = GpuSearch(0)
@@ -336,7 +336,8 @@ def test_tensor4_tile_edges(oracle, snps, n_case, n_ctrl):
     _check_topn(oracle, ds, 4, out, b[0], b[1])
 
 
-@pytest.mark.parametrize("snps,n_case,n_ctrl,out", [(150, 300, 300, 30), (145, 1000, 900, 5)])
+@pytest.mark.parametrize("snps,n_case,n_ctrl,out", [(150, 300, 300, 30), (145, 1000, 900, 5),
+                                                    (140, 5000, 6000, 10)])
 def test_tensor4_search_many_tiles(oracle, snps, n_case, n_ctrl, out):
     """Order-4 tcgen05 search over SNP counts spanning several 128-l tiles, with a
     tight threshold where the bounded estimate rejects nearly every combination:
