@@ -42,9 +42,10 @@ extern "C" {
 /* Counting kernels (fiu_set_kernel, fiu_scan_tables). */
 #define FIU_KERNEL_AUTO 0        /* pick per request (default) */
 #define FIU_KERNEL_FULL 1        /* all 3^order cells, any data, orders 2..8 */
-#define FIU_KERNEL_ELIDED_POPC 2 /* one-hot data, orders 2-3: 2^order cells + exact marginals, POPC */
+#define FIU_KERNEL_ELIDED_POPC 2 /* one-hot data, orders 2-4: 2^order cells + exact marginals, POPC
+                                    (order 4 over the whole data set: pair-major schedule) */
 #define FIU_KERNEL_ELIDED_HS 3   /* as 2, Harley-Seal carry-save counting on the ALU pipe */
-#define FIU_KERNEL_TENSOR 4      /* one-hot data, order 2 or 3, whole data set: core cells on tcgen05 (e4m3, FP32 accumulate) */
+#define FIU_KERNEL_TENSOR 4      /* one-hot data, order 2, 3 or 4, whole data set: core cells on tcgen05 (e4m3, FP32 accumulate) */
 #define FIU_MAX_OUTPUTS 7000  /* largest top-N supported */
 
 typedef struct fiu_ctx fiu_ctx;           /* one per device per host thread */
