@@ -795,17 +795,28 @@ constexpr size_t kT2Smem = 1024 + (size_t)kT2Stages * kT2Stage + (size_t)kT3EpiW
 constexpr uint32_t kT2Idesc = (1u << 4) | ((uint32_t)(kT2N >> 3) << 17) | ((uint32_t)(kT2M >> 4) << 24);
 static_assert(kT2Smem <= 227 * 1024 - 256, "order-2 tensor kernel shared memory");
 
-// Work items of i-tile a (i0 = 64 a): ceil((n-1-i0)/128) j-tiles at j0 = i0+1+128 b.
+// Work items.  i-tiles a (i0 = 64 a) are grouped in bands of kT2Band; j-tiles
+// are global (j0 = 128 b).  Band r covers i-tiles [8 r, 8 r + 8) and j-tiles
+// b >= 4 r (the first j-tile holding a j > i of the band) and lists its items
+// j-tile by j-tile, i-tile fastest: the CTAs working at the same time share
+// a band's eight A tiles and each B tile, so the operands stream from HBM
+// about once per band instead of once per item (items left of the diagonal
+// are masked in the epilogue).  item_begin[r] = first item of band r.
+constexpr int kT2Band = 8;
 __device__ __forceinline__ void t2_decode(const long long* __restrict__ item_begin, int n_itiles, long long g, int& i0,
                                           int& j0) {
-    int lo = 0, hi = n_itiles - 1;
+    const int n_bands = (n_itiles + kT2Band - 1) / kT2Band;
+    int lo = 0, hi = n_bands - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (item_begin[mid] <= g) lo = mid;
         else hi = mid - 1;
     }
-    i0 = kT2I * lo;
-    j0 = i0 + 1 + kT2L * (int)(g - item_begin[lo]);
+    const int ca = min(kT2Band, n_itiles - kT2Band * lo);  // i-tiles in the band
+    const long long idx = g - item_begin[lo];
+    const int b = kT2Band * kT2I / kT2L * lo + (int)(idx / ca);
+    i0 = kT2I * (kT2Band * lo + (int)(idx % ca));
+    j0 = kT2L * b;
 }
 
 // 16-byte chunk of the order-2 transpose buffer holding (cases y0, y1, controls
@@ -1136,17 +1147,21 @@ __global__ void t3_planes_kernel(DevData d, uint8_t* planes, int pitch, int k_ca
     }
 }
 
-// Order-2 items (host): prefix sums over i-tiles of their j-tiles; returns the total.
-static long long t2_items(int n, std::vector<long long>& item_begin) {
-    const int tiles = std::max(1, (n - 1 + kT2I - 1) / kT2I);
-    item_begin.assign((size_t)tiles + 1, 0);
+// Order-2 items (host): prefix sums over the bands of t2_decode; returns the
+// total and the number of i-tiles.
+static long long t2_items(int n, std::vector<long long>& item_begin, int& n_itiles) {
+    n_itiles = std::max(1, (n - 1 + kT2I - 1) / kT2I);
+    const int n_bands = (n_itiles + kT2Band - 1) / kT2Band;
+    const int nb = (n + kT2L - 1) / kT2L;  // global j-tiles
+    item_begin.assign((size_t)n_bands + 1, 0);
     long long total = 0;
-    for (int a = 0; a < tiles; ++a) {
-        item_begin[a] = total;
-        const int i0 = kT2I * a;
-        if (n - 1 - i0 > 0) total += (n - 1 - i0 + kT2L - 1) / kT2L;
+    for (int r = 0; r < n_bands; ++r) {
+        item_begin[r] = total;
+        const int ca = std::min(kT2Band, n_itiles - kT2Band * r);
+        const int b0 = kT2Band * kT2I / kT2L * r;
+        if (nb > b0) total += (long long)ca * (nb - b0);
     }
-    item_begin[tiles] = total;
+    item_begin[n_bands] = total;
     return total;
 }
 
@@ -1225,9 +1240,8 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
     if ((e = t3_map(&plan.map_i, plan.planes, rows, plan.pitch, 2, true)) != cudaSuccess) return e;
     // order 2
     std::vector<long long> ib2;
-    plan.total2 = t2_items(d.snps, ib2);
-    plan.n_itiles = (int)ib2.size() - 1;
-    plan.item2_combos = kT2I * kT2L * 0.9;
+    plan.total2 = t2_items(d.snps, ib2, plan.n_itiles);
+    plan.item2_combos = (double)d.snps * (d.snps - 1) / 2 / std::max(1ll, plan.total2);
     e = cudaMalloc((void**)&plan.item2_begin, ib2.size() * sizeof(long long));
     if (e == cudaSuccess)
         e = cudaMemcpy(plan.item2_begin, ib2.data(), ib2.size() * sizeof(long long), cudaMemcpyHostToDevice);
