@@ -415,9 +415,13 @@ def run_batch_and_serve(args, gs, ctx):
             if delay > 0:
                 time.sleep(delay)
             tickets.append((srv.submit(data[i], specs[i].order, specs[i].outputs), i))
-        lat = []
+        lat, same_served = [], True
         for tk, i in tickets:
-            lat.append(srv.result(tk)[2])
+            r, v64, ms = srv.result(tk)
+            lat.append(ms)
+            # each served result equals the scan searched alone (the plain loop above)
+            same_served &= [x.combination for x in r] == [x.combination for x in a[i][0]] and \
+                np.array_equal(v64, a[i][1])
         makespan = time.perf_counter() - t0
         st = srv.stats()
     finally:
@@ -429,7 +433,8 @@ def run_batch_and_serve(args, gs, ctx):
                      "makespan_s": makespan, "combos_samples_per_s": served_work / makespan,
                      "p50_ms": lat[len(lat) // 2] if lat else None,
                      "p99_ms": lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))] if lat else None,
-                     "rounds": int(st["rounds"]), "unit": UNIT}
+                     "rounds": int(st["rounds"]), "solo": int(st["solo"]),
+                     "identical_to_alone": bool(same_served), "unit": UNIT}
     out["gpu_launches"] = ctx.launches - launches0
     return out
 
@@ -446,7 +451,8 @@ def main():
     ap.add_argument("--kernel", type=int, default=0, help="force a counting kernel (0 = automatic choice)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched / served measurements")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="served stream: Poisson arrivals per second")
-    ap.add_argument("--serve-seconds", type=float, default=10.0, help="served stream: arrival window")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="served stream: arrival window (60 s, the served configuration's loop)")
     args = ap.parse_args()
     import dataclasses
 

@@ -65,8 +65,11 @@ size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 size_t footprint(const ServeScan& s) {
     const size_t snps = s.host.snps, W = s.host.cases_words + s.host.ctrls_words;
-    size_t b = 2 * snps * 3 * W * 8 + (64 * W + 1) * 8 + snps * 16;
-    if (s.order == 3) b += snps * (snps - 1) / 2 * 16;
+    size_t b = 2 * snps * 3 * W * 8 + (64 * W + 1) * 8 + snps * 16;  // data set, transposed copy, c ln c table
+    if (s.order >= 3) b += snps * (snps - 1) / 2 * 16;                     // pair cores
+    if (s.order == 4) b += (size_t)binom((long long)snps, 3) * 32;         // triple cores
+    // e4m3 operand planes of the tensor-core kernels: 2 rows per SNP, each class padded to 128 samples
+    b += 2 * snps * 128 * ((s.host.cases_words + 1) / 2 + (s.host.ctrls_words + 1) / 2);
     const size_t keep = s.outputs + std::max(32u, s.outputs / 8);
     b += std::max<size_t>({32768, 16 * keep, snps + keep}) * sizeof(Cand) + keep * sizeof(ScoredRec) +
          (size_t)s.outputs * (4 * s.order + 12) + 4096;
