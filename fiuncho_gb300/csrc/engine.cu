@@ -4,7 +4,7 @@
 // scan gets a threshold early and later rounds admit few candidates.  A scan
 // whose candidate buffer overflowed is re-run alone on the single-scan path
 // (whose chunking adapts on the host), so results never depend on batching.
-// Scans served by the tensor-core kernels (one-hot order 2 or 3 over the whole
+// Scans served by the tensor-core kernels (one-hot order 2, 3 or 4 over the whole
 // data set) or by the pair-major order-4 kernel (one-hot, whole data set) are
 // not split into rounds: they run alone, one after the other, as they would in
 // a loop of single calls.

@@ -13,7 +13,7 @@
 // scans that arrived meanwhile are admitted before the next round.
 //
 // Scans that run best alone -- those served by the tensor-core kernels
-// (one-hot order 2 or 3) or the pair-major order-4 kernel, full-table scans
+// (one-hot orders 2-4) or the pair-major order-4 kernel, full-table scans
 // above order 4, and any scan admitted while every slot is taken -- go to a
 // second lane: a solo worker thread with its own context and stream runs them
 // one at a time through the single-scan path, concurrently with the rounds,
