@@ -156,9 +156,17 @@ def test_engine_single_rank(gs, golden_testdata):
 @pytest.mark.parametrize("order", [2, 3, 4])
 def test_search_synth_vs_reference(gs, oracle, golden_synth, order):
     from fiuncho_gb300 import Dataset, Distribution
+    from fiuncho_gb300 import GpuSearch
     ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
     res, v64 = gs.run(ds, order, Distribution(ds.snps, order - 1), 50, with_fp64=True)
-    assert gs.last_tile()[0] == 4  # one-hot, whole data set, classes that pack: tcgen05 at every order
+    # one-hot, whole data set: tcgen05 at orders 2-3; at order 4 with 2 000 samples the
+    # pair-major CUDA-core kernel is the faster one, and the forced tcgen05 run agrees
+    assert gs.last_tile()[0] == (4 if order < 4 else 2)
+    if order == 4:
+        g4 = GpuSearch(0, kernel=4)
+        r4, v4 = g4.run(ds, 4, Distribution(ds.snps, 3), 50, with_fp64=True)
+        assert g4.last_tile()[0] == 4
+        assert [x.combination for x in r4] == [x.combination for x in res] and np.array_equal(v4, v64)
     got = _check_topn(oracle, ds, order, 50, res, v64)
     rc = golden_synth["o%d_top50_combos" % order]
     rv = golden_synth["o%d_top50_vals" % order].astype(np.float64)
@@ -357,8 +365,9 @@ def test_tensor4_search_many_tiles(oracle, snps, n_case, n_ctrl, out):
 
 
 def test_order4_reduced_work_is_automatic(gs, golden_synth):
-    """One-hot order-4 searches pick a reduced-work kernel by themselves, also for a
-    Distribution layer (step > 1) of the prefixes; non-one-hot data keeps the full kernel."""
+    """One-hot order-4 searches pick a reduced-work kernel by themselves (pair-major below
+    4 096 samples, tcgen05 above, per-prefix for a Distribution layer with step > 1);
+    non-one-hot data keeps the full kernel."""
     from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident
     ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
     g = GpuSearch(0)
@@ -371,6 +380,10 @@ def test_order4_reduced_work_is_automatic(gs, golden_synth):
     bad = Dataset(100, 70, 9, 2, 2, rng.integers(0, 2 ** 63, 9 * 3 * 4, dtype=np.uint64))
     g.run(bad, 4, Distribution(9, 3), 5)
     assert g.last_tile()[0] == 1
+    # with 4 096 samples or more the tcgen05 kernel takes over
+    big = _one_hot_dataset(9, 24, 2100, 2000)
+    g.run(big, 4, Distribution(24, 3), 10)
+    assert g.last_tile()[0] == 4
 
 
 def test_tensor_kernel_scope(gs, golden_synth):
