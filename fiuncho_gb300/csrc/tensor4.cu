@@ -110,19 +110,6 @@ __device__ __forceinline__ void t4_decode(const long long* __restrict__ begin, c
 // the row-wise writes (fixed ll) and the combination-wise reads (fixed xyz).
 __device__ __forceinline__ int t4_chunk(int kk, int ll, int xyz) { return (kk * 8 + ll) * 8 + (xyz ^ ll); }
 
-// Sum of 27 floats, pairwise (every term takes part in at most 5 roundings).
-__device__ __forceinline__ float t4_sum27(const float* f) {
-    float a[14];
-#pragma unroll
-    for (int q = 0; q < 13; ++q) a[q] = f[2 * q] + f[2 * q + 1];
-    a[13] = f[26];
-    float b[7];
-#pragma unroll
-    for (int q = 0; q < 7; ++q) b[q] = a[2 * q] + a[2 * q + 1];
-    const float c0 = b[0] + b[1], c1 = b[2] + b[3], c2 = b[4] + b[5], c3 = b[6];
-    return (c0 + c1) + (c2 + c3);
-}
-
 // Words of pass PC for combination (k0 + kk, l0 + ll): l-only and prefix
 // sources from the item's shared-memory stage, (k, l) sources from global memory.
 template <int PC>
@@ -149,19 +136,11 @@ template <int PC>
 __device__ __forceinline__ long long t4_estimate_pass(const uint32_t (&cp)[2][8], const T4Item& it, int kk, int ll,
                                                       const uint4* tik, const uint4* tjk, const uint4* pkl,
                                                       uint32_t nc) {
-    const float tiny = 9.5367431640625e-07f;  // 2^-20: c*lg2(c + tiny) = 0 at c = 0
     const E4Words wd = t4_words<PC>(it, ll, tik, tjk, pkl);
     const uint32_t* ps = it.pstar[kk] + 27 * PC;
     long long acc = 0;
-    e4_slices_w<PC>(cp, wd, [&](int q) { return ps[q]; }, [&](int, const uint32_t* t) {
-        float f[27];
-#pragma unroll
-        for (int q = 0; q < 27; ++q) {
-            const float c = u2f(min(t[q], nc));
-            f[q] = c * t3_lg2(c + tiny);
-        }
-        acc += __float2ll_rn(t4_sum27(f) * 65536.0f);
-    });
+    e4_slices_w<PC>(cp, wd, [&](int q) { return ps[q]; },
+                    [&](int, const uint32_t* t) { acc += e4_slice_estimate(t, nc); });
     return acc;
 }
 
