@@ -710,7 +710,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
         // ---------------------------------------------------------------- epilogue
         const int e = warp - (2 + kPBuildWarps);  // 0..7
         const int q = warp & 3;                    // tensor-memory lane quarter this warp may access
-        const int hh = e >> 2;                     // column half: l offsets [64 hh, 64 hh + 64)
+        const int hh = e >> 2;                     // column groups 2 cc + hh (see the loop below)
         uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
         const uint32_t wmask = (1u << pack) - 1u;
@@ -732,8 +732,22 @@ __global__ void __launch_bounds__(kPThreads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
             for (int cc = 0; cc < 8; ++cc) {
+                // column group 2 cc + hh: l offsets 16 cc + 8 hh + [0, 8) (the two warps of a
+                // lane quarter interleave over the item's l range); a group without a valid
+                // combination for this warp is skipped, the region still released
+                const int lg = l0 + 16 * cc + 8 * hh;
+                if (!__any_sync(0xffffffffu, j_ok && lg + 7 > j && lg < n)) {
+                    if (cc == 7) {
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
+                                         : "memory");
+                    }
+                    continue;
+                }
                 {
-                    const uint32_t col = (uint32_t)(kPN * buf + 128 * hh + 16 * cc);
+                    const uint32_t col = (uint32_t)(kPN * buf + 32 * cc + 16 * hh);
                     uint32_t v[16];
                     asm volatile(
                         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
@@ -761,8 +775,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
                 __syncwarp();
 #pragma unroll 1
                 for (int b = 0; b < 2; ++b)
-                    t3_eval(w, sink, thr_f, dump, single, pairs, ebuf, jl, 2 * kp + b, i, j,
-                            l0 + 64 * hh + 8 * cc + 2 * kp + b, j_ok, pij, si, sj, lane);
+                    t3_eval(w, sink, thr_f, dump, single, pairs, ebuf, jl, 2 * kp + b, i, j, lg + 2 * kp + b, j_ok,
+                            pij, si, sj, lane);
                 __syncwarp();
             }
         }
