@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(kT3Threads, 1)
         // ---------------------------------------------------------------- epilogue
         const int e = warp - (2 + kT3BuildWarps);  // 0..7
         const int q = warp & 3;                    // tensor-memory lane quarter this warp may access
-        const int hh = e >> 2;                     // column half: l offsets [48 hh, 48 hh + 48)
+        const int hh = e >> 2;                     // column groups 2 cc + hh: l offsets 16 cc + 8 hh + [0, 8)
         uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
         uint4* stash = stash_all + e * (kT3Stash / 16);  // [word quad][lane]: conflict-free
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(kT3Threads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
             for (int cc = 0; cc < 6; ++cc) {
-                const uint32_t col = (uint32_t)(96 * hh + 16 * cc);
+                const uint32_t col = (uint32_t)(32 * cc + 16 * hh);
                 uint32_t v[16], p[8];
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
@@ -483,8 +483,21 @@ __global__ void __launch_bounds__(kT3Threads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
             for (int cc = 0; cc < 6; ++cc) {
+                // a group without a valid combination for this warp is skipped (the two warps
+                // of a lane quarter interleave over the l range); the columns are still released
+                const int lg = l0 + 16 * cc + 8 * hh;
+                if (!__any_sync(0xffffffffu, j_ok && lg + 7 > j && lg < n)) {
+                    if (cc == 5) {
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ctrl_empty))
+                                         : "memory");
+                    }
+                    continue;
+                }
                 {
-                    const uint32_t col = (uint32_t)(96 * hh + 16 * cc);
+                    const uint32_t col = (uint32_t)(32 * cc + 16 * hh);
                     uint32_t vt[16];
                     asm volatile(
                         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
@@ -516,8 +529,8 @@ __global__ void __launch_bounds__(kT3Threads, 1)
                 __syncwarp();
 #pragma unroll 1
                 for (int b = 0; b < 2; ++b)
-                    t3_eval(w, sink, thr_f, dump, single, pairs, ebuf, jl, 2 * kp + b, i, j,
-                            l0 + 48 * hh + 8 * cc + 2 * kp + b, j_ok, pij, si, sj, lane);
+                    t3_eval(w, sink, thr_f, dump, single, pairs, ebuf, jl, 2 * kp + b, i, j, lg + 2 * kp + b, j_ok,
+                            pij, si, sj, lane);
                 __syncwarp();
             }
         }
@@ -1046,7 +1059,7 @@ __global__ void __launch_bounds__(kT2Threads, 1)
         // ---------------------------------------------------------------- epilogue
         const int e = warp - 2;     // 0..7
         const int q = warp & 3;     // tensor-memory lane quarter this warp may access
-        const int hh = e >> 2;      // column half: j offsets [64 hh, 64 hh + 64)
+        const int hh = e >> 2;      // column groups 2 cc + hh: j offsets 16 cc + 8 hh + [0, 8)
         uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
         const uint32_t wmask = pack ? (1u << pack) - 1u : 0xffffffffu;
@@ -1074,8 +1087,21 @@ __global__ void __launch_bounds__(kT2Threads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
             for (int cc = 0; cc < 8; ++cc) {
+                // the two warps of a lane quarter interleave over the j range; a group without
+                // a valid pair for this warp (left of the diagonal, past the last SNP) is skipped
+                const int jg = j0 + 16 * cc + 8 * hh;
+                if (!__any_sync(0xffffffffu, i_ok && jg + 7 > i && jg < n)) {
+                    if (cc == 7) {
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0)
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
+                                         : "memory");
+                    }
+                    continue;
+                }
                 {
-                    const uint32_t col = (uint32_t)((pack ? kT2N * buf : 0) + 128 * hh + 16 * cc);
+                    const uint32_t col = (uint32_t)((pack ? kT2N * buf : 0) + 32 * cc + 16 * hh);
                     uint32_t v[16], vt[16];
                     asm volatile(
                         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
@@ -1118,7 +1144,7 @@ __global__ void __launch_bounds__(kT2Threads, 1)
 #pragma unroll 1
                 for (int kk = 0; kk < 4; ++kk) {
                     const int k = 4 * kh + kk;
-                    t2_eval(w, sink, thr_f, dump, single, ebuf, ii, k, i, j0 + 64 * hh + 8 * cc + k, i_ok, si, lane);
+                    t2_eval(w, sink, thr_f, dump, single, ebuf, ii, k, i, jg + k, i_ok, si, lane);
                 }
                 __syncwarp();
             }
