@@ -155,11 +155,13 @@ __device__ __forceinline__ void expand3f(const float* core, const uint4& pij, co
 // (x, y)) sit in column group k of this warp's transpose buffer: exact 27-cell tables, the
 // bounded single-precision prefilter, the exact fixed-point key for survivors, and the
 // warp-aggregated append of candidates (warp-synchronous: every lane calls it).
+// When stage is given it holds the item's pair cores (i, l0 + ll) at [ll] and
+// single cores of l0 + ll at [128 + ll] (shared memory).
 __device__ __forceinline__ void t3_eval(const ScanWork& w, const CandSink& sink, float thr_f, uint32_t* dump,
                                         const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
                                         const uint32_t* ebuf, int jl, int k, int i, int j, int l, bool j_ok,
                                         const uint4& pij, const float (&si)[2][2], const float (&sj)[2][2],
-                                        int lane) {
+                                        int lane, const uint4* stage = nullptr, int l0 = 0) {
     const DevData& d = w.d;
     const int n = d.snps;
     const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
@@ -177,9 +179,14 @@ __device__ __forceinline__ void t3_eval(const ScanWork& w, const CandSink& sink,
     }
     uint4 pil = make_uint4(0, 0, 0, 0), pjl = pil, sl4 = pil;
     if (valid) {
-        pil = __ldg(pairs + pair_index(i, l, n));
         pjl = __ldg(pairs + pair_index(j, l, n));
-        sl4 = __ldg(reinterpret_cast<const uint4*>(single) + l);
+        if (stage) {
+            pil = stage[l - l0];
+            sl4 = stage[128 + l - l0];
+        } else {
+            pil = __ldg(pairs + pair_index(i, l, n));
+            sl4 = __ldg(reinterpret_cast<const uint4*>(single) + l);
+        }
     }
     const float sl[2][2] = {{u2f(sl4.x), u2f(sl4.y)}, {u2f(sl4.z), u2f(sl4.w)}};
     float t[2][27];
@@ -560,7 +567,7 @@ constexpr int kPStages = 3;
 constexpr int kPSB = kPN * kT3KB;                         // 32 KB  l rows
 constexpr int kPSA = kT3M * kT3KB;                        // 16 KB  (i,j) rows, 128-byte swizzle
 constexpr int kPStage = kPSB + kPSA + kT3SJ + kT3SI;      // 57 KB, a multiple of 1 KB
-constexpr size_t kPSmem = 1024 + (size_t)kPStages * kPStage + (size_t)kT3EpiWarps * kT3Ebuf;
+constexpr size_t kPSmem = 1024 + (size_t)kPStages * kPStage + (size_t)kT3EpiWarps * kT3Ebuf + 2 * kPL * 16;
 constexpr uint32_t kPIdesc = (1u << 4) | ((uint32_t)(kPN >> 3) << 17) | ((uint32_t)(kT3M >> 4) << 24);
 static_assert(kPSmem <= 227 * 1024 - 256, "packed tensor kernel shared memory");
 static_assert(2 * kPN <= 512, "packed tensor kernel tensor memory");
@@ -728,11 +735,23 @@ __global__ void __launch_bounds__(kPThreads, 1)
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
         const uint32_t wmask = (1u << pack) - 1u;
         const int jl = lane >> 2, xy = lane & 3, kp = lane & 3;
+        const int et = tid - 32 * (2 + kPBuildWarps);  // 0 .. 255
+        // the item's pair cores (i, l) and single cores of l, staged once per item
+        uint4* stage = reinterpret_cast<uint4*>(ebuf_all + kT3EpiWarps * (kT3Ebuf / 4));
         long long item = 0;
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
             int i, j0, l0;
             t3_decode<kPL>(item_begin, n, g, i, j0, l0);
             const int buf = (int)(item & 1);
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * kT3EpiWarps) : "memory");  // last item's readers done
+            {
+                const int ll = et & (kPL - 1), l = l0 + ll;
+                if (l < n) {
+                    if (et < kPL) stage[ll] = __ldg(pairs + pair_index(i, l, n));
+                    else stage[kPL + ll] = __ldg(reinterpret_cast<const uint4*>(single) + l);
+                }
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * kT3EpiWarps) : "memory");
             const int j = j0 + 8 * q + jl;
             const bool j_ok = j < n;
             uint4 pij;
@@ -789,7 +808,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
 #pragma unroll 1
                 for (int b = 0; b < 2; ++b)
                     t3_eval(w, sink, thr_f, dump, single, pairs, ebuf, jl, 2 * kp + b, i, j, lg + 2 * kp + b, j_ok,
-                            pij, si, sj, lane);
+                            pij, si, sj, lane, stage, l0);
                 __syncwarp();
             }
         }
