@@ -58,6 +58,19 @@ __device__ __forceinline__ uint32_t tcell(const uint4& v, int x, int y, int z) {
 
 // Value of pass PC (0 cases, 1 controls, 2 both classes summed) from a
 // per-class pair of values.
+// Sum of 27 floats, pairwise (every term takes part in at most 5 roundings).
+__device__ __forceinline__ float e4_sum27(const float* f) {
+    float a[14];
+#pragma unroll
+    for (int q = 0; q < 13; ++q) a[q] = f[2 * q] + f[2 * q + 1];
+    a[13] = f[26];
+    float b[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) b[q] = a[2 * q] + a[2 * q + 1];
+    const float c0 = b[0] + b[1], c1 = b[2] + b[3], c2 = b[4] + b[5], c3 = b[6];
+    return (c0 + c1) + (c2 + c3);
+}
+
 template <int PC>
 __device__ __forceinline__ uint32_t by_pass(uint32_t a, uint32_t b) {
     return PC == 0 ? a : PC == 1 ? b : a + b;
@@ -139,6 +152,63 @@ __device__ __forceinline__ void e4_slices_w(const uint32_t (&cp)[2][8], const E4
     }
 }
 
+// Both classes' slices at once: use(sw, t0, t1) receives slice sw of the case
+// table (t0) and of the control table (t1); w0 / w1 are the words of passes
+// 0 / 1 (cases / controls), ps0 / ps1 the prefix star tables of the two
+// classes.  The totals follow cell by cell as t0 + t1.
+template <class PS0, class PS1, class Use>
+__device__ __forceinline__ void e4_slices2(const uint32_t (&cp)[2][8], const E4Words& w0, const E4Words& w1,
+                                           const PS0& ps0, const PS1& ps1, Use&& use) {
+    auto star = [&](const E4Words& wd, int cls, int w, int q) -> uint32_t {
+        const int a = q / 9, b = (q / 3) % 3, z = q % 3;
+        if (a < 2 && b < 2 && z < 2) {
+            const uint32_t c = cp[cls][(a * 2 + b) * 2 + z];
+            return w ? c >> 16 : c & 0xffffu;
+        }
+        if (a < 2 && b < 2) return tcell(wd.ta[0], a, b, w);
+        if (a < 2 && z < 2) return tcell(wd.ta[1], a, z, w);
+        if (b < 2 && z < 2) return tcell(wd.ta[2], b, z, w);
+        if (a < 2) return pcore(wd.pil, cls, a, w);
+        if (b < 2) return pcore(wd.pjl, cls, b, w);
+        if (z < 2) return pcore(wd.pkl, cls, z, w);
+        return cls ? (w ? wd.sl.w : wd.sl.z) : (w ? wd.sl.y : wd.sl.x);
+    };
+#pragma unroll
+    for (int sw = 0; sw < 3; ++sw) {
+        uint32_t t0[27], t1[27];
+#pragma unroll
+        for (int q = 0; q < 27; ++q) {
+            t0[q] = sw < 2 ? star(w0, 0, sw, q) : ps0(q) - star(w0, 0, 0, q) - star(w0, 0, 1, q);
+            t1[q] = sw < 2 ? star(w1, 1, sw, q) : ps1(q) - star(w1, 1, 0, q) - star(w1, 1, 1, q);
+        }
+        star_to_table(t0);
+        star_to_table(t1);
+        use(sw, t0, t1);
+    }
+}
+
+// One slice's contribution to the key estimate, cell by cell, in units of
+// 2^-16 bits: the pairwise single-precision sum over its 27 cells of
+// g = a lg2 a + b lg2 b - (a+b) lg2 (a+b) (a cases, b controls; each g lies in
+// [-(a+b), 0]), rounded to 2^-16.
+__device__ __forceinline__ long long e4_slice_estimate2(const uint32_t* t0, const uint32_t* t1, uint32_t n0,
+                                                        uint32_t n1) {
+    const float tiny = 9.5367431640625e-07f;  // 2^-20: c*lg2(c + tiny) = 0 at c = 0
+    float g[27];
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+        const float a = __uint_as_float(0x4B000000u | min(t0[q], n0)) - 8388608.0f;
+        const float b = __uint_as_float(0x4B000000u | min(t1[q], n1)) - 8388608.0f;
+        const float sab = a + b;
+        float la, lb, ls;
+        asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(la) : "f"(a + tiny));
+        asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(lb) : "f"(b + tiny));
+        asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(ls) : "f"(sab + tiny));
+        g[q] = fmaf(a, la, fmaf(b, lb, -sab * ls));
+    }
+    return __float2ll_rn(e4_sum27(g) * 65536.0f);
+}
+
 // The same with the words loaded from their locations (the loads of a pass are
 // not hoisted above the previous pass: fewer registers held across passes).
 template <int PC, class PStar, class Use>
@@ -215,19 +285,6 @@ __device__ __forceinline__ long long e4p_pass(const uint32_t (&cp)[2][8], const 
                                               const long long* __restrict__ ftab, uint32_t nc, uint32_t* o) {
     const E4PrefixStar<PC> ps(pre, nc);
     return e4_pass<PC>(cp, src, ps, ftab, nc, o);
-}
-
-// Sum of 27 floats, pairwise (every term takes part in at most 5 roundings).
-__device__ __forceinline__ float e4_sum27(const float* f) {
-    float a[14];
-#pragma unroll
-    for (int q = 0; q < 13; ++q) a[q] = f[2 * q] + f[2 * q + 1];
-    a[13] = f[26];
-    float b[7];
-#pragma unroll
-    for (int q = 0; q < 7; ++q) b[q] = a[2 * q] + a[2 * q + 1];
-    const float c0 = b[0] + b[1], c1 = b[2] + b[3], c2 = b[4] + b[5], c3 = b[6];
-    return (c0 + c1) + (c2 + c3);
 }
 
 // One slice's contribution to the key estimate, in units of 2^-16 bits: the

@@ -130,17 +130,16 @@ __device__ __forceinline__ E4Words t4_words(const T4Item& it, int ll, const uint
     return wd;
 }
 
-// Estimate of one pass of the key in units of 2^-16 bits: per slice the
-// single-precision sum of c*lg2(c) over its 27 cells, rounded to 2^-16.
-template <int PC>
-__device__ __forceinline__ long long t4_estimate_pass(const uint32_t (&cp)[2][8], const T4Item& it, int kk, int ll,
-                                                      const uint4* tik, const uint4* tjk, const uint4* pkl,
-                                                      uint32_t nc) {
-    const E4Words wd = t4_words<PC>(it, ll, tik, tjk, pkl);
-    const uint32_t* ps = it.pstar[kk] + 27 * PC;
+// Estimate of the key minus the base in units of 2^-16 bits, cell by cell
+// over both classes (the totals as their sum): within t4_margin.
+__device__ __forceinline__ long long t4_estimate(const uint32_t (&cp)[2][8], const T4Item& it, int kk, int ll,
+                                                 const uint4* tik, const uint4* tjk, const uint4* pkl, uint32_t n0,
+                                                 uint32_t n1) {
+    const E4Words w0 = t4_words<0>(it, ll, tik, tjk, pkl), w1 = t4_words<1>(it, ll, tik, tjk, pkl);
+    const uint32_t *p0 = it.pstar[kk], *p1 = it.pstar[kk] + 27;
     long long acc = 0;
-    e4_slices_w<PC>(cp, wd, [&](int q) { return ps[q]; },
-                    [&](int, const uint32_t* t) { acc += e4_slice_estimate(t, nc); });
+    e4_slices2(cp, w0, w1, [&](int q) { return p0[q]; }, [&](int q) { return p1[q]; },
+               [&](int, const uint32_t* t0, const uint32_t* t1) { acc += e4_slice_estimate2(t0, t1, n0, n1); });
     return acc;
 }
 
@@ -190,9 +189,7 @@ __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink,
         bool cand = dump != nullptr;
         if (!cand) {
             const int kk = k - k0, ll = l - l0;
-            const long long est = t4_estimate_pass<0>(cp, it, kk, ll, tik, tjk, pkl, d.n_cases) +
-                                  t4_estimate_pass<1>(cp, it, kk, ll, tik, tjk, pkl, d.n_ctrls) -
-                                  t4_estimate_pass<2>(cp, it, kk, ll, tik, tjk, pkl, d.n_cases + d.n_ctrls);
+            const long long est = t4_estimate(cp, it, kk, ll, tik, tjk, pkl, d.n_cases, d.n_ctrls);
             cand = est >= thr_q;
         }
         if (cand) {
@@ -528,22 +525,23 @@ __global__ void __launch_bounds__(kT4Threads, 1)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
-// Bound (in bits) on |estimate - exact key / (ln2 * 2^32)| over the 243 terms
-// of one combination (81 cells x cases, controls, totals), N samples:
-// the products c*lg2 and the pairwise sums of a 27-term slice round every
-// term at most 6 times (2^-24 each) and sum |c*lg2(c)| over all terms is at
-// most B = 2 N lg2 N; lg2.approx is within 2^-18 of log2 on every input the
-// kernel can see (checked exhaustively by fiu_probe_lg2_error) and sum c over
-// all terms is 2 N; the c + 2^-20 shift moves each term by at most
-// 2^-20 / ln 2, its rounding each count's logarithm by at most 2^-24 / ln 2;
-// each of the 9 slice sums rounds by 2^-17 in fixed point; the integer table
-// rounds each term by 1/2 of 2^-32 nats.  Doubled.
+// Bound (in bits) on |estimate - exact key / (ln2 * 2^32)|, N samples: each
+// sample lies in exactly one of the 81 cells, so sum (a+b) over the cells is
+// N and sum (a+b) lg2 (a+b) <= N lg2 N.  Per cell the three products and two
+// additions of g round at most 5 times by 2^-24 of at most (a+b) lg2 (a+b);
+// lg2.approx is within 2^-18 of log2 on every input the kernel can see
+// (checked exhaustively by fiu_probe_lg2_error), which moves g by at most
+// 2 (a+b) 2^-18; the c + 2^-20 shift moves each of the 243 products by at
+// most 2^-20 / ln 2 and its rounding each logarithm by at most 2^-24 / ln 2;
+// a 27-term pairwise sum rounds 5 times by 2^-24 of at most sum |g| <= N;
+// each of the 3 slice sums rounds by 2^-17 in fixed point; the integer table
+// rounds each of the 243 exact terms by 1/2 of 2^-32 nats.  Doubled.
 double t4_margin(int n_samples) {
-    const double N = n_samples, lgN = std::log2(std::max(2.0, N)), B = 2 * N * lgN;
+    const double N = n_samples, lgN = std::log2(std::max(2.0, N));
     const double u = std::ldexp(1.0, -24), e20 = std::ldexp(1.0, -20), e_lg2 = std::ldexp(1.0, -18);
     const double T = 243;
-    const double err = 6 * u * B + 2 * N * e_lg2 + T * e20 / std::log(2.0) + 2 * N * u / std::log(2.0) +
-                       9 * std::ldexp(1.0, -17) + T * 0.5 / (std::log(2.0) * 4294967296.0);
+    const double err = 5 * u * N * lgN + 2 * N * e_lg2 + T * e20 / std::log(2.0) + 2 * N * u / std::log(2.0) +
+                       5 * u * N + 3 * std::ldexp(1.0, -17) + T * 0.5 / (std::log(2.0) * 4294967296.0);
     return 2 * err + 1e-3;
 }
 
