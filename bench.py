@@ -433,7 +433,7 @@ def run_batch_and_serve(args, gs, ctx):
                      "makespan_s": makespan, "combos_samples_per_s": served_work / makespan,
                      "p50_ms": lat[len(lat) // 2] if lat else None,
                      "p99_ms": lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))] if lat else None,
-                     "rounds": int(st["rounds"]), "solo": int(st["solo"]),
+                     "rounds": int(st["rounds"]), "solo": int(st["solo"]), "overlapped": int(st["overlapped"]),
                      "identical_to_alone": bool(same_served), "unit": UNIT}
     out["gpu_launches"] = ctx.launches - launches0
     return out

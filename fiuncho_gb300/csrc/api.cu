@@ -203,10 +203,11 @@ static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
 
 // Below this many samples an order-4 scan is faster on the CUDA-core
 // pair-major kernel: the tensor kernel's per-combination epilogue then
-// outweighs the counting it saves (measured at 150 SNPs: 1 060 samples
-// 7.1 vs 13.5 ms, 3 800 samples 14.8 vs 14.1 ms, 14 900 samples 44.7 vs
-// 20.5 ms).  Forcing FIU_KERNEL_TENSOR still uses it.
-constexpr int kT4MinSamples = 4096;
+// outweighs the counting it saves (measured at 150 SNPs, pair-major vs
+// tensor: 1 060 samples 7.1 vs 9.6 ms, 1 800 samples 8.9 vs 9.6 ms, 4 000
+// samples 14.7 vs 9.9 ms, 14 900 samples 44.8 vs 17.2 ms).  Forcing
+// FIU_KERNEL_TENSOR still uses it.
+constexpr int kT4MinSamples = 2048;
 
 int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp,
                 bool allow_tensor) {
@@ -446,6 +447,10 @@ int fiu_create(int device, fiu_ctx** out) {
 
 void fiu_destroy(fiu_ctx* ctx) {
     if (!ctx) return;
+    for (fiu_ctx*& l : ctx->lanes) {
+        fiu_destroy(l);
+        l = nullptr;
+    }
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->cand);

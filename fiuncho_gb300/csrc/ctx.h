@@ -40,6 +40,8 @@ struct fiu_ctx {
     size_t arena_cap = 0;
     char* host_arena = nullptr;
     size_t host_arena_cap = 0;
+    // helper lanes of the batched search (own stream and scratch each), made on first use
+    fiu_ctx* lanes[2] = {nullptr, nullptr};
 };
 
 struct fiu_resident {

@@ -6,12 +6,21 @@
 // (whose chunking adapts on the host), so results never depend on batching.
 // Scans served by the tensor-core kernels (one-hot order 2, 3 or 4 over the whole
 // data set) or by the pair-major order-4 kernel (one-hot, whole data set) are
-// not split into rounds: they run alone, one after the other, as they would in
-// a loop of single calls.
+// not split into rounds: each runs on the single-scan path, as in a loop of
+// single calls, but on one of two helper lanes (a context with its own stream
+// and scratch) concurrently with the rounds and with the other lane, and the
+// calling thread joins them once its rounds are done.  Their kernels then
+// share the device: the persistent kernels of one scan take the SMs another
+// leaves idle (launch tails, the host steps between a scan's chunks).  The
+// scans of one data set stay on one lane.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fiuncho_gpu.h"
@@ -89,6 +98,64 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
         plans.push_back(p);
     }
     const int n = (int)plans.size();
+    // ---- scans that run alone: grouped by data set, taken by the helper lanes
+    // (and by this thread after its rounds)
+    std::vector<std::vector<unsigned>> alone;
+    {
+        std::map<const fiu_resident*, size_t> by_res;
+        for (unsigned i : single_path) {
+            auto it = by_res.find(scans[i].res);
+            if (it == by_res.end()) {
+                it = by_res.emplace(scans[i].res, alone.size()).first;
+                alone.emplace_back();
+            }
+            alone[it->second].push_back(i);
+        }
+    }
+    single_path.clear();  // from here on: round scans whose candidate buffer overflowed
+    std::atomic<size_t> next_group{0};
+    std::mutex err_mu;
+    std::string lane_err;  // a lane's last error message, reported on this context after the join
+    auto run_alone = [&](fiu_ctx* lc) {
+        for (size_t g; (g = next_group.fetch_add(1)) < alone.size();)
+            for (unsigned i : alone[g]) {
+                fiu_scan& sc = scans[i];
+                sc.status = search_impl(lc, sc.res, sc.order, &sc.distribution, sc.outputs, sc.out_combinations,
+                                        sc.out_vals, sc.out_vals64, &sc.out_count, 0);
+                if (sc.status && lc != ctx) {
+                    std::lock_guard<std::mutex> g2(err_mu);
+                    lane_err = lc->err;
+                }
+            }
+    };
+    std::vector<std::thread> lane_threads;
+    std::vector<fiu_ctx*> used_lanes;
+    std::vector<unsigned long long> lane_launches0;
+    struct Joiner {  // every return below waits for the lanes first
+        std::vector<std::thread>& t;
+        ~Joiner() {
+            for (std::thread& x : t)
+                if (x.joinable()) x.join();
+        }
+    } joiner{lane_threads};
+    const size_t helpers = std::min<size_t>(2, n > 0 ? alone.size() : (alone.empty() ? 0 : alone.size() - 1));
+    for (size_t l = 0; l < helpers; ++l) {
+        fiu_ctx*& lc = ctx->lanes[l];
+        if (!lc && fiu_create(ctx->device, &lc) != FIU_OK) {
+            lc = nullptr;
+            break;  // fewer lanes: this thread takes what is left
+        }
+        lc->kernel = ctx->kernel;  // the same kernel choice and tuned tiles as this context
+        lc->autotune = ctx->autotune;
+        lc->tuned = ctx->tuned;
+        used_lanes.push_back(lc);
+        lane_launches0.push_back(lc->launches);
+        lane_threads.emplace_back([lc, &run_alone] {
+            cudaSetDevice(lc->device);
+            Scope lane_scope(lc);
+            run_alone(lc);
+        });
+    }
     if (n > 0) {
         // ---- round schedule: per round, the entries of each kernel family
         // (round_family) and l-tile width, each group with its own item space
@@ -242,5 +309,9 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
         sc.status = search_impl(ctx, sc.res, sc.order, &sc.distribution, sc.outputs, sc.out_combinations,
                                 sc.out_vals, sc.out_vals64, &sc.out_count, 0);
     }
+    run_alone(ctx);
+    for (std::thread& t : lane_threads) t.join();
+    for (size_t l = 0; l < used_lanes.size(); ++l) ctx->launches += used_lanes[l]->launches - lane_launches0[l];
+    if (!lane_err.empty()) ctx->err = lane_err;
     return FIU_OK;
 }

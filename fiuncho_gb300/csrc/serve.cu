@@ -14,10 +14,16 @@
 //
 // Scans that run best alone -- those served by the tensor-core kernels
 // (one-hot orders 2-4) or the pair-major order-4 kernel, full-table scans
-// above order 4, and any scan admitted while every slot is taken -- go to a
-// second lane: a solo worker thread with its own context and stream runs them
-// one at a time through the single-scan path, concurrently with the rounds,
-// so both lanes share the device.
+// above order 4, and any scan admitted while every slot is taken -- go to the
+// solo lanes: kSoloLanes worker threads, each with its own context and
+// stream, take them from one FIFO and run each through the single-scan path.
+// The lanes run concurrently with one another and with the rounds, so the
+// kernels of several scans share the device: a persistent kernel of one scan
+// takes the SMs that another leaves idle (launch tails, the host gaps between
+// a scan's chunks, its selection and re-scoring), and a small scan that
+// arrives behind a large one starts at once instead of waiting for it.
+// fiu_serve_stats.overlapped counts the scans whose device work overlapped
+// another scan's.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -36,6 +42,7 @@ using Clock = std::chrono::steady_clock;
 namespace {
 
 constexpr int kSlots = 256;                // concurrently admitted scans
+constexpr int kSoloLanes = 2;              // solo worker threads (one context and stream each)
 constexpr double kRoundBudget = 1.5e11;    // combinations x samples per scan per round
 
 struct ServeScan {
@@ -55,6 +62,7 @@ struct ServeScan {
     size_t off_scored = 0, off_comb = 0, off_val = 0, off_val64 = 0;
     int status = FIU_OK;
     bool finished = false;
+    bool overlap = false;  // its device work overlapped another scan's (under the server mutex)
     std::vector<int32_t> comb;
     std::vector<float> vals;
     std::vector<double> vals64;
@@ -89,11 +97,12 @@ struct fiu_server {
     uint64_t next_ticket = 1;
     bool stop = false;
     std::thread worker;
-    // solo lane
-    fiu_ctx* solo_ctx = nullptr;
+    // solo lanes
+    fiu_ctx* solo_ctx[kSoloLanes] = {};
     std::deque<ServeScan*> solo_queue;
     std::condition_variable cv_solo;
-    std::thread solo_worker;
+    std::thread solo_worker[kSoloLanes];
+    std::vector<ServeScan*> running;  // scans with device work in flight, any lane (under mu)
     ScanDesc* d_desc = nullptr;
     ScanState* d_state = nullptr;
     unsigned* d_zero = nullptr;
@@ -101,7 +110,7 @@ struct fiu_server {
     size_t ents_cap = 0;
     std::vector<int> free_slots;
     // statistics (under mu)
-    uint64_t submitted = 0, completed = 0, failed = 0, rounds = 0, bytes_in_use = 0, solo = 0;
+    uint64_t submitted = 0, completed = 0, failed = 0, rounds = 0, bytes_in_use = 0, solo = 0, overlapped = 0;
     std::vector<double> lat_ms;
     double combos_samples = 0;
     int init_status = FIU_OK;
@@ -125,6 +134,16 @@ void release(fiu_server* sv, ServeScan* s, fiu_ctx* ctx) {
     std::vector<uint64_t>().swap(s->data);
 }
 
+// A scan's device work starts (called under sv->mu): it and every scan
+// already in flight on any lane overlap.
+void start_run(fiu_server* sv, ServeScan* s) {
+    if (!sv->running.empty()) {
+        s->overlap = true;
+        for (ServeScan* o : sv->running) o->overlap = true;
+    }
+    sv->running.push_back(s);
+}
+
 void finish(fiu_server* sv, ServeScan* s, int status, fiu_ctx* ctx = nullptr) {
     s->status = status;
     release(sv, s, ctx ? ctx : sv->ctx);
@@ -132,8 +151,10 @@ void finish(fiu_server* sv, ServeScan* s, int status, fiu_ctx* ctx = nullptr) {
     s->done = Clock::now();
     s->finished = true;
     sv->bytes_in_use -= s->bytes;
+    sv->running.erase(std::remove(sv->running.begin(), sv->running.end(), s), sv->running.end());
     if (status == FIU_OK) {
         sv->completed++;
+        if (s->overlap) sv->overlapped++;
         sv->lat_ms.push_back(std::chrono::duration<double, std::milli>(s->done - s->submitted).count());
         sv->combos_samples += (double)binom(s->host.snps, s->order) * (double)(s->host.cases + s->host.ctrls);
     } else {
@@ -216,6 +237,8 @@ bool admit(fiu_server* sv, ServeScan* s) {
     const double per = (double)binom(s->w.dist_n, s->order) / std::max(1.0, (double)binom(s->w.dist_n, s->order - 1));
     s->chunk = std::max<long long>(1, (long long)(s->keep / std::max(1.0, per)));
     s->max_chunk = std::max<long long>(1, (long long)(kRoundBudget / std::max(1.0, per * (double)(s->host.cases + s->host.ctrls))));
+    std::lock_guard<std::mutex> g(sv->mu);
+    start_run(sv, s);
     return true;
 }
 
@@ -310,9 +333,11 @@ int run_round(fiu_server* sv) {
     return FIU_OK;
 }
 
-// The solo lane: scans that run alone, FIFO, on the lane's own stream.
-void solo_main(fiu_server* sv) {
-    Scope scope(sv->solo_ctx);
+// A solo lane: takes scans that run alone from the shared FIFO and runs each
+// on the lane's own stream.
+void solo_main(fiu_server* sv, int lane) {
+    fiu_ctx* ctx = sv->solo_ctx[lane];
+    Scope scope(ctx);
     for (;;) {
         ServeScan* s = nullptr;
         {
@@ -321,15 +346,16 @@ void solo_main(fiu_server* sv) {
             if (sv->stop) return;
             s = sv->solo_queue.front();
             sv->solo_queue.pop_front();
+            start_run(sv, s);
         }
         fiu_distribution dist{(int)s->host.snps, (int)s->order - 1, 1, 0};
-        const int rc = search_impl(sv->solo_ctx, s->res, s->order, &dist, s->outputs, s->comb.data(),
-                                   s->vals.data(), s->vals64.data(), &s->count, 0);
+        const int rc = search_impl(ctx, s->res, s->order, &dist, s->outputs, s->comb.data(), s->vals.data(),
+                                   s->vals64.data(), &s->count, 0);
         {
             std::lock_guard<std::mutex> g(sv->mu);
             sv->solo++;
         }
-        finish(sv, s, rc, sv->solo_ctx);
+        finish(sv, s, rc, ctx);
     }
 }
 
@@ -379,11 +405,13 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
         return rc;
     }
     sv->budget = budget_bytes ? budget_bytes : 120ull * 1000 * 1000 * 1000;
-    if ((rc = fiu_create(device, &sv->solo_ctx))) {
-        fiu_destroy(sv->ctx);
-        delete sv;
-        return rc;
-    }
+    for (int l = 0; l < kSoloLanes; ++l)
+        if ((rc = fiu_create(device, &sv->solo_ctx[l]))) {
+            for (int m = 0; m < l; ++m) fiu_destroy(sv->solo_ctx[m]);
+            fiu_destroy(sv->ctx);
+            delete sv;
+            return rc;
+        }
     cudaSetDevice(device);
     if (cudaMalloc((void**)&sv->d_desc, kSlots * sizeof(ScanDesc)) != cudaSuccess ||
         cudaMalloc((void**)&sv->d_state, kSlots * sizeof(ScanState)) != cudaSuccess ||
@@ -394,7 +422,7 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
         cudaFree(sv->d_desc);
         cudaFree(sv->d_state);
         cudaFree(sv->d_zero);
-        fiu_destroy(sv->solo_ctx);
+        for (fiu_ctx* c : sv->solo_ctx) fiu_destroy(c);
         fiu_destroy(sv->ctx);
         delete sv;
         return FIU_ERR_CUDA;
@@ -404,10 +432,11 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
         cudaSetDevice(sv->ctx->device);
         worker_main(sv);
     });
-    sv->solo_worker = std::thread([sv] {
-        cudaSetDevice(sv->ctx->device);
-        solo_main(sv);
-    });
+    for (int l = 0; l < kSoloLanes; ++l)
+        sv->solo_worker[l] = std::thread([sv, l] {
+            cudaSetDevice(sv->ctx->device);
+            solo_main(sv, l);
+        });
     *out = sv;
     return FIU_OK;
 }
@@ -473,6 +502,7 @@ int fiu_server_stats(fiu_server* sv, fiu_serve_stats* out) {
     out->active = sv->submitted - sv->completed - sv->failed - sv->queue.size();
     out->rounds = sv->rounds;
     out->solo = sv->solo;
+    out->overlapped = sv->overlapped;
     out->bytes_in_use = sv->bytes_in_use;
     out->combos_samples = sv->combos_samples;
     if (!sv->lat_ms.empty()) {
@@ -498,7 +528,8 @@ void fiu_server_destroy(fiu_server* sv) {
     sv->cv_work.notify_all();
     sv->cv_solo.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
-    if (sv->solo_worker.joinable()) sv->solo_worker.join();
+    for (std::thread& t : sv->solo_worker)
+        if (t.joinable()) t.join();
     cudaSetDevice(sv->ctx->device);
     for (ServeScan* s : sv->active) release(sv, s, sv->ctx);
     for (auto& kv : sv->tickets) {
@@ -509,7 +540,7 @@ void fiu_server_destroy(fiu_server* sv) {
     cudaFree(sv->d_state);
     cudaFree(sv->d_zero);
     cudaFree(sv->d_ents);
-    fiu_destroy(sv->solo_ctx);
+    for (fiu_ctx* c : sv->solo_ctx) fiu_destroy(c);
     fiu_destroy(sv->ctx);
     delete sv;
 }

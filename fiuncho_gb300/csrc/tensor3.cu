@@ -702,11 +702,22 @@ __global__ void __launch_bounds__(kPThreads, 1)
                 uint8_t* sA = st + kPSB;
                 const uint8_t* sJ = sA + kPSA;
                 const uint8_t* sI = sJ + kT3SJ;
+                // every load of the stage first, then the ANDs and stores: the loads
+                // overlap instead of waiting one by one behind the stores
                 const uint4 i0 = *reinterpret_cast<const uint4*>(sI + (c << 4));
                 const uint4 i1 = *reinterpret_cast<const uint4*>(sI + 128 + ((c ^ 1) << 4));
+                constexpr int kRows = (2 * kT3J + 4 * kPBuildWarps - 1) / (4 * kPBuildWarps);
+                uint4 jrow[kRows];
 #pragma unroll
-                for (int r = t >> 3; r < 2 * kT3J; r += 4 * kPBuildWarps) {  // j row r = (jj, y)
-                    const uint4 jv = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((c ^ (r & 7)) << 4));
+                for (int u = 0; u < kRows; ++u) {  // j row r = (jj, y)
+                    const int r = (t >> 3) + 4 * kPBuildWarps * u;
+                    if (r < 2 * kT3J) jrow[u] = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((c ^ (r & 7)) << 4));
+                }
+#pragma unroll
+                for (int u = 0; u < kRows; ++u) {
+                    const int r = (t >> 3) + 4 * kPBuildWarps * u;
+                    if (r >= 2 * kT3J) break;
+                    const uint4 jv = jrow[u];
                     const int m0 = 4 * (r >> 1) + (r & 1), m1 = m0 + 2;  // A rows (jj, x, y), x = 0, 1
                     uint4 v;
                     v.x = jv.x & i0.x;
@@ -1237,15 +1248,15 @@ static long long t3_items(int n, int L, std::vector<long long>& item_begin) {
 }
 
 static PFN_cuTensorMapEncodeTiled_v12000 t3_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         cudaDriverEntryPointQueryResult q;
         void* p = nullptr;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+            return (PFN_cuTensorMapEncodeTiled_v12000)p;
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     return fn;
 }
 
@@ -1398,16 +1409,16 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     if (w.order == 4)
         return launch_tensor4(w, plan.map_l, plan.map_a2, plan.map_k4, plan.map_i, plan.item4_begin, plan.item4_per,
                               plan.k_cases, plan.pack, g0, g1, sink, dump, single, pairs, triples, status, s, sms);
-    static bool attr = false;
-    if (!attr) {
+    // set once, by whichever host thread comes first (thread-safe static initialisation)
+    static const cudaError_t attr = [] {
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(tensor3p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(tensor2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2Smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+        return e;
+    }();
+    if (attr != cudaSuccess) return attr;
     const long long items = g1 - g0;
     if (items <= 0) return cudaSuccess;
     const double scale = 1.0 / (std::log(2.0) * 4294967296.0);

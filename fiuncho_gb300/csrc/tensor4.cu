@@ -12,7 +12,7 @@
 // N 128 region and the control samples into another (the MMA instruction
 // costs the same for N 128 as for N 256).  B rows are plane rows 2l+w
 // by TMA; A rows are the bytewise AND of the i, j and k plane rows, built in
-// shared memory by six producer warps from the TMA-staged rows (i AND j once
+// shared memory by two producer warps from the TMA-staged rows (i AND j once
 // per stage, then AND each k row).  Two accumulator regions alternate between
 // items so the next item's GEMM overlaps the epilogue.
 //
@@ -40,8 +40,14 @@ namespace fiu {
 
 constexpr int kT4K = 16, kT4L = 128;                // k and l SNPs per work item (64 l in the split form)
 constexpr int kT4M = 8 * kT4K, kT4N = 2 * kT4L;     // 128 x 256 GEMM tile
-constexpr int kT4BuildWarps = 6, kT4EpiWarps = 8;
-constexpr int kT4Threads = 32 * (2 + kT4BuildWarps + kT4EpiWarps);  // 512
+// Two A builders keep pace with the MMA (about 130 instructions per builder
+// thread and k-step against ~640 tensor cycles); 12 warps (three per SM
+// sub-partition) leave 168 registers a thread, which the epilogue's
+// derivation needs (128 at 16 warps made it spill ~1 KB a thread).
+constexpr int kT4BuildWarps = 2, kT4EpiWarps = 8;
+constexpr int kT4Threads = 32 * (2 + kT4BuildWarps + kT4EpiWarps);  // 384
+constexpr int kT4BuildRows = 2 * kT4K / (4 * kT4BuildWarps);          // k rows per builder thread and stage
+static_assert(2 * kT4K % (4 * kT4BuildWarps) == 0, "builder threads split the k rows evenly");
 constexpr int kT4Stages = 3;
 constexpr int kT4SB = kT4N * kT3KB;                 // 32 KB  l rows
 constexpr int kT4SA = kT4M * kT3KB;                 // 16 KB  A (k, x, y, z)
@@ -372,22 +378,32 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                 const uint8_t* sI = sK + kT4SK;
                 const uint8_t* sJ = sI + kT4SI;
                 // 128-byte swizzle: chunk c of box row r sits at chunk c ^ (r & 7)
+                // every load of the stage first, then the ANDs and stores: the loads
+                // overlap instead of waiting one by one behind the stores
                 const uint4 i0 = *reinterpret_cast<const uint4*>(sI + (c << 4));
                 const uint4 i1 = *reinterpret_cast<const uint4*>(sI + 128 + ((c ^ 1) << 4));
                 const uint4 j0 = *reinterpret_cast<const uint4*>(sJ + (c << 4));
                 const uint4 j1 = *reinterpret_cast<const uint4*>(sJ + 128 + ((c ^ 1) << 4));
+                uint4 kv[kT4BuildRows];
+#pragma unroll
+                for (int u = 0; u < kT4BuildRows; ++u) {  // k row r = (kk, z)
+                    const int r = (t >> 3) + 4 * kT4BuildWarps * u;
+                    kv[u] = *reinterpret_cast<const uint4*>(sK + r * 128 + ((c ^ (r & 7)) << 4));
+                }
                 uint4 ij[4];  // (x, y) = (0,0), (0,1), (1,0), (1,1)
                 ij[0] = make_uint4(i0.x & j0.x, i0.y & j0.y, i0.z & j0.z, i0.w & j0.w);
                 ij[1] = make_uint4(i0.x & j1.x, i0.y & j1.y, i0.z & j1.z, i0.w & j1.w);
                 ij[2] = make_uint4(i1.x & j0.x, i1.y & j0.y, i1.z & j0.z, i1.w & j0.w);
                 ij[3] = make_uint4(i1.x & j1.x, i1.y & j1.y, i1.z & j1.z, i1.w & j1.w);
-                for (int r = t >> 3; r < 2 * kT4K; r += 4 * kT4BuildWarps) {  // k row r = (kk, z)
-                    const uint4 kv = *reinterpret_cast<const uint4*>(sK + r * 128 + ((c ^ (r & 7)) << 4));
+#pragma unroll
+                for (int u = 0; u < kT4BuildRows; ++u) {
+                    const int r = (t >> 3) + 4 * kT4BuildWarps * u;
                     const int kk = r >> 1, z = r & 1;
 #pragma unroll
                     for (int xy = 0; xy < 4; ++xy) {
                         const int m = kk * 8 + xy * 2 + z;  // A row (kk, x, y, z)
-                        const uint4 v = make_uint4(ij[xy].x & kv.x, ij[xy].y & kv.y, ij[xy].z & kv.z, ij[xy].w & kv.w);
+                        const uint4 v =
+                            make_uint4(ij[xy].x & kv[u].x, ij[xy].y & kv[u].y, ij[xy].z & kv[u].z, ij[xy].w & kv[u].w);
                         *reinterpret_cast<uint4*>(sA + m * 128 + ((c ^ (m & 7)) << 4)) = v;
                     }
                 }

@@ -16,13 +16,10 @@ static cudaError_t sort_small(T* data, unsigned n, T worst, cudaStream_t st) {
     unsigned p = 1;
     while (p < n) p <<= 1;
     const size_t bytes = (size_t)p * sizeof(T);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(sort_block<T, Better>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(kSortCap * sizeof(T)));
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    // set once, by whichever host thread comes first (thread-safe static initialisation)
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        sort_block<T, Better>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSortCap * sizeof(T)));
+    if (attr != cudaSuccess) return attr;
     sort_block<T, Better><<<1, kSortThreads, bytes, st>>>(data, n, worst);
     count_launch();
     return cudaGetLastError();

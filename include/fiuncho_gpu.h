@@ -163,7 +163,8 @@ int fiu_search_batch(fiu_ctx *ctx, fiu_scan *scans, unsigned n_scans, int use_gr
  * buffers and running top-N resident and progress in rounds shared with every
  * other admitted scan, so a scan that arrives while others run starts in the
  * next round.  Scans that run best alone (tensor-core and pair-major order-4
- * scans) take a second lane with its own stream, concurrent with the rounds.
+ * scans) take one of two solo lanes (a worker thread with its own stream
+ * each), concurrent with each other and with the rounds.
  * Each scan's result is identical to fiu_search on it alone.
  * Thread-safe: submit/poll/stats may be called from any thread. */
 typedef struct fiu_server fiu_server;
@@ -173,9 +174,11 @@ typedef struct {
     uint64_t bytes_in_use;        /* device bytes held by admitted scans */
     double p50_ms, p99_ms, mean_ms, max_ms;  /* submit -> result latency of completed scans */
     double combos_samples;        /* combinations x samples completed */
-    uint64_t solo;                /* scans run alone on the solo lane (tensor-core and pair-major
-                                     order-4 scans, full-table scans above order 4), on their
-                                     own stream beside the rounds */
+    uint64_t solo;                /* scans run alone on a solo lane (tensor-core and pair-major
+                                     order-4 scans, full-table scans above order 4), on the
+                                     lane's own stream beside the rounds */
+    uint64_t overlapped;          /* completed scans whose device work overlapped another
+                                     scan's (either lane) */
 } fiu_serve_stats;
 /* budget_bytes: device memory the admitted scans may hold (0 = 120 GB). */
 int fiu_server_create(int device, uint64_t budget_bytes, fiu_server **out);

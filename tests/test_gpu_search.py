@@ -366,7 +366,7 @@ def test_tensor4_search_many_tiles(oracle, snps, n_case, n_ctrl, out):
 
 def test_order4_reduced_work_is_automatic(gs, golden_synth):
     """One-hot order-4 searches pick a reduced-work kernel by themselves (pair-major below
-    4 096 samples, tcgen05 above, per-prefix for a Distribution layer with step > 1);
+    2 048 samples, tcgen05 above, per-prefix for a Distribution layer with step > 1);
     non-one-hot data keeps the full kernel."""
     from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident
     ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
@@ -380,7 +380,7 @@ def test_order4_reduced_work_is_automatic(gs, golden_synth):
     bad = Dataset(100, 70, 9, 2, 2, rng.integers(0, 2 ** 63, 9 * 3 * 4, dtype=np.uint64))
     g.run(bad, 4, Distribution(9, 3), 5)
     assert g.last_tile()[0] == 1
-    # with 4 096 samples or more the tcgen05 kernel takes over
+    # with 2 048 samples or more the tcgen05 kernel takes over
     big = _one_hot_dataset(9, 24, 2100, 2000)
     g.run(big, 4, Distribution(24, 3), 10)
     assert g.last_tile()[0] == 4

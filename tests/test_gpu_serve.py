@@ -104,3 +104,22 @@ def test_server_concurrent_submitters():
         pass
     finally:
         srv.close()
+
+
+def test_server_solo_lanes_overlap():
+    """Two tensor-core scans submitted together run on the two solo lanes at the
+    same time (their device work overlaps) and give the results of each alone."""
+    from fiuncho_gb300 import Distribution, GpuSearch, Server
+    gs = GpuSearch(0)
+    data = [_ds(50 + i, 1500, 3000, 3000) for i in range(2)]
+    ref = [gs.run(ds, 3, Distribution(ds.snps, 2), 40, with_fp64=True) for ds in data]
+    srv = Server(0)
+    try:
+        tickets = [srv.submit(ds, 3, 40) for ds in data]
+        for t, r in zip(tickets, ref):
+            _same(srv.result(t), r)
+        st = srv.stats()
+        assert st["completed"] == 2 and st["solo"] == 2
+        assert st["overlapped"] == 2
+    finally:
+        srv.close()
