@@ -204,10 +204,11 @@ static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
 // Below this many samples an order-4 scan is faster on the CUDA-core
 // pair-major kernel: the tensor kernel's per-combination epilogue then
 // outweighs the counting it saves (measured at 150 SNPs, pair-major vs
-// tensor: 1 060 samples 7.1 vs 9.6 ms, 1 800 samples 8.9 vs 9.6 ms, 4 000
-// samples 14.7 vs 9.9 ms, 14 900 samples 44.8 vs 17.2 ms).  Forcing
-// FIU_KERNEL_TENSOR still uses it.
-constexpr int kT4MinSamples = 2048;
+// tensor: 1 060 samples 7.1 vs 6.2 ms, 1 800 samples 8.9 vs 6.3 ms, 4 000
+// samples 14.8 vs 7.0 ms, 14 900 samples 44.8 vs 16.9 ms; the pair-major
+// time falls with the samples, the tensor kernel's hardly below 6 ms).
+// Forcing FIU_KERNEL_TENSOR still uses it.
+constexpr int kT4MinSamples = 1024;
 
 int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int requested_kernel, int& kernel, int& tp,
                 bool allow_tensor) {

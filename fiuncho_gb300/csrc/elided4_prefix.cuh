@@ -152,53 +152,69 @@ __device__ __forceinline__ void e4_slices_w(const uint32_t (&cp)[2][8], const E4
     }
 }
 
-// Both classes' slices at once: use(sw, t0, t1) receives slice sw of the case
-// table (t0) and of the control table (t1); w0 / w1 are the words of passes
-// 0 / 1 (cases / controls), ps0 / ps1 the prefix star tables of the two
-// classes.  The totals follow cell by cell as t0 + t1.
-template <class PS0, class PS1, class Use>
-__device__ __forceinline__ void e4_slices2(const uint32_t (&cp)[2][8], const E4Words& w0, const E4Words& w1,
-                                           const PS0& ps0, const PS1& ps1, Use&& use) {
-    auto star = [&](const E4Words& wd, int cls, int w, int q) -> uint32_t {
+// Both classes in one derivation, packed: a cell's case count in the low and
+// its control count in the high 16 bits of one word.  Every count lies below
+// 2^16 (classes of at most 65 535 samples) and every intermediate count of a
+// consistent one-hot data set is non-negative, so the packed subtractions never
+// borrow across the halves.
+__device__ __forceinline__ uint32_t pk16(uint32_t c, uint32_t t, int hi) {
+    return __byte_perm(c, t, hi ? 0x7632 : 0x5410);  // (c half, t half) -> c | t << 16
+}
+
+// Sub-combination cores of one combination (i, j, k, l) for both classes: the
+// case (tc) and control (tt) words of the triples (i,j,l), (i,k,l), (j,k,l),
+// and the pair / single words (both classes in each).
+struct E4Both {
+    uint4 tc[3], tt[3];
+    uint4 pil, pjl, pkl, sl;
+};
+
+// The three slices, packed; use(sw, t) receives slice sw's 27 cells
+// t[(x*3+y)*3+z]; ps(q) is the prefix's packed star table.
+template <class PS, class Use>
+__device__ __forceinline__ void e4_slices_packed(const uint32_t (&cp)[2][8], const E4Both& wd, const PS& ps,
+                                                 Use&& use) {
+    auto star = [&](int w, int q) -> uint32_t {
         const int a = q / 9, b = (q / 3) % 3, z = q % 3;
         if (a < 2 && b < 2 && z < 2) {
-            const uint32_t c = cp[cls][(a * 2 + b) * 2 + z];
-            return w ? c >> 16 : c & 0xffffu;
+            const int r = (a * 2 + b) * 2 + z;
+            return pk16(cp[0][r], cp[1][r], w);
         }
-        if (a < 2 && b < 2) return tcell(wd.ta[0], a, b, w);
-        if (a < 2 && z < 2) return tcell(wd.ta[1], a, z, w);
-        if (b < 2 && z < 2) return tcell(wd.ta[2], b, z, w);
-        if (a < 2) return pcore(wd.pil, cls, a, w);
-        if (b < 2) return pcore(wd.pjl, cls, b, w);
-        if (z < 2) return pcore(wd.pkl, cls, z, w);
-        return cls ? (w ? wd.sl.w : wd.sl.z) : (w ? wd.sl.y : wd.sl.x);
+        auto tri = [&](int u, int x, int y) {
+            const int c = x * 4 + y * 2 + w;
+            return pk16((&wd.tc[u].x)[c >> 1], (&wd.tt[u].x)[c >> 1], c & 1);
+        };
+        auto pr = [&](const uint4& v, int x) { return pk16((&v.x)[x], (&v.x)[2 + x], w); };
+        if (a < 2 && b < 2) return tri(0, a, b);
+        if (a < 2 && z < 2) return tri(1, a, z);
+        if (b < 2 && z < 2) return tri(2, b, z);
+        if (a < 2) return pr(wd.pil, a);
+        if (b < 2) return pr(wd.pjl, b);
+        if (z < 2) return pr(wd.pkl, z);
+        return __byte_perm(w ? wd.sl.y : wd.sl.x, w ? wd.sl.w : wd.sl.z, 0x5410);
     };
 #pragma unroll
     for (int sw = 0; sw < 3; ++sw) {
-        uint32_t t0[27], t1[27];
+        uint32_t t[27];
 #pragma unroll
-        for (int q = 0; q < 27; ++q) {
-            t0[q] = sw < 2 ? star(w0, 0, sw, q) : ps0(q) - star(w0, 0, 0, q) - star(w0, 0, 1, q);
-            t1[q] = sw < 2 ? star(w1, 1, sw, q) : ps1(q) - star(w1, 1, 0, q) - star(w1, 1, 1, q);
-        }
-        star_to_table(t0);
-        star_to_table(t1);
-        use(sw, t0, t1);
+        for (int q = 0; q < 27; ++q) t[q] = sw < 2 ? star(sw, q) : ps(q) - star(0, q) - star(1, q);
+        star_to_table(t);
+        use(sw, t);
     }
 }
 
 // One slice's contribution to the key estimate, cell by cell, in units of
-// 2^-16 bits: the pairwise single-precision sum over its 27 cells of
+// 2^-16 bits: the pairwise single-precision sum over its 27 packed cells of
 // g = a lg2 a + b lg2 b - (a+b) lg2 (a+b) (a cases, b controls; each g lies in
-// [-(a+b), 0]), rounded to 2^-16.
-__device__ __forceinline__ long long e4_slice_estimate2(const uint32_t* t0, const uint32_t* t1, uint32_t n0,
-                                                        uint32_t n1) {
+// [-(a+b), 0]), rounded to 2^-16.  Each 16-bit half becomes the float 2^23 + c
+// by a byte permutation, minus 2^23.
+__device__ __forceinline__ long long e4_slice_estimate_packed(const uint32_t* t) {
     const float tiny = 9.5367431640625e-07f;  // 2^-20: c*lg2(c + tiny) = 0 at c = 0
     float g[27];
 #pragma unroll
     for (int q = 0; q < 27; ++q) {
-        const float a = __uint_as_float(0x4B000000u | min(t0[q], n0)) - 8388608.0f;
-        const float b = __uint_as_float(0x4B000000u | min(t1[q], n1)) - 8388608.0f;
+        const float a = __uint_as_float(__byte_perm(t[q], 0x4B000000u, 0x7610)) - 8388608.0f;
+        const float b = __uint_as_float(__byte_perm(t[q], 0x4B000000u, 0x7632)) - 8388608.0f;
         const float sab = a + b;
         float la, lb, ls;
         asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(la) : "f"(a + tiny));
@@ -276,6 +292,30 @@ struct E4PrefixStar {
         if (b < 2) return sg(sj, b);
         if (z < 2) return sg(sk, z);
         return nc;
+    }
+};
+
+// Packed star table of the prefix triple (i, j, k) (both classes), entry q,
+// from the prefix's cores: triple (cases tc, controls tt), pairs (i,j), (i,k),
+// (j,k), singles i, j, k; nn = n_cases | n_ctrls << 16.
+struct E4PrefixStarPacked {
+    uint4 tc, tt, pij, pik, pjk, si, sj, sk;
+    uint32_t nn;
+    __device__ __forceinline__ uint32_t operator()(int q) const {
+        const int a = q / 9, b = (q / 3) % 3, z = q % 3;
+        auto pr = [](const uint4& v, int x, int y) { return pk16((&v.x)[x], (&v.x)[2 + x], y); };
+        auto sg = [](const uint4& v, int x) { return __byte_perm(x ? v.y : v.x, x ? v.w : v.z, 0x5410); };
+        if (a < 2 && b < 2 && z < 2) {
+            const int c = a * 4 + b * 2 + z;
+            return pk16((&tc.x)[c >> 1], (&tt.x)[c >> 1], c & 1);
+        }
+        if (a < 2 && b < 2) return pr(pij, a, b);
+        if (a < 2 && z < 2) return pr(pik, a, z);
+        if (b < 2 && z < 2) return pr(pjk, b, z);
+        if (a < 2) return sg(si, a);
+        if (b < 2) return sg(sj, b);
+        if (z < 2) return sg(sk, z);
+        return nn;
     }
 };
 

@@ -57,16 +57,22 @@ constexpr int kT4SJ = 1024;                         // j rows
 constexpr int kT4Stage = kT4SB + kT4SA + kT4SK + kT4SI + kT4SJ;  // 54 KB, a multiple of 1 KB
 constexpr int kT4Ebuf = 4096;                       // per epilogue warp: 32 combinations x 8 (x,y,z) x 16 B
 
-// Sources of the epilogue that depend on one of k or l only, staged in shared
-// memory once per item by the epilogue warps: the star tables of the prefix
-// triples (i, j, k0 + kk) for cases, controls and totals, and the triple
-// (i, j, l), pair (i, l), (j, l) and single l cores of every l of the item.
+// Sources of the epilogue that depend on one of k or l only, copied into
+// shared memory by the epilogue threads (cp.async: global to shared without
+// registers) one item ahead, into two alternating buffers: the triple
+// (i, j, l), pair (i, l), (j, l) and single l cores of every l of the item,
+// and the triple (i, j, k), pair (i, k), (j, k) and single k cores of every k
+// with the pair (i, j) and singles i, j (the prefix star tables follow from
+// these in the epilogue).
 struct T4Item {
-    uint32_t pstar[kT4K][81];
     uint4 tijl[kT4L][2];
     uint4 pil[kT4L], pjl[kT4L], sl[kT4L];
+    uint4 tijk[kT4K][2];
+    uint4 pik[kT4K], pjk[kT4K], sk[kT4K];
+    uint4 pij, si, sj;
 };
-constexpr size_t kT4Smem = 1024 + (size_t)kT4Stages * kT4Stage + (size_t)kT4EpiWarps * kT4Ebuf + sizeof(T4Item);
+constexpr size_t kT4Smem =
+    1024 + (size_t)kT4Stages * kT4Stage + (size_t)kT4EpiWarps * kT4Ebuf + 2 * sizeof(T4Item);
 // instruction descriptor: e4m3 x e4m3 -> FP32, M 128, N 256 (packed) or 128 (split)
 constexpr uint32_t t4_idesc(int N) { return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kT4M >> 4) << 24); }
 static_assert(kT4Smem <= 227 * 1024 - 256, "order-4 tensor kernel shared memory");
@@ -116,37 +122,78 @@ __device__ __forceinline__ void t4_decode(const long long* __restrict__ begin, c
 // the row-wise writes (fixed ll) and the combination-wise reads (fixed xyz).
 __device__ __forceinline__ int t4_chunk(int kk, int ll, int xyz) { return (kk * 8 + ll) * 8 + (xyz ^ ll); }
 
-// Words of pass PC for combination (k0 + kk, l0 + ll): l-only and prefix
-// sources from the item's shared-memory stage, (k, l) sources from global memory.
-template <int PC>
-__device__ __forceinline__ E4Words t4_words(const T4Item& it, int ll, const uint4* tik, const uint4* tjk,
-                                            const uint4* pkl) {
-    asm volatile("" ::: "memory");
-    E4Words wd;
-    wd.ta[0] = it.tijl[ll][PC == 1 ? 1 : 0];
-    wd.tb[0] = PC == 2 ? it.tijl[ll][1] : make_uint4(0, 0, 0, 0);
-    wd.ta[1] = __ldg(tik + (PC == 1 ? 1 : 0));
-    wd.tb[1] = PC == 2 ? __ldg(tik + 1) : make_uint4(0, 0, 0, 0);
-    wd.ta[2] = __ldg(tjk + (PC == 1 ? 1 : 0));
-    wd.tb[2] = PC == 2 ? __ldg(tjk + 1) : make_uint4(0, 0, 0, 0);
+// Estimate of the key minus the base in units of 2^-16 bits, cell by cell
+// over both classes in one packed derivation (the totals as their sum):
+// within t4_margin.  l-only and prefix sources come from the item's
+// shared-memory stage, (k, l) sources from global memory.
+__device__ __forceinline__ long long t4_estimate(const uint32_t (&cp)[2][8], const T4Item& it, int kk, int ll,
+                                                 const uint4* tik, const uint4* tjk, const uint4* pkl, uint32_t nn) {
+    E4Both wd;
+    wd.tc[0] = it.tijl[ll][0];
+    wd.tt[0] = it.tijl[ll][1];
+    wd.tc[1] = __ldg(tik);
+    wd.tt[1] = __ldg(tik + 1);
+    wd.tc[2] = __ldg(tjk);
+    wd.tt[2] = __ldg(tjk + 1);
     wd.pil = it.pil[ll];
     wd.pjl = it.pjl[ll];
     wd.pkl = __ldg(pkl);
     wd.sl = it.sl[ll];
-    return wd;
+    E4PrefixStarPacked ps;
+    ps.tc = it.tijk[kk][0];
+    ps.tt = it.tijk[kk][1];
+    ps.pij = it.pij;
+    ps.pik = it.pik[kk];
+    ps.pjk = it.pjk[kk];
+    ps.si = it.si;
+    ps.sj = it.sj;
+    ps.sk = it.sk[kk];
+    ps.nn = nn;
+    long long acc = 0;
+    e4_slices_packed(cp, wd, ps, [&](int, const uint32_t* t) { acc += e4_slice_estimate_packed(t); });
+    return acc;
 }
 
-// Estimate of the key minus the base in units of 2^-16 bits, cell by cell
-// over both classes (the totals as their sum): within t4_margin.
-__device__ __forceinline__ long long t4_estimate(const uint32_t (&cp)[2][8], const T4Item& it, int kk, int ll,
-                                                 const uint4* tik, const uint4* tjk, const uint4* pkl, uint32_t n0,
-                                                 uint32_t n1) {
-    const E4Words w0 = t4_words<0>(it, ll, tik, tjk, pkl), w1 = t4_words<1>(it, ll, tik, tjk, pkl);
-    const uint32_t *p0 = it.pstar[kk], *p1 = it.pstar[kk] + 27;
-    long long acc = 0;
-    e4_slices2(cp, w0, w1, [&](int q) { return p0[q]; }, [&](int q) { return p1[q]; },
-               [&](int, const uint32_t* t0, const uint32_t* t1) { acc += e4_slice_estimate2(t0, t1, n0, n1); });
-    return acc;
+// 16-byte asynchronous copy global -> shared (both addresses 16-byte aligned).
+__device__ __forceinline__ void t4_cp16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+// Copies item g's k-only and l-only sources into it (epilogue thread et of
+// 256), then commits this thread's copy group.
+template <int L>
+__device__ __forceinline__ void t4_stage(T4Item& it, long long g, int et, const long long* __restrict__ begin,
+                                         const long long* __restrict__ per, int n, const uint32_t* __restrict__ single,
+                                         const uint4* __restrict__ pairs, const uint4* __restrict__ triples) {
+    int i, j, k0, l0;
+    t4_decode<L>(begin, per, n, g, i, j, k0, l0);
+    const uint4* single4 = reinterpret_cast<const uint4*>(single);
+    if (et < L) {
+        const int l = l0 + et;
+        if (l < n) {
+            const uint4* t = triples + 2 * triple_index(i, j, l, n);
+            t4_cp16(&it.tijl[et][0], t);
+            t4_cp16(&it.tijl[et][1], t + 1);
+            t4_cp16(&it.pil[et], pairs + pair_index(i, l, n));
+            t4_cp16(&it.pjl[et], pairs + pair_index(j, l, n));
+            t4_cp16(&it.sl[et], single4 + l);
+        }
+    } else if (et >= kT4L && et < kT4L + kT4K) {
+        const int kk = et - kT4L, k = k0 + kk;
+        if (k < n) {
+            const uint4* t = triples + 2 * triple_index(i, j, k, n);
+            t4_cp16(&it.tijk[kk][0], t);
+            t4_cp16(&it.tijk[kk][1], t + 1);
+            t4_cp16(&it.pik[kk], pairs + pair_index(i, k, n));
+            t4_cp16(&it.pjk[kk], pairs + pair_index(j, k, n));
+            t4_cp16(&it.sk[kk], single4 + k);
+        }
+    } else if (et == kT4L + kT4K) {
+        t4_cp16(&it.pij, pairs + pair_index(i, j, n));
+        t4_cp16(&it.si, single4 + i);
+        t4_cp16(&it.sj, single4 + j);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
 // Exact key of one combination (and its tables when o): the rare path, kept
@@ -195,7 +242,7 @@ __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink,
         bool cand = dump != nullptr;
         if (!cand) {
             const int kk = k - k0, ll = l - l0;
-            const long long est = t4_estimate(cp, it, kk, ll, tik, tjk, pkl, d.n_cases, d.n_ctrls);
+            const long long est = t4_estimate(cp, it, kk, ll, tik, tjk, pkl, d.n_cases | d.n_ctrls << 16);
             cand = est >= thr_q;
         }
         if (cand) {
@@ -424,54 +471,23 @@ __global__ void __launch_bounds__(kT4Threads, 1)
         const int kkw = lane >> 3, xyz = lane & 7;  // this thread's accumulator row (4 q + kkw, xyz)
         const int kkc = lane >> 3, llc = lane & 7;  // this lane's combination in a column group
         const int et = tid - 32 * (2 + kT4BuildWarps);  // 0..255
-        T4Item& it = *reinterpret_cast<T4Item*>(ebuf_all + kT4EpiWarps * (kT4Ebuf / 4));
-        const uint4* single4 = reinterpret_cast<const uint4*>(single);
+        T4Item* items = reinterpret_cast<T4Item*>(ebuf_all + kT4EpiWarps * (kT4Ebuf / 4));  // two buffers
         long long item = 0;
+        if (g0 + blockIdx.x < g1)
+            t4_stage<L>(items[0], g0 + blockIdx.x, et, begin, per, n, single, pairs, triples);
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
             int i, j, k0, l0;
             t4_decode<L>(begin, per, n, g, i, j, k0, l0);
             const int buf = (int)(item & 1);
             const int k = k0 + 4 * q + kkc;
-            // stage the item's k-only and l-only sources (named barrier 1: the 256 epilogue threads)
+            // this thread's copies of the item's sources have landed; the named
+            // barrier (the 256 epilogue threads) makes everyone's visible and
+            // frees the other buffer (every thread is done with the previous item)
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
             asm volatile("bar.sync 1, %0;" ::"n"(32 * kT4EpiWarps) : "memory");
-            if (et < L) {
-                const int l = l0 + et;
-                if (l < n) {
-                    const uint4* t = triples + 2 * triple_index(i, j, l, n);
-                    it.tijl[et][0] = __ldg(t);
-                    it.tijl[et][1] = __ldg(t + 1);
-                    it.pil[et] = __ldg(pairs + pair_index(i, l, n));
-                    it.pjl[et] = __ldg(pairs + pair_index(j, l, n));
-                    it.sl[et] = __ldg(single4 + l);
-                }
-            } else if (et >= kT4L && et < kT4L + 3 * kT4K) {
-                const int kk = (et - kT4L) / 3, pc = (et - kT4L) % 3, kp = k0 + kk;
-                if (kp < n) {
-                    E4Prefix pre;
-                    pre.tijk = triples + 2 * triple_index(i, j, kp, n);
-                    pre.pij = pairs + pair_index(i, j, n);
-                    pre.pik = pairs + pair_index(i, kp, n);
-                    pre.pjk = pairs + pair_index(j, kp, n);
-                    pre.si = single4 + i;
-                    pre.sj = single4 + j;
-                    pre.sk = single4 + kp;
-                    uint32_t* ps = it.pstar[kk] + 27 * pc;
-                    if (pc == 0) {
-                        const E4PrefixStar<0> st(pre, d.n_cases);
-#pragma unroll 1
-                        for (int qq = 0; qq < 27; ++qq) ps[qq] = st(qq);
-                    } else if (pc == 1) {
-                        const E4PrefixStar<1> st(pre, d.n_ctrls);
-#pragma unroll 1
-                        for (int qq = 0; qq < 27; ++qq) ps[qq] = st(qq);
-                    } else {
-                        const E4PrefixStar<2> st(pre, d.n_cases + d.n_ctrls);
-#pragma unroll 1
-                        for (int qq = 0; qq < 27; ++qq) ps[qq] = st(qq);
-                    }
-                }
-            }
-            asm volatile("bar.sync 1, %0;" ::"n"(32 * kT4EpiWarps) : "memory");
+            if (g + gridDim.x < g1)
+                t4_stage<L>(items[buf ^ 1], g + gridDim.x, et, begin, per, n, single, pairs, triples);
+            const T4Item& it = items[buf];
             if (!t3_wait(smem_u32(&acc_full[buf]), (uint32_t)((item >> 1) & 1), abort)) {
                 ok = false;
                 break;
@@ -533,6 +549,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                         valid ? l : 3, valid, lane);
             }
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");  // no copy in flight at exit (after an abort)
     }
     if (!ok) *abort = 1;
     asm volatile("tcgen05.fence::before_thread_sync;");

@@ -159,14 +159,14 @@ def test_search_synth_vs_reference(gs, oracle, golden_synth, order):
     from fiuncho_gb300 import GpuSearch
     ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
     res, v64 = gs.run(ds, order, Distribution(ds.snps, order - 1), 50, with_fp64=True)
-    # one-hot, whole data set: tcgen05 at orders 2-3; at order 4 with 2 000 samples the
-    # pair-major CUDA-core kernel is the faster one, and the forced tcgen05 run agrees
-    assert gs.last_tile()[0] == (4 if order < 4 else 2)
+    # one-hot, whole data set: the tcgen05 kernels at orders 2-4; at order 4 the forced
+    # pair-major CUDA-core kernel agrees
+    assert gs.last_tile()[0] == 4
     if order == 4:
-        g4 = GpuSearch(0, kernel=4)
-        r4, v4 = g4.run(ds, 4, Distribution(ds.snps, 3), 50, with_fp64=True)
-        assert g4.last_tile()[0] == 4
-        assert [x.combination for x in r4] == [x.combination for x in res] and np.array_equal(v4, v64)
+        g2 = GpuSearch(0, kernel=2)
+        r2, v2 = g2.run(ds, 4, Distribution(ds.snps, 3), 50, with_fp64=True)
+        assert g2.last_tile()[0] == 2
+        assert [x.combination for x in r2] == [x.combination for x in res] and np.array_equal(v2, v64)
     got = _check_topn(oracle, ds, order, 50, res, v64)
     rc = golden_synth["o%d_top50_combos" % order]
     rv = golden_synth["o%d_top50_vals" % order].astype(np.float64)
@@ -366,7 +366,7 @@ def test_tensor4_search_many_tiles(oracle, snps, n_case, n_ctrl, out):
 
 def test_order4_reduced_work_is_automatic(gs, golden_synth):
     """One-hot order-4 searches pick a reduced-work kernel by themselves (pair-major below
-    2 048 samples, tcgen05 above, per-prefix for a Distribution layer with step > 1);
+    1 024 samples, tcgen05 above, per-prefix for a Distribution layer with step > 1);
     non-one-hot data keeps the full kernel."""
     from fiuncho_gb300 import Dataset, Distribution, GpuSearch, Resident
     ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
@@ -380,7 +380,10 @@ def test_order4_reduced_work_is_automatic(gs, golden_synth):
     bad = Dataset(100, 70, 9, 2, 2, rng.integers(0, 2 ** 63, 9 * 3 * 4, dtype=np.uint64))
     g.run(bad, 4, Distribution(9, 3), 5)
     assert g.last_tile()[0] == 1
-    # with 2 048 samples or more the tcgen05 kernel takes over
+    # below 1 024 samples the pair-major kernel, with 1 024 or more the tcgen05 kernel
+    small = _one_hot_dataset(8, 24, 300, 300)
+    g.run(small, 4, Distribution(24, 3), 10)
+    assert g.last_tile()[0] == 2
     big = _one_hot_dataset(9, 24, 2100, 2000)
     g.run(big, 4, Distribution(24, 3), 10)
     assert g.last_tile()[0] == 4
