@@ -22,10 +22,10 @@ cores.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--workload order3_2000x8000]
 
-With --gpus N > 1 (launched by torch.distributed.run), every rank takes the
-Distribution(snps, order-1, N, rank) share of the prefixes (no data-path
-collective), rank 0 gathers the top-N lists; value = all ranks' work / the
-slowest rank's time.
+With --gpus N > 1 (launched by torch.distributed.run), rank r searches shard r
+of N of the whole search (equal ranges of the serving kernel's work units, so
+every GPU keeps the whole-data-set kernels; no data-path collective), rank 0
+gathers the top-N lists; value = all ranks' work / the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -206,9 +206,12 @@ def run_gpu(args, spec):
     ctx = gs.ctx
     lib = ctx.lib
     res = Resident(ctx, ds)
-    dist_ = Distribution(ds.snps, spec.order - 1, ws, rank)
-    combos = combos_of(ds.snps, spec.order, ws, rank) if ws > 1 else math.comb(ds.snps, spec.order)
+    # rank r of N searches shard r of the whole search's work units (the same
+    # whole-data-set kernels on every GPU); N = 1 is the whole search
     total_combos = math.comb(ds.snps, spec.order)
+
+    def search():
+        return gs.run_shard(res, spec.order, rank, ws, spec.outputs)
     stream = torch.cuda.ExternalStream(lib.fiu_stream(ctx.h), device=torch.device("cuda", local))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 512 MB > L2 (129 MB)
 
@@ -221,7 +224,7 @@ def run_gpu(args, spec):
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
-        out = gs.run(res, spec.order, dist_, spec.outputs)
+        out = search()
     # ---- timed region: resident data set, one event pair per step on the library's stream
     ctx.check(lib.fiu_set_kernel_timing(ctx.h, 1))
     launches0 = ctx.launches
@@ -233,7 +236,7 @@ def run_gpu(args, spec):
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            out = gs.run(res, spec.order, dist_, spec.outputs)
+            out = search()
             e1.record(stream)
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
@@ -259,11 +262,10 @@ def run_gpu(args, spec):
     comb = np.zeros(spec.outputs * spec.order, np.int32)
     vals = np.zeros(spec.outputs, np.float32)
     cnt = C.c_uint(0)
-    dstruct = dist_.c_struct()
 
     def e2e_call():
-        ctx.check(lib.fiu_search(ctx.h, C.byref(hds), spec.order, C.byref(dstruct), spec.outputs,
-                                 _lib.ptr(comb, C.c_int32), _lib.ptr(vals, C.c_float), C.byref(cnt)))
+        ctx.check(lib.fiu_search_shard(ctx.h, C.byref(hds), spec.order, rank, ws, spec.outputs,
+                                       _lib.ptr(comb, C.c_int32), _lib.ptr(vals, C.c_float), C.byref(cnt)))
 
     e2e_call()
     e2e_t = []
@@ -332,7 +334,7 @@ def run_gpu(args, spec):
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": args.workload, "snps": spec.snps, "cases": spec.cases, "ctrls": spec.ctrls,
                    "order": spec.order, "outputs": spec.outputs, "combinations": total_combos,
-                   "parallelism": "prefix-distribution over %d rank(s)" % ws,
+                   "parallelism": "work-unit shards over %d rank(s)" % ws,
                    "l2": "flushed between steps (512 MB write); data set %.1f MB is L2-resident by design"
                          % (ds_bytes / 1e6),
                    "top1": (top.combination if top else None), "planted": [list(p) for p in planted]},

@@ -84,6 +84,10 @@ _SIGS = {
                                       C.POINTER(C.c_uint)]),
     "fiu_search_resident64": (C.c_int, [_vp, _vp, C.c_uint, C.POINTER(Distribution_t), C.c_uint, _i32p, _f32p,
                                         _f64p, C.POINTER(C.c_uint)]),
+    "fiu_search_shard": (C.c_int, [_vp, C.POINTER(Dataset_t), C.c_uint, C.c_uint, C.c_uint, C.c_uint, _i32p, _f32p,
+                                   C.POINTER(C.c_uint)]),
+    "fiu_search_shard_resident64": (C.c_int, [_vp, _vp, C.c_uint, C.c_uint, C.c_uint, C.c_uint, _i32p, _f32p,
+                                              _f64p, C.POINTER(C.c_uint)]),
     "fiu_combine": (C.c_int, [_vp, _u64p, C.c_uint, _u64p, C.c_uint64, C.c_uint64, _u64p]),
     "fiu_combine_and_popcnt": (C.c_int, [_vp, _u64p, C.c_uint, _u64p, C.c_uint64, C.c_uint64, _u32p, _u32p,
                                          C.c_uint]),

@@ -306,11 +306,12 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
 // The search on a resident data set (ThreadedSearch::run semantics).
 int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
                 unsigned outputs, int32_t* out_comb, float* out_vals, double* out_vals64, unsigned* out_count,
-                int kernel) {
+                int kernel, unsigned shard, unsigned n_shards) {
     if (!ctx) return FIU_ERR_INVALID;
     Scope scope(ctx);
     if (!out_count || (outputs && (!out_comb || !out_vals)))
         return fail(ctx, FIU_ERR_INVALID, "null output pointer");
+    if (n_shards == 0 || shard >= n_shards) return fail(ctx, FIU_ERR_INVALID, "shard out of range");
     *out_count = 0;
     ScanWork w;
     int rc = make_work(ctx, res, order, dist, outputs, w);
@@ -343,9 +344,10 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
                             : pair_major ? (double)binom(w.dist_n, 4) / std::max(1ll, res->e4_items)
                                          : per_prefix;
     long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_unit)));
-    long long m = 0;
-    while (m < units) {
-        const long long m1 = std::min(units, m + chunk);
+    long long m = units / n_shards * shard + std::min<long long>(shard, units % n_shards);
+    const long long m_end = m + units / n_shards + (shard < units % n_shards ? 1 : 0);
+    while (m < m_end) {
+        const long long m1 = std::min(m_end, m + chunk);
         ctx->pinned[0] = have;
         ctx->pinned[1] = 0;
         CK(cudaMemcpyAsync(count, ctx->pinned, 2 * sizeof(unsigned), cudaMemcpyHostToDevice, s), "reset counters");
@@ -631,6 +633,28 @@ int fiu_search_resident64(fiu_ctx* ctx, const fiu_resident* res, unsigned order,
                           const fiu_distribution* distribution, unsigned outputs, int32_t* out_combinations,
                           float* out_vals, double* out_vals64, unsigned* out_count) {
     return search_impl(ctx, res, order, distribution, outputs, out_combinations, out_vals, out_vals64, out_count, 0);
+}
+
+int fiu_search_shard(fiu_ctx* ctx, const fiu_dataset* dataset, unsigned order, unsigned shard, unsigned n_shards,
+                     unsigned outputs, int32_t* out_combinations, float* out_vals, unsigned* out_count) {
+    if (!ctx || !dataset) return FIU_ERR_INVALID;
+    fiu_resident* r = nullptr;
+    int rc = fiu_dataset_upload(ctx, dataset, &r);
+    if (rc) return rc;
+    const fiu_distribution whole{(int)dataset->snps, (int)order - 1, 1, 0};
+    rc = search_impl(ctx, r, order, &whole, outputs, out_combinations, out_vals, nullptr, out_count, 0, shard,
+                     n_shards);
+    fiu_dataset_free(ctx, r);
+    return rc;
+}
+
+int fiu_search_shard_resident64(fiu_ctx* ctx, const fiu_resident* res, unsigned order, unsigned shard,
+                                unsigned n_shards, unsigned outputs, int32_t* out_combinations, float* out_vals,
+                                double* out_vals64, unsigned* out_count) {
+    if (!ctx || !res) return FIU_ERR_INVALID;
+    const fiu_distribution whole{(int)res->d.snps, (int)order - 1, 1, 0};
+    return search_impl(ctx, res, order, &whole, outputs, out_combinations, out_vals, out_vals64, out_count, 0, shard,
+                       n_shards);
 }
 
 int fiu_combine(fiu_ctx* ctx, const uint64_t* t1, unsigned size1, const uint64_t* t2, uint64_t cases_words,

@@ -88,9 +88,12 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
 bool e4_pair_major(int kernel, const fiu_resident* res, const ScanWork& w);
 cudaError_t launch_kernel(int kernel, int tp, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
                           const CandSink& sink, uint32_t* dump, cudaStream_t s, int sms);
+// shard / n_shards: the search covers the shard-th of n_shards contiguous
+// ranges of the serving kernel's work units (tensor work items, pair-major
+// items or prefix ordinals).
 int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* dist,
                 unsigned outputs, int32_t* out_comb, float* out_vals, double* out_vals64, unsigned* out_count,
-                int kernel);
+                int kernel, unsigned shard = 0, unsigned n_shards = 1);
 cudaError_t prepare_round_kernels(size_t smem);
 
 }  // namespace fiu

@@ -887,8 +887,8 @@ __device__ __forceinline__ int t2_chunk(int ii, int k, int x) {
 // cores and the single cores, the bounded single-precision prefilter, the exact
 // fixed-point key for survivors, warp-aggregated append (every lane calls it).
 __device__ __forceinline__ void t2_eval(const ScanWork& w, const CandSink& sink, float thr_f, uint32_t* dump,
-                                        const uint32_t* __restrict__ single, const uint32_t* ebuf, int ii, int k,
-                                        int i, int j, bool i_ok, const float (&si)[2][2], int lane) {
+                                        const uint4& sjp, const uint32_t* ebuf, int ii, int k, int i, int j,
+                                        bool i_ok, const float (&si)[2][2], int lane) {
     const DevData& d = w.d;
     const int n = d.snps;
     const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
@@ -904,8 +904,12 @@ __device__ __forceinline__ void t2_eval(const ScanWork& w, const CandSink& sink,
         t[1][x * 3 + 0] = u2f(c4.z);
         t[1][x * 3 + 1] = u2f(c4.w);
     }
-    uint4 sj4 = make_uint4(0, 0, 0, 0);
-    if (valid) sj4 = __ldg(reinterpret_cast<const uint4*>(single) + j);
+    // single cores of j = jg + k, loaded by lane k of the warp for the column group
+    uint4 sj4;
+    sj4.x = __shfl_sync(0xffffffffu, sjp.x, k);
+    sj4.y = __shfl_sync(0xffffffffu, sjp.y, k);
+    sj4.z = __shfl_sync(0xffffffffu, sjp.z, k);
+    sj4.w = __shfl_sync(0xffffffffu, sjp.w, k);
     const float sj[2][2] = {{u2f(sj4.x), u2f(sj4.y)}, {u2f(sj4.z), u2f(sj4.w)}};
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -1130,6 +1134,10 @@ __global__ void __launch_bounds__(kT2Threads, 1)
                     }
                     continue;
                 }
+                // the group's 8 single cores of j: lane t loads j = jg + (t & 7) before the
+                // accumulator reads, so that its latency overlaps them
+                const int jl = jg + (lane & 7);
+                const uint4 sjp = jl < n ? __ldg(reinterpret_cast<const uint4*>(single) + jl) : make_uint4(0, 0, 0, 0);
                 {
                     const uint32_t col = (uint32_t)((pack ? kT2N * buf : 0) + 32 * cc + 16 * hh);
                     uint32_t v[16], vt[16];
@@ -1174,7 +1182,7 @@ __global__ void __launch_bounds__(kT2Threads, 1)
 #pragma unroll 1
                 for (int kk = 0; kk < 4; ++kk) {
                     const int k = 4 * kh + kk;
-                    t2_eval(w, sink, thr_f, dump, single, ebuf, ii, k, i, jg + k, i_ok, si, lane);
+                    t2_eval(w, sink, thr_f, dump, sjp, ebuf, ii, k, i, jg + k, i_ok, si, lane);
                 }
                 __syncwarp();
             }

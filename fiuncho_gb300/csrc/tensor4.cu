@@ -65,9 +65,9 @@ constexpr int kT4Ebuf = 4096;                       // per epilogue warp: 32 com
 // with the pair (i, j) and singles i, j (the prefix star tables follow from
 // these in the epilogue).
 struct T4Item {
-    uint4 tijl[kT4L][2];
+    uint4 tijl[2][kT4L];  // [cases, controls][l]: 16-byte stride across the lanes' l
     uint4 pil[kT4L], pjl[kT4L], sl[kT4L];
-    uint4 tijk[kT4K][2];
+    uint4 tijk[2][kT4K];
     uint4 pik[kT4K], pjk[kT4K], sk[kT4K];
     uint4 pij, si, sj;
 };
@@ -122,26 +122,47 @@ __device__ __forceinline__ void t4_decode(const long long* __restrict__ begin, c
 // the row-wise writes (fixed ll) and the combination-wise reads (fixed xyz).
 __device__ __forceinline__ int t4_chunk(int kk, int ll, int xyz) { return (kk * 8 + ll) * 8 + (xyz ^ ll); }
 
+// The cores of one combination that depend on both k and l: triples (i,k,l)
+// and (j,k,l) (cases, controls) and pair (k,l), loaded from global memory at
+// the start of a column group so that their latency overlaps the
+// accumulator reads.
+struct T4KL {
+    uint4 ikl_c, ikl_t, jkl_c, jkl_t, kl;
+};
+
+__device__ __forceinline__ T4KL t4_load_kl(const uint4* __restrict__ pairs, const uint4* __restrict__ triples, int i,
+                                           int j, int k, int l, int n) {
+    const uint4* tik = triples + 2 * triple_index(i, k, l, n);
+    const uint4* tjk = triples + 2 * triple_index(j, k, l, n);
+    T4KL v;
+    v.ikl_c = __ldg(tik);
+    v.ikl_t = __ldg(tik + 1);
+    v.jkl_c = __ldg(tjk);
+    v.jkl_t = __ldg(tjk + 1);
+    v.kl = __ldg(pairs + pair_index(k, l, n));
+    return v;
+}
+
 // Estimate of the key minus the base in units of 2^-16 bits, cell by cell
 // over both classes in one packed derivation (the totals as their sum):
 // within t4_margin.  l-only and prefix sources come from the item's
-// shared-memory stage, (k, l) sources from global memory.
+// shared-memory stage, (k, l) sources from registers.
 __device__ __forceinline__ long long t4_estimate(const uint32_t (&cp)[2][8], const T4Item& it, int kk, int ll,
-                                                 const uint4* tik, const uint4* tjk, const uint4* pkl, uint32_t nn) {
+                                                 const T4KL& kl, uint32_t nn) {
     E4Both wd;
-    wd.tc[0] = it.tijl[ll][0];
-    wd.tt[0] = it.tijl[ll][1];
-    wd.tc[1] = __ldg(tik);
-    wd.tt[1] = __ldg(tik + 1);
-    wd.tc[2] = __ldg(tjk);
-    wd.tt[2] = __ldg(tjk + 1);
+    wd.tc[0] = it.tijl[0][ll];
+    wd.tt[0] = it.tijl[1][ll];
+    wd.tc[1] = kl.ikl_c;
+    wd.tt[1] = kl.ikl_t;
+    wd.tc[2] = kl.jkl_c;
+    wd.tt[2] = kl.jkl_t;
     wd.pil = it.pil[ll];
     wd.pjl = it.pjl[ll];
-    wd.pkl = __ldg(pkl);
+    wd.pkl = kl.kl;
     wd.sl = it.sl[ll];
     E4PrefixStarPacked ps;
-    ps.tc = it.tijk[kk][0];
-    ps.tt = it.tijk[kk][1];
+    ps.tc = it.tijk[0][kk];
+    ps.tt = it.tijk[1][kk];
     ps.pij = it.pij;
     ps.pik = it.pik[kk];
     ps.pjk = it.pjk[kk];
@@ -172,8 +193,8 @@ __device__ __forceinline__ void t4_stage(T4Item& it, long long g, int et, const 
         const int l = l0 + et;
         if (l < n) {
             const uint4* t = triples + 2 * triple_index(i, j, l, n);
-            t4_cp16(&it.tijl[et][0], t);
-            t4_cp16(&it.tijl[et][1], t + 1);
+            t4_cp16(&it.tijl[0][et], t);
+            t4_cp16(&it.tijl[1][et], t + 1);
             t4_cp16(&it.pil[et], pairs + pair_index(i, l, n));
             t4_cp16(&it.pjl[et], pairs + pair_index(j, l, n));
             t4_cp16(&it.sl[et], single4 + l);
@@ -182,8 +203,8 @@ __device__ __forceinline__ void t4_stage(T4Item& it, long long g, int et, const 
         const int kk = et - kT4L, k = k0 + kk;
         if (k < n) {
             const uint4* t = triples + 2 * triple_index(i, j, k, n);
-            t4_cp16(&it.tijk[kk][0], t);
-            t4_cp16(&it.tijk[kk][1], t + 1);
+            t4_cp16(&it.tijk[0][kk], t);
+            t4_cp16(&it.tijk[1][kk], t + 1);
             t4_cp16(&it.pik[kk], pairs + pair_index(i, k, n));
             t4_cp16(&it.pjk[kk], pairs + pair_index(j, k, n));
             t4_cp16(&it.sk[kk], single4 + k);
@@ -229,20 +250,17 @@ __device__ __noinline__ long long t4_exact(const ScanWork& w, const uint32_t (&c
 __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink, long long thr_q, uint32_t* dump,
                                         const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
                                         const uint4* __restrict__ triples, const T4Item& it,
-                                        const uint32_t (&cp)[2][8], int i, int j, int k0, int l0, int k, int l,
-                                        bool valid, int lane) {
+                                        const uint32_t (&cp)[2][8], const T4KL& kl, int i, int j, int k0, int l0,
+                                        int k, int l, bool valid, int lane) {
     const DevData& d = w.d;
     const int n = d.snps;
     long long key = w.base_key;
     bool pass = false;
     if (valid) {
-        const uint4* tik = triples + 2 * triple_index(i, k, l, n);
-        const uint4* tjk = triples + 2 * triple_index(j, k, l, n);
-        const uint4* pkl = pairs + pair_index(k, l, n);
         bool cand = dump != nullptr;
         if (!cand) {
             const int kk = k - k0, ll = l - l0;
-            const long long est = t4_estimate(cp, it, kk, ll, tik, tjk, pkl, d.n_cases | d.n_ctrls << 16);
+            const long long est = t4_estimate(cp, it, kk, ll, kl, d.n_cases | d.n_ctrls << 16);
             cand = est >= thr_q;
         }
         if (cand) {
@@ -509,6 +527,8 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     }
                     continue;
                 }
+                T4KL kl{};
+                if (valid && !dump) kl = t4_load_kl(pairs, triples, i, j, k, l, n);
                 {
                     const uint32_t col = (uint32_t)(kT4N * buf + 32 * cc + 16 * hh);
                     uint32_t v[16], vt[16];
@@ -545,7 +565,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     cp[1][r] = c4.z | (c4.w << 16);
                 }
                 __syncwarp();
-                t4_eval(w, sink, thr_q, dump, single, pairs, triples, it, cp, i, j, k0, l0, valid ? k : 2,
+                t4_eval(w, sink, thr_q, dump, single, pairs, triples, it, cp, kl, i, j, k0, l0, valid ? k : 2,
                         valid ? l : 3, valid, lane);
             }
         }

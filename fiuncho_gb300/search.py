@@ -209,6 +209,36 @@ class GpuSearch:
             return out, v64[: n.value].copy()
         return out
 
+    def run_shard(self, dataset, order: int, shard: int, n_shards: int, outputs: int, with_fp64: bool = False):
+        """Shard ``shard`` of ``n_shards`` of the whole search (fiu_search_shard): equal
+        ranges of the serving kernel's work units, so every shard keeps the
+        whole-data-set kernels.  Merging all shards' results by (MI descending,
+        combination ascending) gives the whole search's result."""
+        lib, ctx = self.ctx.lib, self.ctx
+        outputs = int(outputs)
+        comb = np.zeros(max(outputs, 1) * order, np.int32)
+        vals = np.zeros(max(outputs, 1), np.float32)
+        v64 = np.zeros(max(outputs, 1), np.float64)
+        n = C.c_uint(0)
+        if isinstance(dataset, Resident):
+            ctx.check(lib.fiu_search_shard_resident64(ctx.h, dataset.h, order, int(shard), int(n_shards), outputs,
+                                                      _lib.ptr(comb, C.c_int32), _lib.ptr(vals, C.c_float),
+                                                      _lib.ptr(v64, C.c_double), C.byref(n)))
+        else:
+            if with_fp64:
+                res = Resident(ctx, dataset)
+                try:
+                    return self.run_shard(res, order, shard, n_shards, outputs, with_fp64=True)
+                finally:
+                    res.free()
+            cds, keep = _c_dataset(dataset)
+            ctx.check(lib.fiu_search_shard(ctx.h, C.byref(cds), order, int(shard), int(n_shards), outputs,
+                                           _lib.ptr(comb, C.c_int32), _lib.ptr(vals, C.c_float), C.byref(n)))
+        out = _results(order, n.value, comb, vals)
+        if with_fp64:
+            return out, v64[: n.value].copy()
+        return out
+
     def run_batch(self, requests, use_graph: bool = True):
         """Many scans at once: requests = [(Resident, order, Distribution, outputs), ...].
         Returns [(results, fp64 values)] in request order; raises if any scan failed."""
@@ -376,9 +406,14 @@ class MPIEngine:
         ds = dataset if dataset is not None else Dataset.read(inputs)
         if ds.snps > 2 ** 31 - 1:
             raise FiunchoError(_lib.FIU_ERR_INVALID, "Input data limit exceeded: more than INT_MAX SNPs")
-        distribution = Distribution(ds.snps, order - 1, self.size, self.rank)
         search = search_cls(*args)
-        local = search.run(ds, order, distribution, outputs)
+        if hasattr(search, "run_shard"):
+            # the GPU search keeps the whole-data-set kernels: rank r searches
+            # shard r of the work units instead of the strided prefix set
+            # Distribution(snps, order-1, size, r); the gathered result is the same
+            local = search.run_shard(ds, order, self.rank, self.size, outputs)
+        else:
+            local = search.run(ds, order, Distribution(ds.snps, order - 1, self.size, self.rank), outputs)
         return self.gather(local, outputs)
 
     def gather(self, local, outputs):

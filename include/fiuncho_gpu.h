@@ -134,6 +134,19 @@ int fiu_search_resident(fiu_ctx *ctx, const fiu_resident *res, unsigned order,
 int fiu_search_resident64(fiu_ctx *ctx, const fiu_resident *res, unsigned order,
                           const fiu_distribution *distribution, unsigned outputs, int32_t *out_combinations,
                           float *out_vals, double *out_vals64, unsigned *out_count);
+/* One shard of the whole search (Distribution(snps, order-1, 1, 0)): shard
+ * `shard` of `n_shards` contiguous, equal ranges of the work units of the
+ * kernel that serves the whole data set (tensor-core work items, pair-major
+ * items, or prefix ordinals).  The shards cover every combination exactly
+ * once, so each GPU of a multi-GPU search keeps the whole-data-set kernels
+ * (where MPIEngine.h:133-174 gives rank r the strided Distribution(snps,
+ * order-1, N, r)); merging the shards' results by (MI descending,
+ * combination ascending) and truncating gives the whole search's result. */
+int fiu_search_shard(fiu_ctx *ctx, const fiu_dataset *dataset, unsigned order, unsigned shard, unsigned n_shards,
+                     unsigned outputs, int32_t *out_combinations, float *out_vals, unsigned *out_count);
+int fiu_search_shard_resident64(fiu_ctx *ctx, const fiu_resident *res, unsigned order, unsigned shard,
+                                unsigned n_shards, unsigned outputs, int32_t *out_combinations, float *out_vals,
+                                double *out_vals64, unsigned *out_count);
 
 /* ---- many scans at once (batched form) ---------------------------------------
  * Each scan is a search of its own resident data set with its own order,

@@ -200,6 +200,30 @@ def test_rank_split_merges_to_full_run(gs, golden_synth):
     assert [r.combination for r in merged] == [r.combination for r in full]
 
 
+@pytest.mark.parametrize("order,n_shards", [(2, 3), (3, 2), (3, 7), (4, 3)])
+def test_shards_merge_to_full_run(gs, golden_synth, order, n_shards):
+    """The shards of the whole search (equal ranges of the serving kernel's work units)
+    merged by (MI descending, combination ascending) == one full run, results and FP64
+    values; each shard keeps the whole-data-set kernel."""
+    from fiuncho_gb300 import Dataset, Distribution, FiunchoError, MPIEngine
+    ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
+    full, v_full = gs.run(ds, order, Distribution(ds.snps, order - 1), 40, with_fp64=True)
+    kernel = gs.last_tile()[0]
+    parts = []
+    for sh in range(n_shards):
+        r, v = gs.run_shard(ds, order, sh, n_shards, 40, with_fp64=True)
+        assert gs.last_tile()[0] == kernel
+        parts += [(-float(x), tuple(c.combination), float(x)) for c, x in zip(r, v)]
+    parts.sort()
+    assert [list(p[1]) for p in parts[:40]] == [r.combination for r in full]
+    assert np.array_equal(np.array([p[2] for p in parts[:40]]), v_full)
+    # MPIEngine's gather of the shards' Result lists gives the same combinations
+    lists = sum((gs.run_shard(ds, order, sh, n_shards, 40) for sh in range(n_shards)), [])
+    assert [r.combination for r in MPIEngine().gather(lists, 40)] == [r.combination for r in full]
+    with pytest.raises(FiunchoError):
+        gs.run_shard(ds, order, n_shards, n_shards, 40)
+
+
 # --------------------------------------------------------------- edge cases
 def test_edge_cases(gs, oracle):
     from fiuncho_gb300 import Dataset, Distribution, FiunchoError
