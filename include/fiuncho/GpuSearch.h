@@ -16,6 +16,15 @@
  *
  * Errors are reported as std::runtime_error, like the reference.  There is no
  * CPU fallback: without a usable GPU the constructor throws.
+ *
+ * Multi-GPU: MPIEngine gives rank r of N the strided prefix share
+ * Distribution(snps, order-1, N, r), which the whole-data-set tensor-core
+ * kernels cannot serve.  With shard_ranks = true such a rank share runs as
+ * shard r of N of the whole search instead (fiu_search_shard: equal ranges of
+ * the tensor-core work units); the rank's own list then differs from the
+ * strided share's, but MPIEngine's gathered result is the same:
+ *
+ *     engine.run<GpuSearch>({tped, tfam}, order, outputs, local_rank, true);
  */
 #ifndef FIUNCHO_GPUSEARCH_H
 #define FIUNCHO_GPUSEARCH_H
@@ -32,12 +41,15 @@
 class GpuSearch : public Search
 {
     fiu_ctx *ctx = nullptr;
+    bool shard_ranks = false;
 
   public:
     /**
      * @param device CUDA device ordinal used by this search object
+     * @param shard_ranks run a rank share Distribution(snps, order-1, N, r) as
+     * shard r of N of the whole search (see above)
      */
-    explicit GpuSearch(int device = 0)
+    explicit GpuSearch(int device = 0, bool shard_ranks = false) : shard_ranks(shard_ranks)
     {
         if (fiu_create(device, &ctx) != FIU_OK) {
             throw std::runtime_error("GpuSearch: cannot create a context on CUDA device " +
@@ -81,7 +93,14 @@ class GpuSearch : public Search
         std::vector<int32_t> comb((size_t)outputs * order);
         std::vector<float> vals(outputs);
         unsigned count = 0;
-        if (fiu_search(ctx, &d, order, &dist, outputs, comb.data(), vals.data(), &count) != FIU_OK) {
+        const bool rank_share = shard_ranks && distribution.n == (int)dataset.snps && distribution.k == order - 1 &&
+                                distribution.step >= 1 && distribution.offset >= 0 &&
+                                distribution.offset < distribution.step;
+        const int rc = rank_share ? fiu_search_shard(ctx, &d, order, (unsigned)distribution.offset,
+                                                     (unsigned)distribution.step, outputs, comb.data(), vals.data(),
+                                                     &count)
+                                  : fiu_search(ctx, &d, order, &dist, outputs, comb.data(), vals.data(), &count);
+        if (rc != FIU_OK) {
             throw std::runtime_error(std::string("GpuSearch::run: ") + fiu_last_error(ctx));
         }
         results.resize(count);

@@ -8,6 +8,7 @@
 #include <fiuncho/GpuSearch.h>
 #include <fiuncho/MPIEngine.h>
 
+#include <algorithm>
 #include <cmath>
 #include <fstream>
 #include <iostream>
@@ -83,6 +84,27 @@ int main(int argc, char **argv)
         auto r = engine.run<GpuSearch>({argv[1]}, o, 90, 0);
         common_checks(r, o, "MPIEngine order " + std::to_string(o));
         if (o == 3) CHECK(matches_mpi3snp(r, argv[2]), "MPIEngine order 3 vs MPI3SNP");
+    }
+    // shard mode: the rank shares of 3 ranks run as shards of the whole search;
+    // merged (value descending, combination ascending) they give the whole result
+    GpuSearch sharded(0, true);
+    for (int o = 2; o < 5; ++o) {
+        Distribution<int> whole((int)dataset.snps, o - 1, 1, 0);
+        auto ref = search.run(dataset, o, whole, 90);
+        std::vector<Result<int, float>> merged;
+        for (int r = 0; r < 3; ++r) {
+            Distribution<int> share((int)dataset.snps, o - 1, 3, r);
+            auto part = sharded.run(dataset, o, share, 90);
+            merged.insert(merged.end(), part.begin(), part.end());
+        }
+        std::sort(merged.begin(), merged.end(), [](const Result<int, float> &a, const Result<int, float> &b) {
+            return a.val != b.val ? a.val > b.val : a.combination < b.combination;
+        });
+        if (merged.size() > ref.size()) merged.resize(ref.size());
+        std::map<std::vector<int>, float> want, got;
+        for (const auto &x : ref) want[x.combination] = x.val;
+        for (const auto &x : merged) got[x.combination] = x.val;
+        CHECK(want == got, "sharded rank shares merge to the whole result, order " + std::to_string(o));
     }
     bool threw = false;
     try {
