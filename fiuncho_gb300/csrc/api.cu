@@ -390,7 +390,10 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
             have = M;
         }
         m = m1;
-        if (fresh < cap / 8) chunk *= 4;
+        // grow fast while a chunk admits few candidates: every chunk costs a
+        // launch and a host round trip, which dominate small scans
+        if (fresh < cap / 64) chunk *= 16;
+        else if (fresh < cap / 8) chunk *= 4;
         else if (fresh > cap / 2) chunk = std::max<long long>(1, chunk / 2);
     }
     if (tensor) {
