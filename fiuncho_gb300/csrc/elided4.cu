@@ -251,9 +251,8 @@ __global__ void __launch_bounds__(kEThreads, 2)
                 pre.pjk = pairs + pair_index(j, k, S);
                 pre.sk = single4 + k;
                 uint32_t* o = dump ? dump + ((size_t)triple_index(i, j, k, S) * S + l) * 2 * 81 : nullptr;
-                key += e4p_pass<0>(cp, src, pre, d.ftab, d.n_cases, o);
-                key += e4p_pass<1>(cp, src, pre, d.ftab, d.n_ctrls, o);
-                key -= e4p_pass<2>(cp, src, pre, d.ftab, d.n_cases + d.n_ctrls, o);
+                key += e4_exact_packed(cp, e4_load_both(src), e4_prefix_packed(pre, d.n_cases, d.n_ctrls), d.ftab,
+                                       d.n_cases, d.n_ctrls, o);
             }
             if (sink.evaluated) {
                 const unsigned vm = __ballot_sync(0xffffffffu, valid);

@@ -31,8 +31,8 @@ __host__ __device__ __forceinline__ long long triple_index(int i, int j, int k, 
 }
 
 // Shared-memory words of one group: 8 prefix rows of cw + tw words, then the
-// prefix triple's full table for cases, controls and totals (81 uint32).
-__host__ __device__ inline size_t elided4_words(int cw, int tw) { return 8 * (size_t)(cw + tw) + 41; }
+// prefix triple's packed star table (27 uint32: cases | controls << 16).
+__host__ __device__ inline size_t elided4_words(int cw, int tw) { return 8 * (size_t)(cw + tw) + 14; }
 
 // The star table of three SNPs holds at (a, b, c), a, b, c in {0, 1, 2}
 // ((a*3+b)*3+c; 2 = any genotype), the core count of the SNPs not at "any".
@@ -319,6 +319,66 @@ struct E4PrefixStarPacked {
     }
 };
 
+// Both classes' words of one combination, loaded from their locations.
+__device__ __forceinline__ E4Both e4_load_both(const E4Src& src) {
+    E4Both wd;
+    const uint4* tp[3] = {src.tij, src.tik, src.tjk};
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+        wd.tc[u] = __ldg(tp[u]);
+        wd.tt[u] = __ldg(tp[u] + 1);
+    }
+    wd.pil = __ldg(src.pil);
+    wd.pjl = __ldg(src.pjl);
+    wd.pkl = __ldg(src.pkl);
+    wd.sl = __ldg(src.sl);
+    return wd;
+}
+
+// The packed star table of a prefix triple from its cores' locations.
+__device__ __forceinline__ E4PrefixStarPacked e4_prefix_packed(const E4Prefix& pre, uint32_t n0, uint32_t n1) {
+    E4PrefixStarPacked ps;
+    ps.tc = __ldg(pre.tijk);
+    ps.tt = __ldg(pre.tijk + 1);
+    ps.pij = __ldg(pre.pij);
+    ps.pik = __ldg(pre.pik);
+    ps.pjk = __ldg(pre.pjk);
+    ps.si = __ldg(pre.si);
+    ps.sj = __ldg(pre.sj);
+    ps.sk = __ldg(pre.sk);
+    ps.nn = n0 | n1 << 16;
+    return ps;
+}
+
+// The exact key of one combination (minus the base) from one packed
+// derivation of both classes: the sum over the 81 cells of
+// T[a] + T[b] - T[a + b] (a cases, b controls; each clamped to its class
+// size, so that an inconsistent input stays inside the table).  Equal to the
+// three passes e4_pass<0> + e4_pass<1> - e4_pass<2> on consistent one-hot
+// data; writes the tables to o (cases at o[q*3+sw], controls at
+// o[81+q*3+sw]) if o.
+template <class PS>
+__device__ __forceinline__ long long e4_exact_packed(const uint32_t (&cp)[2][8], const E4Both& wd, const PS& ps,
+                                                     const long long* __restrict__ ftab, uint32_t n0, uint32_t n1,
+                                                     uint32_t* o) {
+    long long part = 0;
+    e4_slices_packed(cp, wd, ps, [&](int sw, const uint32_t* t) {
+#pragma unroll
+        for (int q = 0; q < 27; ++q) {
+            const uint32_t a = min(t[q] & 0xffffu, n0), b = min(t[q] >> 16, n1);
+            part += __ldg(ftab + a) + __ldg(ftab + b) - __ldg(ftab + a + b);
+        }
+        if (o) {
+#pragma unroll
+            for (int q = 0; q < 27; ++q) {
+                o[q * 3 + sw] = t[q] & 0xffffu;
+                o[81 + q * 3 + sw] = t[q] >> 16;
+            }
+        }
+    });
+    return part;
+}
+
 // Exact pass with the prefix star table computed from the prefix's cores.
 template <int PC>
 __device__ __forceinline__ long long e4p_pass(const uint32_t (&cp)[2][8], const E4Src& src, const E4Prefix& pre,
@@ -371,31 +431,18 @@ __device__ __forceinline__ void elided4_prefix(const ScanWork& w, long long m, c
                 __ldg(d.ref + (size_t)c[1] * per_snp + off + (size_t)((r >> 1) & 1) * W) &
                 __ldg(d.ref + (size_t)c[2] * per_snp + off + (size_t)(r & 1) * W);
     }
-    if (gt == 0) {  // star table of the prefix triple, per pass
-        const long long ti = triple_index(c[0], c[1], c[2], S);
-        const uint4 tc[2] = {__ldg(triples + 2 * ti), __ldg(triples + 2 * ti + 1)};
-        const uint4 p01 = __ldg(pairs + pair_index(c[0], c[1], S)), p02 = __ldg(pairs + pair_index(c[0], c[2], S)),
-                    p12 = __ldg(pairs + pair_index(c[1], c[2], S));
-        const uint4 sv[3] = {__ldg(single4 + c[0]), __ldg(single4 + c[1]), __ldg(single4 + c[2])};
-        const uint32_t ncls[2] = {(uint32_t)d.n_cases, (uint32_t)d.n_ctrls};
+    if (gt == 0) {  // packed star table of the prefix triple
+        E4Prefix pre;
+        pre.tijk = triples + 2 * triple_index(c[0], c[1], c[2], S);
+        pre.pij = pairs + pair_index(c[0], c[1], S);
+        pre.pik = pairs + pair_index(c[0], c[2], S);
+        pre.pjk = pairs + pair_index(c[1], c[2], S);
+        pre.si = single4 + c[0];
+        pre.sj = single4 + c[1];
+        pre.sk = single4 + c[2];
+        const E4PrefixStarPacked st = e4_prefix_packed(pre, d.n_cases, d.n_ctrls);
 #pragma unroll
-        for (int cls = 0; cls < 2; ++cls)
-#pragma unroll
-            for (int q = 0; q < 27; ++q) {
-                const int a = q / 9, b = (q / 3) % 3, z = q % 3;
-                uint32_t v;
-                if (a < 2 && b < 2 && z < 2) v = tcell(tc[cls], a, b, z);
-                else if (a < 2 && b < 2) v = pcore(p01, cls, a, b);
-                else if (a < 2 && z < 2) v = pcore(p02, cls, a, z);
-                else if (b < 2 && z < 2) v = pcore(p12, cls, b, z);
-                else if (a < 2) v = (&sv[0].x)[cls * 2 + a];
-                else if (b < 2) v = (&sv[1].x)[cls * 2 + b];
-                else if (z < 2) v = (&sv[2].x)[cls * 2 + z];
-                else v = ncls[cls];
-                ptab[27 * cls + q] = v;
-            }
-#pragma unroll 1
-        for (int q = 0; q < 27; ++q) ptab[54 + q] = ptab[q] + ptab[27 + q];
+        for (int q = 0; q < 27; ++q) ptab[q] = st(q);
     }
     group_sync<TP>(grp);
 
@@ -456,9 +503,8 @@ __device__ __forceinline__ void elided4_prefix(const ScanWork& w, long long m, c
             src.sl = single4 + l;
             uint32_t* o = dump ? dump + ((size_t)m * S + l) * 2 * 81 : nullptr;
             // key = base + sum over the 81 cells of T[case] + T[control] - T[total]
-            key += e4_pass<0>(cp, src, [&](int q) { return ptab[q]; }, d.ftab, d.n_cases, o);
-            key += e4_pass<1>(cp, src, [&](int q) { return ptab[27 + q]; }, d.ftab, d.n_ctrls, o);
-            key -= e4_pass<2>(cp, src, [&](int q) { return ptab[54 + q]; }, d.ftab, d.n_cases + d.n_ctrls, o);
+            key += e4_exact_packed(cp, e4_load_both(src), [&](int q) { return ptab[q]; }, d.ftab, d.n_cases,
+                                   d.n_ctrls, o);
         }
         const bool pass = valid && key >= sink.thr;
         const unsigned mask = __ballot_sync(0xffffffffu, pass);
