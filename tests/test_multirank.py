@@ -30,13 +30,32 @@ class OracleSearch:
         return [Result(list(map(int, cc)), float(x)) for cc, x in zip(c, v64)]
 
 
+class ShardedOracleSearch(OracleSearch):
+    """A search with run_shard (as GpuSearch has): MPIEngine then gives rank r
+    shard r of N instead of the strided Distribution.  The oracle's shard r is
+    a contiguous range of the prefix ordinals (the whole search's work units
+    split in N equal ranges), searched prefix by prefix."""
+
+    def run_shard(self, ds, order, shard, n_shards, outputs):
+        from fiuncho_gb300 import Distribution, Result
+        import math
+        units = math.comb(ds.snps, order - 1)
+        lo = units // n_shards * shard + min(shard, units % n_shards)
+        hi = lo + units // n_shards + (1 if shard < units % n_shards else 0)
+        res = []
+        for m in range(lo, hi):
+            res += self.run(ds, order, Distribution(ds.snps, order - 1, units, m), outputs)
+        res.sort(key=lambda r: (-r.val, r.combination))
+        return [Result(r.combination, r.val) for r in res[:outputs]]
+
+
 def _free_port():
     with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
         s.bind(("127.0.0.1", 0))
         return s.getsockname()[1]
 
 
-def _rank_main(rank, world, port, data_path, out_path):
+def _rank_main(rank, world, port, data_path, out_path, sharded=False):
     import sys
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
@@ -49,13 +68,16 @@ def _rank_main(rank, world, port, data_path, out_path):
     try:
         z = np.load(data_path)
         ds = Dataset.from_genotypes(z["geno"], z["is_case"])
-        res = MPIEngine().run(OracleSearch, None, 3, 25, dataset=ds)
+        res = MPIEngine().run(ShardedOracleSearch if sharded else OracleSearch, None, 3, 25, dataset=ds)
         np.save(out_path % rank, np.array([r.combination + [r.val] for r in res], np.float64).reshape(-1, 4))
     finally:
         dist.destroy_process_group()
 
 
-def test_two_rank_gather_equals_single_rank(tmp_path):
+@pytest.mark.parametrize("sharded", [False, True])
+def test_two_rank_gather_equals_single_rank(tmp_path, sharded):
+    """Strided Distribution shares, or (a search with run_shard, as GpuSearch) shards
+    of the whole search: either way rank 0's gathered result is the whole search's."""
     import multiprocessing as mp
 
     from fiuncho_gb300 import Dataset, Distribution
@@ -70,7 +92,7 @@ def test_two_rank_gather_equals_single_rank(tmp_path):
     out_path = str(tmp_path / "rank%d.npy")
     port = _free_port()
     ctx = mp.get_context("spawn")
-    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, data_path, out_path)) for r in range(2)]
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, data_path, out_path, sharded)) for r in range(2)]
     for p in procs:
         p.start()
     for p in procs:
