@@ -837,10 +837,14 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
         e = launch_kernel(kernel, tp, res, w, 0, w.n_prefixes, sink, d, s, ctx->sms);
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, need * 4, cudaMemcpyDeviceToHost, s);
+    int t_status = 0;  // a tensor kernel that gave up on a wait leaves incomplete tables: report it
+    if (e == cudaSuccess && kernel == FIU_KERNEL_TENSOR)
+        e = cudaMemcpyAsync(&t_status, ctx->ctl + 16, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(d, s);
     cudaError_t e2 = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "scan tables");
+    if (t_status) return fail(ctx, FIU_ERR_TIMEOUT, "tensor kernel: a tensor-memory wait ran past its limit");
     return FIU_OK;
 }
 
