@@ -75,6 +75,7 @@ _SIGS = {
     "fiu_kernel_timing": (C.c_int, [_vp, _f64p, _u64p, _u64p]),
     "fiu_probe_popc_rate": (C.c_int, [_vp, _f64p]),
     "fiu_probe_lg2_error": (C.c_int, [_vp, C.c_uint, _f64p]),
+    "fiu_probe_wait_limit": (C.c_int, [_vp, C.c_uint, C.c_int, C.POINTER(C.c_int), _f64p]),
     "fiu_dataset_upload": (C.c_int, [_vp, C.POINTER(Dataset_t), C.POINTER(_vp)]),
     "fiu_dataset_free": (None, [_vp, _vp]),
     "fiu_dataset_is_one_hot": (C.c_int, [_vp]),

@@ -548,6 +548,14 @@ int fiu_probe_lg2_error(fiu_ctx* ctx, unsigned max_c, double* max_abs_err) {
     return FIU_OK;
 }
 
+int fiu_probe_wait_limit(fiu_ctx* ctx, unsigned limit_us, int arrive, int* completed, double* elapsed_ms) {
+    if (!ctx || !completed || !elapsed_ms || limit_us > 1000000) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(probe_wait_limit(limit_us, arrive, completed, elapsed_ms, ctx->stream), "wait probe");
+    return FIU_OK;
+}
+
 int fiu_dataset_upload(fiu_ctx* ctx, const fiu_dataset* h, fiu_resident** out) {
     if (!ctx || !out) return FIU_ERR_INVALID;
     Scope scope(ctx);

@@ -202,6 +202,7 @@ cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l256, const
                            const uint4* triples, int* status, cudaStream_t s, int sms);
 // Largest absolute error of the kernel's single-precision log2 over all its inputs (counts <= max_c).
 cudaError_t probe_lg2_error(unsigned max_c, double* max_abs_err, cudaStream_t s);
+cudaError_t probe_wait_limit(unsigned limit_us, int arrive, int* completed, double* elapsed_ms, cudaStream_t s);
 
 // layout.cu -- device layouts of a data set.
 cudaError_t launch_transpose(const uint64_t* ref, uint64_t* tr, int snps, int rows, cudaStream_t s);

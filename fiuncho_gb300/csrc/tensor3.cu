@@ -1379,6 +1379,48 @@ static double t3_margin(int n_samples) {
     return 2 * err + 1e-3;
 }
 
+// Self-check of the bounded mbarrier wait the tensor kernels use: one thread
+// initialises an mbarrier (one arrival expected), arrives on it first when
+// `arrive` is set, then waits for phase 0 with the given limit in the same
+// try-wait loop as t3_wait.  Without the arrival nothing completes the phase
+// and the wait must give up after the limit; out[0] = 1 if it completed,
+// out[1] = elapsed ns.
+__global__ void t3_wait_probe_kernel(unsigned long long limit_ns, int arrive, unsigned long long* out) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (arrive) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
+    const unsigned long long t0 = t3_now();
+    bool done = false;
+    for (;;) {
+        if (t3_try(smem_u32(&bar), 0)) {
+            done = true;
+            break;
+        }
+        if (t3_now() - t0 > limit_ns) break;
+    }
+    out[0] = done ? 1 : 0;
+    out[1] = t3_now() - t0;
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bar)) : "memory");
+}
+
+cudaError_t probe_wait_limit(unsigned limit_us, int arrive, int* completed, double* elapsed_ms, cudaStream_t s) {
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    unsigned long long h[2] = {0, 0};
+    t3_wait_probe_kernel<<<1, 32, 0, s>>>((unsigned long long)limit_us * 1000ull, arrive, d);
+    count_launch();
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    *completed = (int)h[0];
+    *elapsed_ms = (double)h[1] / 1e6;
+    return e;
+}
+
 // Every input of t3_lg2 in the kernel is x = (float)(c + 2^-20) for an integer
 // count c in [0, max_c]; largest |t3_lg2(x) - log2(x)| over them, log2 in FP64.
 __global__ void t3_lg2_probe_kernel(unsigned max_c, unsigned long long* worst_bits) {

@@ -97,6 +97,14 @@ int fiu_probe_popc_rate(fiu_ctx *ctx, double *word_ops_per_s);
  * every input it can see (x = c + 2^-20 rounded to float, integer counts c in
  * [0, max_c]).  The prefilter's error bound assumes it stays below 2^-18. */
 int fiu_probe_lg2_error(fiu_ctx *ctx, unsigned max_c, double *max_abs_err);
+/* Self-check of the bounded device waits (the failure detection of the
+ * tensor kernels, which report FIU_ERR_TIMEOUT when a wait runs out): a
+ * one-thread kernel waits, with a limit of limit_us (at most 1 s), on an
+ * mbarrier phase that nothing completes -- or, with arrive != 0, that the
+ * thread completes itself first.  *completed = 1 if the phase completed,
+ * 0 if the wait gave up; *elapsed_ms = time spent waiting.  No GPU fault
+ * and no hang either way: the wait always ends. */
+int fiu_probe_wait_limit(fiu_ctx *ctx, unsigned limit_us, int arrive, int *completed, double *elapsed_ms);
 
 /* Forces a counting kernel for this context's searches (FIU_KERNEL_*);
  * FIU_KERNEL_AUTO restores the automatic choice.  A kernel that cannot serve a

@@ -507,6 +507,22 @@ def test_lg2_prefilter_bound(gs):
     assert 0 <= err.value < 2.0 ** -18, err.value
 
 
+def test_bounded_wait_gives_up(gs):
+    """Failure detection without a fault: a device wait on an mbarrier phase that
+    nothing completes gives up after its limit (the tensor kernels then report
+    FIU_ERR_TIMEOUT) and the context stays usable; with the arrival it completes
+    at once."""
+    import ctypes as C
+    done, ms = C.c_int(-1), C.c_double(-1)
+    gs.ctx.check(gs.ctx.lib.fiu_probe_wait_limit(gs.ctx.h, 20000, 0, C.byref(done), C.byref(ms)))
+    assert done.value == 0 and 20.0 <= ms.value < 1000.0, (done.value, ms.value)
+    gs.ctx.check(gs.ctx.lib.fiu_probe_wait_limit(gs.ctx.h, 20000, 1, C.byref(done), C.byref(ms)))
+    assert done.value == 1 and ms.value < 20.0, (done.value, ms.value)
+    from fiuncho_gb300 import Dataset, Distribution
+    ds = _one_hot_dataset(3, 30, 200, 200)  # the context still searches
+    assert len(gs.run(ds, 3, Distribution(30, 2), 5)) == 5
+
+
 def _one_hot_dataset(seed, snps, n_case, n_ctrl):
     from fiuncho_gb300 import Dataset
     rng = np.random.default_rng(seed)
