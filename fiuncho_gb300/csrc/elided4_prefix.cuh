@@ -387,22 +387,6 @@ __device__ __forceinline__ long long e4p_pass(const uint32_t (&cp)[2][8], const 
     return e4_pass<PC>(cp, src, ps, ftab, nc, o);
 }
 
-// One slice's contribution to the key estimate, in units of 2^-16 bits: the
-// single-precision sum of c*lg2(c) over its 27 cells (counts < 2^23 are exact
-// floats), rounded to 2^-16.  lg2.approx is the hardware base-2 logarithm.
-__device__ __forceinline__ long long e4_slice_estimate(const uint32_t* t, uint32_t nc) {
-    const float tiny = 9.5367431640625e-07f;  // 2^-20: c*lg2(c + tiny) = 0 at c = 0
-    float f[27];
-#pragma unroll
-    for (int q = 0; q < 27; ++q) {
-        const float c = __uint_as_float(0x4B000000u | min(t[q], nc)) - 8388608.0f;
-        float l2;
-        asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l2) : "f"(c + tiny));
-        f[q] = c * l2;
-    }
-    return __float2ll_rn(e4_sum27(f) * 65536.0f);
-}
-
 // One prefix (owned ordinal m): the TP threads of group grp, one last SNP per
 // thread; sp holds elided4_words(cw, tw) words.  Synchronises the group only.
 template <bool HS, int TP>
