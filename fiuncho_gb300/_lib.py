@@ -104,6 +104,7 @@ _SIGS = {
     "fiu_server_destroy": (None, [_vp]),
     "fiu_tables": (C.c_int, [_vp, _vp, C.c_uint, _i32p, C.c_size_t, _u32p, _u32p]),
     "fiu_scan_tables": (C.c_int, [_vp, _vp, C.c_uint, C.POINTER(Distribution_t), C.c_int, _u32p, C.c_size_t]),
+    "fiu_scan_digest": (C.c_int, [_vp, _vp, C.c_uint, C.POINTER(Distribution_t), C.c_int, _u64p, _u64p]),
 }
 
 _lib = None

@@ -11,6 +11,7 @@
 
 #include "../../include/fiuncho_gpu.h"
 #include "ctx.h"
+#include "digest.cuh"
 
 namespace fiu {
 thread_local unsigned long long* g_launch_counter = nullptr;
@@ -853,6 +854,67 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
     if (e == cudaSuccess) e = e2;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "scan tables");
     if (t_status) return fail(ctx, FIU_ERR_TIMEOUT, "tensor kernel: a tensor-memory wait ran past its limit");
+    return FIU_OK;
+}
+
+int fiu_scan_digest(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu_distribution* distribution,
+                    int kernel, uint64_t* digest, uint64_t* combinations) {
+    if (!ctx) return FIU_ERR_INVALID;
+    Scope scope(ctx);
+    if (!digest || !combinations) return fail(ctx, FIU_ERR_INVALID, "null output pointer");
+    *digest = 0;
+    *combinations = 0;
+    ScanWork w;
+    int rc = make_work(ctx, res, order, distribution, 1, w);
+    if (rc) return rc;
+    if (w.n_prefixes == 0) return FIU_OK;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    int tp = 256;
+    if ((rc = choose_tile(ctx, res, w, kernel ? kernel : ctx->kernel, kernel, tp, true))) return rc;
+    if (kernel == FIU_KERNEL_FULL && order > 4)
+        return fail(ctx, FIU_ERR_UNSUPPORTED, "the full-table kernel's digest covers orders 2-4");
+    const bool tensor = kernel == FIU_KERNEL_TENSOR;
+    const bool pair_major = e4_pair_major(kernel, res, w);
+    const long long units = tensor ? tensor_units(*res->t3, (int)order) : pair_major ? res->e4_items : w.n_prefixes;
+    // order-4 and full-table kernels assemble each table in a per-thread row
+    // (2 x 81 words) of scratch: room for every thread the launch can hold
+    const bool scratch = order == 4 || kernel == FIU_KERNEL_FULL;
+    const unsigned threads = scratch ? (unsigned)ctx->sms * 2048u : 0u;
+    cudaStream_t s = ctx->stream;
+    unsigned long long* d = nullptr;  // kDigestSlots sums, then the combination counter
+    uint32_t* sc = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d, (kDigestSlots + 1) * sizeof(unsigned long long), s);
+    if (e == cudaSuccess && scratch) e = cudaMallocAsync((void**)&sc, (size_t)threads * 2 * 81 * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, (kDigestSlots + 1) * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ctl, 0, 2 * sizeof(unsigned), s);
+    int* t_status = (int*)(ctx->ctl + 16);
+    if (e == cudaSuccess && tensor) e = cudaMemsetAsync(t_status, 0, sizeof(int), s);
+    CandSink sink{ctx->cand, ctx->ctl, ctx->ctl + 1, 0, (long long)0x7fffffffffffffffll, d + kDigestSlots,
+                  d, sc, threads};
+    if (e == cudaSuccess) {
+        if (tensor)
+            e = launch_tensor3(w, *res->t3, 0, units, sink, nullptr, res->single, res->pairs, res->triples, t_status, s,
+                               ctx->sms);
+        else if (pair_major)
+            e = launch_elided4p(w, res->e4_begin, 0, units, sink, nullptr, res->single, res->pairs, res->triples, s,
+                                ctx->sms);
+        else
+            e = launch_kernel(kernel, tp, res, w, 0, units, sink, nullptr, s, ctx->sms);
+    }
+    std::vector<unsigned long long> h(kDigestSlots + 1, 0);
+    int st = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && tensor) e = cudaMemcpyAsync(&st, t_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (sc) cudaFreeAsync(sc, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scan digest");
+    if (st) return fail(ctx, FIU_ERR_TIMEOUT, "tensor kernel: a tensor-memory wait ran past its limit");
+    unsigned long long sum = 0;
+    for (int i = 0; i < kDigestSlots; ++i) sum += h[i];
+    *digest = sum;
+    *combinations = h[kDigestSlots];
     return FIU_OK;
 }
 

@@ -151,6 +151,9 @@ std::vector<long long> e4p_item_begin(int snps) {
 
 size_t e4p_smem(int cw, int tw) { return (size_t)(kEThreads / 32) * 4 * (cw + tw) * sizeof(uint64_t); }
 
+// DIGEST: the digest mode of fiu_scan_digest, compiled separately (the search's
+// instantiation carries none of its code).
+template <bool DIGEST>
 __global__ void __launch_bounds__(kEThreads, 2)
     count_elided4p(ScanWork w, const long long* __restrict__ begin, long long g0, long long g1, CandSink sink,
                    uint32_t* dump, const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
@@ -208,6 +211,7 @@ __global__ void __launch_bounds__(kEThreads, 2)
             const int b = valid ? (int)(t - (long long)a * (2 * mm - a - 1) / 2) + a + 1 : 1;
             const int k = j + 1 + a, l = j + 1 + b;
             long long key = w.base_key;
+            unsigned long long dg = 0;
             if (valid) {
                 uint32_t cnt[2][16];
 #pragma unroll
@@ -251,9 +255,16 @@ __global__ void __launch_bounds__(kEThreads, 2)
                 pre.pjk = pairs + pair_index(j, k, S);
                 pre.sk = single4 + k;
                 uint32_t* o = dump ? dump + ((size_t)triple_index(i, j, k, S) * S + l) * 2 * 81 : nullptr;
+                const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+                if (DIGEST && gtid < sink.dscratch_threads) o = sink.dscratch + (size_t)gtid * 2 * 81;
                 key += e4_exact_packed(cp, e4_load_both(src), e4_prefix_packed(pre, d.n_cases, d.n_ctrls), d.ftab,
                                        d.n_cases, d.n_ctrls, o);
+                if (DIGEST && o) {
+                    const int cmb[4] = {i, j, k, l};
+                    dg = dg_table(cmb, 4, S, o, 81);
+                }
             }
+            if (DIGEST) dg_warp_add(sink.digest, dg);
             if (sink.evaluated) {
                 const unsigned vm = __ballot_sync(0xffffffffu, valid);
                 if (lane == 0) atomicAdd(sink.evaluated, (unsigned long long)__popc(vm));
@@ -285,15 +296,17 @@ cudaError_t launch_elided4p(const ScanWork& w, const long long* begin, long long
     if (w.order != 4 || !begin || !single || !pairs || !triples) return cudaErrorInvalidValue;
     const size_t smem = e4p_smem(w.d.cw, w.d.tw);
     if (smem > kMaxGroupSmem) return cudaErrorInvalidConfiguration;
-    static LaunchCache cache;
+    static LaunchCache cache[2];
+    const bool dg = sink.digest != nullptr;
+    auto fn = dg ? count_elided4p<true> : count_elided4p<false>;
     int per_sm = 1;
-    const cudaError_t e = blocks_per_sm(cache, count_elided4p, kEThreads, smem, per_sm);
+    const cudaError_t e = blocks_per_sm(cache[dg ? 1 : 0], fn, kEThreads, smem, per_sm);
     if (e != cudaSuccess) return e;
     constexpr int WPB = kEThreads / 32;
     const long long ctas = (g1 - g0 + WPB - 1) / WPB;
     if (ctas <= 0) return cudaSuccess;
     const long long grid = ctas < (long long)sms * per_sm ? ctas : (long long)sms * per_sm;
-    count_elided4p<<<(unsigned)grid, kEThreads, smem, s>>>(w, begin, g0, g1, sink, dump, single, pairs, triples);
+    fn<<<(unsigned)grid, kEThreads, smem, s>>>(w, begin, g0, g1, sink, dump, single, pairs, triples);
     count_launch();
     return cudaGetLastError();
 }

@@ -434,6 +434,7 @@ __device__ __forceinline__ void elided4_prefix(const ScanWork& w, long long m, c
         const int l = l0 + gt;
         const bool valid = l < S;
         long long key = w.base_key;
+        unsigned long long dg = 0;
         if (valid) {
             uint32_t cnt[2][16];
 #pragma unroll
@@ -486,10 +487,17 @@ __device__ __forceinline__ void elided4_prefix(const ScanWork& w, long long m, c
             src.pkl = pairs + pair_index(c[2], l, S);
             src.sl = single4 + l;
             uint32_t* o = dump ? dump + ((size_t)m * S + l) * 2 * 81 : nullptr;
+            const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+            if (sink.digest && gtid < sink.dscratch_threads) o = sink.dscratch + (size_t)gtid * 2 * 81;
             // key = base + sum over the 81 cells of T[case] + T[control] - T[total]
             key += e4_exact_packed(cp, e4_load_both(src), [&](int q) { return ptab[q]; }, d.ftab, d.n_cases,
                                    d.n_ctrls, o);
+            if (sink.digest && o) {
+                c[3] = l;
+                dg = dg_table(c, 4, S, o, 81);
+            }
         }
+        if (sink.digest) dg_warp_add(sink.digest, dg);
         const bool pass = valid && key >= sink.thr;
         const unsigned mask = __ballot_sync(0xffffffffu, pass);
         if (mask) {

@@ -3,6 +3,7 @@
 // Semantics: see elided.cu.
 #pragma once
 
+#include "digest.cuh"
 #include "internal.h"
 
 namespace fiu {
@@ -154,6 +155,7 @@ __device__ __forceinline__ void elided_prefix(const ScanWork& w, long long m, co
             const int l = l0 + gt;
             const bool valid = l < S;
             long long key = w.base_key;
+            unsigned long long dg = 0;
             uint32_t cnt[2][CC];
             if (valid) {
 #pragma unroll
@@ -268,7 +270,14 @@ __device__ __forceinline__ void elided_prefix(const ScanWork& w, long long m, co
                         o[CELLS + q] = full[1][q];
                     }
                 }
+                if (sink.digest) {
+                    c[P] = l;
+                    dg = dg_begin(c, K, S);
+#pragma unroll
+                    for (int q = 0; q < CELLS; ++q) dg = dg_cell(dg, full[0][q], full[1][q]);
+                }
             }
+            if (sink.digest) dg_warp_add(sink.digest, dg);
             const bool pass = valid && key >= sink.thr;
             const unsigned mask = __ballot_sync(0xffffffffu, pass);
             if (mask) {

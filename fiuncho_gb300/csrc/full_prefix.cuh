@@ -3,6 +3,7 @@
 // Semantics: see count.cu.
 #pragma once
 
+#include "digest.cuh"
 #include "internal.h"
 
 namespace fiu {
@@ -98,8 +99,13 @@ __device__ __forceinline__ void full_prefix(const ScanWork& w, long long m, cons
                         const uint32_t a = acc[0][q], b = acc[1][q];
                         key += __ldg(d.ftab + a) + __ldg(d.ftab + b) - __ldg(d.ftab + a + b);
                     }
-                    if (dump) {
-                        uint32_t* o = dump + ((size_t)m * S + l) * 2 * CELLS + g * RG * 3;
+                    // the digest mode of orders <= 4 assembles the table in the thread's scratch row
+                    uint32_t* o = dump ? dump + ((size_t)m * S + l) * 2 * CELLS : nullptr;
+                    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+                    if (K <= 4 && sink.digest && gtid < sink.dscratch_threads)
+                        o = sink.dscratch + (size_t)gtid * 2 * CELLS;
+                    if (o) {
+                        o += g * RG * 3;
 #pragma unroll
                         for (int q = 0; q < RG * 3; ++q) {
                             o[q] = acc[0][q];
@@ -107,6 +113,15 @@ __device__ __forceinline__ void full_prefix(const ScanWork& w, long long m, cons
                         }
                     }
                 }
+            }
+            if (K <= 4 && sink.digest) {
+                unsigned long long dg = 0;
+                const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+                if (valid && gtid < sink.dscratch_threads) {
+                    c[P] = l;
+                    dg = dg_table(c, K, S, sink.dscratch + (size_t)gtid * 2 * CELLS, CELLS);
+                }
+                dg_warp_add(sink.digest, dg);
             }
             // Top-N filter: warp-aggregated append of candidates >= threshold.
             const bool pass = valid && key >= sink.thr;

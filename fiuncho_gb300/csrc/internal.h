@@ -20,6 +20,14 @@ struct CandSink {
     unsigned cap;
     long long thr;
     unsigned long long* evaluated;  // optional: += combinations evaluated
+    // Digest mode (fiu_scan_digest; off when null): every valid combination
+    // gets its exact tables and adds its term (digest.cuh) to one of the
+    // kDigestSlots sums at digest.  The order-4 kernels assemble a table in
+    // dscratch (2 x 81 words per thread of the grid, dscratch_threads threads;
+    // a thread beyond them adds a wrong term, so the digest cannot match).
+    unsigned long long* digest;
+    uint32_t* dscratch;
+    unsigned dscratch_threads;
 };
 
 // ---- multi-scan engine (batch.cu, engine.cu) ----------------------------------

@@ -41,7 +41,7 @@
 //
 // Reference semantics: GenotypeTable::combine_and_popcnt for order 3
 // (src/base/gt_popcnt.cpp:4-35) and MutualInformation::compute
-// (src/base/mutual_information.cpp:8-39) over the combinations ThreadedSearch
+// (src/base/mi_compute.cpp:16-41) over the combinations ThreadedSearch
 // visits (include/fiuncho/ThreadedSearch.h:157-180) with one worker.
 #include <cudaTypedefs.h>
 
@@ -202,9 +202,10 @@ __device__ __forceinline__ void t3_eval(const ScanWork& w, const CandSink& sink,
         kf = fmaf(bb, t3_lg2(bb + tiny), kf);
         kf = fmaf(-s, t3_lg2(s + tiny), kf);
     }
-    const bool cand = valid && (dump != nullptr || kf >= thr_f);
+    const bool cand = valid && (dump != nullptr || sink.digest != nullptr || kf >= thr_f);
     long long key = w.base_key;
     bool pass = false;
+    unsigned long long dg = 0;
     if (cand) {
 #pragma unroll
         for (int c = 0; c < 27; ++c) {
@@ -221,7 +222,14 @@ __device__ __forceinline__ void t3_eval(const ScanWork& w, const CandSink& sink,
                 o[27 + c] = f2u(t[1][c]);
             }
         }
+        if (sink.digest) {
+            const int cmb[3] = {i, j, l};
+            dg = dg_begin(cmb, 3, n);
+#pragma unroll
+            for (int c = 0; c < 27; ++c) dg = dg_cell(dg, f2u(t[0][c]), f2u(t[1][c]));
+        }
     }
+    if (sink.digest) dg_warp_add(sink.digest, dg);
     if (sink.evaluated) {
         const unsigned vmask = __ballot_sync(0xffffffffu, valid);
         if (lane == 0 && vmask) atomicAdd(sink.evaluated, (unsigned long long)__popc(vmask));
@@ -927,9 +935,10 @@ __device__ __forceinline__ void t2_eval(const ScanWork& w, const CandSink& sink,
         kf = fmaf(bb, t3_lg2(bb + tiny), kf);
         kf = fmaf(-s, t3_lg2(s + tiny), kf);
     }
-    const bool cand = valid && (dump != nullptr || kf >= thr_f);
+    const bool cand = valid && (dump != nullptr || sink.digest != nullptr || kf >= thr_f);
     long long key = w.base_key;
     bool pass = false;
+    unsigned long long dg = 0;
     if (cand) {
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
@@ -946,7 +955,14 @@ __device__ __forceinline__ void t2_eval(const ScanWork& w, const CandSink& sink,
                 o[9 + c] = f2u(t[1][c]);
             }
         }
+        if (sink.digest) {
+            const int cmb[2] = {i, j};
+            dg = dg_begin(cmb, 2, n);
+#pragma unroll
+            for (int c = 0; c < 9; ++c) dg = dg_cell(dg, f2u(t[0][c]), f2u(t[1][c]));
+        }
     }
+    if (sink.digest) dg_warp_add(sink.digest, dg);
     if (sink.evaluated) {
         const unsigned vmask = __ballot_sync(0xffffffffu, valid);
         if (lane == 0 && vmask) atomicAdd(sink.evaluated, (unsigned long long)__popc(vmask));

@@ -29,7 +29,7 @@
 //
 // Reference semantics: GenotypeTable::combine_and_popcnt for order 4
 // (src/base/gt_popcnt.cpp:4-35) and MutualInformation::compute
-// (src/base/mutual_information.cpp:8-39) over the combinations
+// (src/base/mi_compute.cpp:16-41) over the combinations
 // ThreadedSearch visits (include/fiuncho/ThreadedSearch.h:157-180) with one
 // worker.
 #include <algorithm>
@@ -249,6 +249,7 @@ __device__ __noinline__ long long t4_exact(const ScanWork& w, const uint32_t (&c
     return key;
 }
 
+template <bool DIGEST>
 __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink, long long thr_q, uint32_t* dump,
                                         const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
                                         const uint4* __restrict__ triples, const T4Item& it,
@@ -258,8 +259,9 @@ __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink,
     const int n = d.snps;
     long long key = w.base_key;
     bool pass = false;
+    unsigned long long dg = 0;
     if (valid) {
-        bool cand = dump != nullptr;
+        bool cand = DIGEST || dump != nullptr;
         if (!cand) {
             const int kk = k - k0, ll = l - l0;
             const long long est = t4_estimate(cp, it, kk, ll, kl, d.n_cases | d.n_ctrls << 16);
@@ -267,10 +269,17 @@ __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink,
         }
         if (cand) {
             uint32_t* o = dump ? dump + ((size_t)triple_index(i, j, k, n) * n + l) * 2 * 81 : nullptr;
+            const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
+            if (DIGEST && gt < sink.dscratch_threads) o = sink.dscratch + (size_t)gt * 2 * 81;
             key += t4_exact(w, cp, i, j, k, l, single, pairs, triples, o);
             pass = key >= sink.thr;
+            if (DIGEST) {
+                const int cmb[4] = {i, j, k, l};
+                dg = o ? dg_table(cmb, 4, n, o, 81) : 0;
+            }
         }
     }
+    if (DIGEST) dg_warp_add(sink.digest, dg);
     if (sink.evaluated) {
         const unsigned vm = __ballot_sync(0xffffffffu, valid);
         if (lane == 0 && vm) atomicAdd(sink.evaluated, (unsigned long long)__popc(vm));
@@ -302,7 +311,9 @@ __device__ __forceinline__ void t4_ld16(uint32_t taddr, uint32_t (&v)[16]) {
         : "r"(taddr));
 }
 
-template <bool PACK>
+// DIGEST: the digest mode of fiu_scan_digest (every valid combination's tables hashed), compiled
+// separately so that the search's instantiation carries none of its code.
+template <bool PACK, bool DIGEST>
 __global__ void __launch_bounds__(kT4Threads, 1)
     tensor4p_kernel(const __grid_constant__ T4Maps maps, ScanWork w, const long long* __restrict__ begin,
                     const long long* __restrict__ per, long long g0, long long g1, int k_cases, int pack,
@@ -567,7 +578,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     cp[1][r] = c4.z | (c4.w << 16);
                 }
                 __syncwarp();
-                t4_eval(w, sink, thr_q, dump, single, pairs, triples, it, cp, kl, i, j, k0, l0, valid ? k : 2,
+                t4_eval<DIGEST>(w, sink, thr_q, dump, single, pairs, triples, it, cp, kl, i, j, k0, l0, valid ? k : 2,
                         valid ? l : 3, valid, lane);
             }
         }
@@ -616,10 +627,12 @@ cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l256, const
                            const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
                            const uint4* triples, int* status, cudaStream_t s, int sms) {
     if (!triples || !pairs || !single || !begin || !per) return cudaErrorInvalidValue;
-    static LaunchCache cache_p, cache_s;
+    static LaunchCache cache[4];
+    const bool dg = sink.digest != nullptr;
+    auto fn = pack ? (dg ? tensor4p_kernel<true, true> : tensor4p_kernel<true, false>)
+                   : (dg ? tensor4p_kernel<false, true> : tensor4p_kernel<false, false>);
     int per_sm = 1;
-    cudaError_t e = pack ? blocks_per_sm(cache_p, tensor4p_kernel<true>, kT4Threads, kT4Smem, per_sm)
-                         : blocks_per_sm(cache_s, tensor4p_kernel<false>, kT4Threads, kT4Smem, per_sm);
+    cudaError_t e = blocks_per_sm(cache[(pack ? 2 : 0) + (dg ? 1 : 0)], fn, kT4Threads, kT4Smem, per_sm);
     if (e != cudaSuccess) return e;
     const long long items = g1 - g0;
     if (items <= 0) return cudaSuccess;
@@ -628,15 +641,9 @@ cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l256, const
     const double thr = ((double)sink.thr - (double)w.base_key) * scale - t4_margin(w.d.n_cases + w.d.n_ctrls) * 65536.0;
     const long long thr_q = (long long)std::floor(std::max(-9.0e18, std::min(9.0e18, thr)));
     const unsigned grid = (unsigned)(items < sms ? items : sms);
-    if (pack) {
-        T4Maps maps{map_l256, map_k, map_i};
-        tensor4p_kernel<true><<<grid, kT4Threads, kT4Smem, s>>>(maps, w, begin, per, g0, g1, k_cases, pack, sink,
-                                                                thr_q, dump, single, pairs, triples, status);
-    } else {
-        T4Maps maps{map_l128, map_k, map_i};
-        tensor4p_kernel<false><<<grid, kT4Threads, kT4Smem, s>>>(maps, w, begin, per, g0, g1, k_cases, pack, sink,
-                                                                 thr_q, dump, single, pairs, triples, status);
-    }
+    const T4Maps maps{pack ? map_l256 : map_l128, map_k, map_i};
+    fn<<<grid, kT4Threads, kT4Smem, s>>>(maps, w, begin, per, g0, g1, k_cases, pack, sink, thr_q, dump, single, pairs,
+                                         triples, status);
     count_launch();
     return cudaGetLastError();
 }

@@ -291,6 +291,16 @@ class GpuSearch:
                                                     _lib.ptr(out, C.c_uint32), out.size))
         return out.reshape(owned, resident.snps, 2, cells)
 
+    def scan_digest(self, resident: Resident, order: int, distribution: Distribution = None, kernel: int = 0):
+        """Digest of every table of a scan as `kernel` computes them (fiu_scan_digest):
+        (digest, combinations)."""
+        dg, cnt = C.c_uint64(0), C.c_uint64(0)
+        dist = distribution.c_struct() if distribution is not None else None
+        self.ctx.check(self.ctx.lib.fiu_scan_digest(self.ctx.h, resident.h, order,
+                                                    C.byref(dist) if dist is not None else None, kernel,
+                                                    C.byref(dg), C.byref(cnt)))
+        return int(dg.value), int(cnt.value)
+
     def combine(self, t1, size1, t2, cases_words, ctrls_words):
         t1 = np.ascontiguousarray(t1, np.uint64)
         t2 = np.ascontiguousarray(t2, np.uint64)

@@ -20,6 +20,11 @@ Named workloads (``WORKLOADS``):
   with penetrance 0.6.  Top-1 000.
 * ``order4_300x8000``   -- 300 SNPs, 4 000 / 4 000, order 4, MAF ~ U(0.05,
   0.5); one planted quadruple: all four carry a minor allele -> 0.7.  Top-100.
+* ``order3_500x18800`` / ``order4_100x18800`` -- 500 (100) SNPs, 9 000 cases /
+  9 800 controls (the class sizes of the reference's test data set), order 3
+  (4), MAF ~ U(0.05, 0.5), one planted triple (quadruple) with penetrance 0.65
+  (0.7).  Top-100 (top-50).  Classes this large do not share one FP32
+  accumulator, so these exercise the per-class tensor kernels.
 * ``batch_specs()``      -- 64 independent scans, seeds 1000+i: SNPs
   log-uniform in [500, 20 000], samples log-uniform in [1 000, 32 000], case
   fraction U(0.3, 0.7), order uniform in {2, 3, 4} (order-4 scans capped at
@@ -61,6 +66,8 @@ WORKLOADS = {
     "order2_40000x16000": ScanSpec(40000, 8000, 8000, 2, 1000, seed=3, maf="beta", planted=(2, 2, 2, 2, 2),
                                    penetrance=0.6),
     "order4_300x8000": ScanSpec(300, 4000, 4000, 4, 100, seed=4, planted=(4,), penetrance=0.7),
+    "order3_500x18800": ScanSpec(500, 9000, 9800, 3, 100, seed=5, planted=(3,), penetrance=0.65),
+    "order4_100x18800": ScanSpec(100, 9000, 9800, 4, 50, seed=6, planted=(4,), penetrance=0.7),
 }
 
 

@@ -234,20 +234,23 @@ int fiu_combine_and_popcnt(fiu_ctx *ctx, const uint64_t *t1, unsigned size1, con
 int fiu_mi_compute(fiu_ctx *ctx, const uint32_t *cases, const uint32_t *ctrls, size_t cells, size_t count,
                    unsigned n_cases, unsigned n_ctrls, int mode, float *out, double *out64);
 /* No counterpart in the reference.  MutualInformation::compute's fixed-point
- * arithmetic (mode 0 of fiu_mi_compute) for callers that cannot allocate
- * device memory at run time (a host that has handed all GPU memory to its own
- * pool, a pipeline that cannot take cudaMalloc's device-wide synchronisation,
- * a plugin host owning the memory policy).  Allocates nothing: tables and
- * outputs are the caller's device buffers (d_cases/d_ctrls: count x cells
- * uint32 each, d_out: count floats), and the only scratch is a library-owned
- * static device table sized for n_cases + n_ctrls <= FIU_NOALLOC_MAX_SAMPLES
- * (512 KiB per GPU that loads the library, kept until exit); larger requests
- * return FIU_ERR_UNSUPPORTED.  Work is enqueued on `stream` (a cudaStream_t,
- * NULL = legacy default stream) and not waited for.  The first call on a device
- * looks up the table's device address with that device current; make that
- * first call before any stream capture.  All calls share the table and it
- * keeps the last call's contents, so calls that overlap on the GPU (different
- * streams, different threads) race and must be serialised by the caller. */
+ * arithmetic (mode 0 of fiu_mi_compute, bit-identical results) for callers
+ * that cannot allocate device memory at run time (a host that has handed all
+ * GPU memory to its own pool, a pipeline that cannot take cudaMalloc's
+ * device-wide synchronisation, a plugin host owning the memory policy).
+ * Allocates nothing: tables and outputs are the caller's device buffers
+ * (d_cases/d_ctrls: count x cells uint32 each, d_out: count floats), and the
+ * only scratch is a library-owned static device table of c ln c values sized
+ * for n_cases + n_ctrls <= FIU_NOALLOC_MAX_SAMPLES (512 KiB per GPU that loads
+ * the library, kept until exit); larger requests return FIU_ERR_UNSUPPORTED.
+ * Work is enqueued on `stream` (a cudaStream_t, NULL = legacy default stream)
+ * and not waited for.  Set-up: the first call on a device -- and the first
+ * after the device's context changed, e.g. after cudaDeviceReset, which
+ * discards the table -- looks up the table's device address with that device
+ * current and fills it with a synchronous 512 KiB copy; make that call before
+ * any stream capture.  Calls after the set-up only read the table, so calls
+ * may overlap; a set-up that overlaps another call on the same device (in
+ * another thread) races with it. */
 #define FIU_NOALLOC_MAX_SAMPLES 65536
 int fiu_mi_compute_noalloc(const uint32_t *d_cases, const uint32_t *d_ctrls, size_t cells, size_t count,
                            unsigned n_cases, unsigned n_ctrls, float *d_out, void *stream);
@@ -261,6 +264,23 @@ int fiu_tables(fiu_ctx *ctx, const fiu_resident *res, unsigned order, const int3
  * prefix ordinal m and last SNP l (entries with l <= prefix end stay as given). */
 int fiu_scan_tables(fiu_ctx *ctx, const fiu_resident *res, unsigned order, const fiu_distribution *distribution,
                     int kernel, uint32_t *out, size_t out_words);
+/* Digest of every table of a scan, for parity checks at full size.  No
+ * counterpart in the reference's API; it checks what combine_and_popcnt
+ * (src/base/gt_popcnt.cpp:4-35) gives for every combination ThreadedSearch
+ * visits (include/fiuncho/ThreadedSearch.h:157-180) without storing the tables.
+ * The kernel `kernel` (FIU_KERNEL_*, FIU_KERNEL_AUTO = the search's own
+ * choice; orders <= 4 for FIU_KERNEL_FULL) evaluates every combination of
+ * `distribution` (NULL = the whole data set) and
+ *   *digest = sum over the combinations c (mod 2^64) of h(c), where
+ *   v = c[0] snps^(order-1) + ... + c[order-1]   (uint64, wrapping),
+ *   h = mix(v + 0x9E3779B97F4A7C15), then for each cell x in the reference's
+ *   cell order (first SNP most significant) h = mix(h ^ (cases[x] << 32 | ctrls[x])),
+ *   mix(z): z = (z ^ z >> 30) * 0xBF58476D1CE4E5B9; z = (z ^ z >> 27) * 0x94D049BB133111EB;
+ *           z ^ z >> 31  (the SplitMix64 output function);
+ * *combinations = the number of combinations hashed.  The same sum over the
+ * reference's own tables must come out equal. */
+int fiu_scan_digest(fiu_ctx *ctx, const fiu_resident *res, unsigned order, const fiu_distribution *distribution,
+                    int kernel, uint64_t *digest, uint64_t *combinations);
 
 #ifdef __cplusplus
 }

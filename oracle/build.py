@@ -24,6 +24,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# The reference tree this recipe compiles from: FIUNCHO_REFERENCE, else the
+# development container's read-only checkout (absent on the GPU hosts, where
+# nothing of it is built or read).
 REF_ROOT = os.environ.get("FIUNCHO_REFERENCE", "/root/reference")
 REF_OUT = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
@@ -44,7 +47,7 @@ def _stale(out, srcs):
 
 def build_oracle(force: bool = False) -> str:
     src = os.path.join(HERE, "oracle.c")
-    if force or _stale(ORACLE_SO, [src, os.path.abspath(__file__)]):
+    if force or _stale(ORACLE_SO, [src, os.path.join(HERE, "ref", "tabledigest.h"), os.path.abspath(__file__)]):
         # hardware popcount: part of the aarch64 base ISA, an explicit flag on x86-64
         isa = ["-mpopcnt"] if platform.machine() in ("x86_64", "AMD64") else []
         _run(["gcc", "-O3", "-std=gnu11", "-fPIC", "-shared", "-pthread"] + isa + [src, "-o", ORACLE_SO + ".tmp",
@@ -76,17 +79,18 @@ def build_ref(force: bool = False) -> dict:
     inc = ["-I", os.path.join(REF_ROOT, "include"), "-I", os.path.join(HERE, "ref")]
     driver = os.path.join(HERE, "ref", "ref_driver.cpp")
     shim = os.path.join(HERE, "ref", "mpi.h")
+    digest_h = os.path.join(HERE, "ref", "tabledigest.h")
     built = {}
     base_srcs = [os.path.join(REF_ROOT, "src", "base", f) for f in ("gt_combine.cpp", "gt_popcnt.cpp", "mi_compute.cpp")]
     out = os.path.join(REF_OUT, "libref_base.so")
-    if force or _stale(out, [driver, shim] + base_srcs):
+    if force or _stale(out, [driver, shim, digest_h] + base_srcs):
         _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread"] + inc + [driver] + base_srcs + ["-o", out])
     built["base"] = out
     if _has_avx512bw():
         d = os.path.join(REF_ROOT, "src", "avx512bw")
         srcs = [os.path.join(d, f) for f in ("gt_combine.cpp", "gt_popcnt_avx512bw_lu.cpp", "mi_compute_512.cpp")]
         out = os.path.join(REF_OUT, "libref_avx512.so")
-        if force or _stale(out, [driver, shim] + srcs):
+        if force or _stale(out, [driver, shim, digest_h] + srcs):
             _run(["g++", "-O3", "-std=c++17", "-march=native", "-ffast-math", "-DALIGN=64", "-fPIC", "-shared",
                   "-pthread"] + inc + [driver] + srcs + ["-o", out, "-lmvec"])
         built["avx512"] = out

@@ -25,6 +25,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "ref/tabledigest.h"
+
 #define ORC_MAX_ORDER 8
 
 static inline uint32_t popc64(uint64_t x) { return (uint32_t)__builtin_popcountll(x); }
@@ -240,6 +242,8 @@ typedef struct {
     int order, n, step, offset, mi_mode;
     orc_maxarray max;
     uint64_t combos;
+    int digest_mode; /* 1: add each table's digest term (ref/tabledigest.h) instead of ranking */
+    uint64_t digest;
 } orc_thread_args;
 
 static void *orc_thread_main(void *p)
@@ -275,6 +279,14 @@ static void *orc_thread_main(void *p)
             const uint64_t *lc = a->data + (size_t)l * per_snp, *lt = lc + 3 * a->cw;
             orc_popcnt(pc, sz, lc, a->cw, ctc, cells);
             orc_popcnt(pt, sz, lt, a->tw, ctt, cells);
+            if (a->digest_mode) {
+                int cmb[ORC_MAX_ORDER];
+                for (int i = 0; i < k; ++i) cmb[i] = it.c[i];
+                cmb[k] = l;
+                a->digest += td_term(cmb, order, a->snps, ctc, ctt, (int)cells);
+                a->combos++;
+                continue;
+            }
             orc_result res;
             memset(&res, 0, sizeof(res));
             for (int i = 0; i < k; ++i) res.c[i] = it.c[i];
@@ -426,4 +438,40 @@ void orc_mi_batch(const uint32_t *cases, const uint32_t *ctrls, size_t size, siz
         if (out32) out32[q] = orc_mi_f32(cases + q * size, ctrls + q * size, size, n_cases, n_ctrls);
         if (out64) out64[q] = orc_mi_f64(cases + q * size, ctrls + q * size, size, n_cases, n_ctrls);
     }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Digest (ref/tabledigest.h) of the tables of every combination that
+ * orc_search would visit for the same distribution and threads, built by the
+ * same combine / popcnt chain (ThreadedSearch.h:157-180).  Returns the number
+ * of combinations hashed, or a negative error. */
+long orc_table_digest(const uint64_t *data, size_t snps, size_t cases_words, size_t ctrls_words, int order,
+                      int dist_n, int dist_step, int dist_offset, int nthreads, uint64_t *digest)
+{
+    if (order < 2 || order > ORC_MAX_ORDER || nthreads < 1 || dist_step < 1) return -1;
+    orc_thread_args *args = (orc_thread_args *)calloc((size_t)nthreads, sizeof(orc_thread_args));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int t = 0; t < nthreads; ++t) {
+        orc_thread_args *a = &args[t];
+        a->data = data;
+        a->snps = snps;
+        a->cw = cases_words;
+        a->tw = ctrls_words;
+        a->order = order;
+        a->n = dist_n;
+        a->step = dist_step * nthreads;
+        a->offset = dist_offset * nthreads + t;
+        a->digest_mode = 1;
+        pthread_create(&th[t], NULL, orc_thread_main, a);
+    }
+    uint64_t sum = 0, combos = 0;
+    for (int t = 0; t < nthreads; ++t) {
+        pthread_join(th[t], NULL);
+        sum += args[t].digest;
+        combos += args[t].combos;
+    }
+    free(args);
+    free(th);
+    *digest = sum;
+    return (long)combos;
 }

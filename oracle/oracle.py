@@ -47,6 +47,9 @@ class Oracle:
         L.orc_tables.argtypes = [_u64p, C.c_size_t, C.c_size_t, C.c_int, _i32p, C.c_size_t, _u32p, _u32p]
         L.orc_tables.restype = C.c_int
         L.orc_mi_batch.argtypes = [_u32p, _u32p, C.c_size_t, C.c_size_t, C.c_uint32, C.c_uint32, _f32p, _f64p]
+        L.orc_table_digest.argtypes = [_u64p, C.c_size_t, C.c_size_t, C.c_size_t, C.c_int, C.c_int, C.c_int,
+                                       C.c_int, C.c_int, C.POINTER(C.c_uint64)]
+        L.orc_table_digest.restype = C.c_long
         self.L = L
 
     # -- data model ---------------------------------------------------------
@@ -118,6 +121,17 @@ class Oracle:
         return combos[: r * order].reshape(r, order), v32[:r], v64[:r], int(done.value)
 
 
+    def table_digest(self, data, snps, cases_words, ctrls_words, order, threads=1, dist=None):
+        """Digest (oracle/ref/tabledigest.h) of every table of a scan: (digest, combinations)."""
+        n, step, offset = dist if dist is not None else (snps, 1, 0)
+        out = C.c_uint64(0)
+        r = self.L.orc_table_digest(np.ascontiguousarray(data, np.uint64), snps, cases_words, ctrls_words, order, n,
+                                    step, offset, threads, C.byref(out))
+        if r < 0:
+            raise ValueError("oracle digest: invalid arguments")
+        return int(out.value), int(r)
+
+
 class Reference:
     """The reference's own code (built from its sources by oracle/build.py)."""
 
@@ -143,6 +157,9 @@ class Reference:
         L.ref_tables.restype = C.c_int
         L.ref_mi.argtypes = [C.c_int, _u32p, _u32p, C.c_size_t, C.c_uint, C.c_uint, _f32p]
         L.ref_mi.restype = C.c_int
+        L.ref_table_digest.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint64),
+                                       C.POINTER(C.c_uint64)]
+        L.ref_table_digest.restype = C.c_int
         self.L = L
         self.flavour = flavour
         self.align = L.ref_align()
@@ -198,6 +215,14 @@ class RefDataset:
         if r < 0:
             raise RuntimeError(self.ref.L.ref_last_error().decode())
         return combos[: r * order].reshape(r, order), vals[:r]
+
+    def table_digest(self, order, threads=1, step=1, offset=0):
+        """Digest (oracle/ref/tabledigest.h) of the reference's tables of every
+        combination of Distribution(snps, order-1, step, offset): (digest, combinations)."""
+        dg, cnt = C.c_uint64(0), C.c_uint64(0)
+        if self.ref.L.ref_table_digest(self.h, order, threads, step, offset, C.byref(dg), C.byref(cnt)) != 0:
+            raise RuntimeError(self.ref.L.ref_last_error().decode())
+        return int(dg.value), int(cnt.value)
 
     def tables(self, order, combos):
         combos = np.ascontiguousarray(combos, np.int32).reshape(-1, order)

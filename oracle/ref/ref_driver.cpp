@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "mpi.h"
+#include "tabledigest.h"
 
 #define private public
 #include <fiuncho/Dataset.h>
@@ -204,4 +205,58 @@ int ref_mi(int order, const uint32_t *cases, const uint32_t *ctrls, size_t count
     return 0;
 }
 
+/* Digest (tabledigest.h) of the contingency tables of every combination a
+ * Distribution(snps, order-1, step, offset) owns, visited exactly as
+ * ThreadedSearch::nonsegmented_search visits them (ThreadedSearch.h:142-182):
+ * each of `threads` threads owns distribution.layer(threads, t), builds the
+ * prefix table with chained GenotypeTable::combine and fills each table with
+ * GenotypeTable::combine_and_popcnt.  *count receives the combinations hashed. */
+int ref_table_digest(void *h, int order, int threads, int step, int offset, uint64_t *digest, uint64_t *count)
+{
+    try {
+        const auto &d = *((Handle *)h)->d;
+        const Distribution<int> dist((int)d.snps, order - 1, step, offset);
+        int cells = 1;
+        for (int i = 0; i < order; ++i) cells *= 3;
+        std::vector<uint64_t> sums(threads, 0), counts(threads, 0);
+        std::vector<std::thread> ts;
+        for (int t = 0; t < threads; ++t)
+            ts.emplace_back([&, t]() {
+                std::vector<GenotypeTable<uint64_t>> gts;
+                gts.reserve(order);
+                for (int o = 2; o < order; ++o) gts.emplace_back(o, d[0].cases_words, d[0].ctrls_words);
+                ContingencyTable<uint32_t> ct(order);
+                std::vector<int> comb(order);
+                const Distribution<int> mine = dist.layer(threads, t);
+                uint64_t s = 0, cnt = 0;
+                for (auto c = mine.begin(); c < mine.end(); ++c) {
+                    for (int i = 0; i < order - 2; ++i)
+                        GenotypeTable<uint64_t>::combine(i > 0 ? gts[i - 1] : d[c[0]], d[c[i + 1]], gts[i]);
+                    for (int i = 0; i < order - 1; ++i) comb[i] = c[i];
+                    for (int l = c->back() + 1; l < (int)d.snps; ++l) {
+                        GenotypeTable<uint64_t>::combine_and_popcnt(order > 2 ? gts.back() : d[c[0]], d[l], ct);
+                        comb[order - 1] = l;
+                        s += td_term(comb.data(), order, d.snps, ct.cases, ct.ctrls, cells);
+                        ++cnt;
+                    }
+                }
+                sums[t] = s;
+                counts[t] = cnt;
+            });
+        uint64_t s = 0, cnt = 0;
+        for (int t = 0; t < threads; ++t) {
+            ts[t].join();
+            s += sums[t];
+            cnt += counts[t];
+        }
+        *digest = s;
+        *count = cnt;
+        return 0;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
 } // extern "C"
+

@@ -1,7 +1,7 @@
 """Generates the golden fixtures in this folder from the reference itself.
 
-Run in a checkout where the reference tree is present (``FIUNCHO_REFERENCE``,
-default /root/reference) -- it builds the reference's own sources through
+Run in a checkout where the reference tree is present (``FIUNCHO_REFERENCE``
+names it) -- it builds the reference's own sources through
 ``oracle/build.py`` and calls them through ``oracle/ref/ref_driver.cpp``:
 
     python tests/golden/make_golden.py
@@ -20,7 +20,9 @@ Outputs:
 * ``reference_synth.npz`` -- a small seeded synthetic scan with odd class
   sizes (999 cases / 1 001 controls, 48 SNPs) as genotype codes, with the
   reference's ThreadedSearch top-50 for orders 2, 3 and 4, its tables/MI for
-  1 500 sampled order-3 combinations, and a 3-thread and a step-2/offset-1 run.
+  1 500 sampled order-3 combinations, a 3-thread and a step-2/offset-1 run, and
+  the digest (oracle/ref/tabledigest.h) of the reference's tables of every
+  combination at orders 2, 3 and 4 and of a step-3/offset-2 order-3 layer.
 """
 from __future__ import annotations
 
@@ -99,6 +101,12 @@ def main():
     out["o3_t3_combos"], out["o3_t3_vals"] = c, v
     c, v = rd.search(3, 50, threads=1, step=2, offset=1)
     out["o3_step2_off1_combos"], out["o3_step2_off1_vals"] = c, v
+    # digest (oracle/ref/tabledigest.h) of every table of the scan, per order, and of a step-3/offset-2 layer
+    for order in (2, 3, 4):
+        dg, cnt = rd.table_digest(order, threads=2)
+        out["o%d_digest" % order], out["o%d_digest_count" % order] = np.array(dg, np.uint64), np.array(cnt)
+    dg, cnt = rd.table_digest(3, threads=1, step=3, offset=2)
+    out["o3_step3_off2_digest"], out["o3_step3_off2_digest_count"] = np.array(dg, np.uint64), np.array(cnt)
     cmb = all_combos(ds.snps, 3)
     cmb = cmb[np.sort(np.random.default_rng(11).choice(len(cmb), 1500, replace=False))]
     cc, tt, mi = rd.tables(3, cmb)

@@ -60,7 +60,7 @@ def test_engine_single_rank_gather_sorts_and_truncates():
 def test_dataset_readers_match_packed_fixture(golden_testdata):
     """Our TPED / RAW / GAMETES readers produce the reference's packed bits (needs the reference's data files)."""
     from fiuncho_gb300 import Dataset
-    root = os.environ.get("FIUNCHO_REFERENCE", "/root/reference")
+    from oracle.build import REF_ROOT as root
     d = os.path.join(root, "tests", "data")
     if not os.path.exists(os.path.join(d, "test.tped")):
         pytest.skip("reference test data not present")

@@ -6,7 +6,7 @@ import subprocess
 import numpy as np
 import pytest
 
-REF = os.environ.get("FIUNCHO_REFERENCE", "/root/reference")
+from oracle.build import REF_ROOT as REF  # noqa: E402
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 

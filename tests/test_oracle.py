@@ -209,3 +209,58 @@ def test_synth_sampled_tables(oracle, golden_synth):
     assert np.array_equal(cc, golden_synth["o3_cases"]) and np.array_equal(tt, golden_synth["o3_ctrls"])
     o32, _ = oracle.mi_batch(cc, tt, ds.cases, ds.ctrls)
     assert np.array_equal(o32, golden_synth["o3_mi_base"])
+
+
+# ---------------------------------------------------------------- table digest
+def _synth_ds(g):
+    from fiuncho_gb300.dataset import Dataset
+    return Dataset.from_genotypes(g["geno"], g["is_case"])
+
+
+@pytest.mark.parametrize("order", [2, 3, 4])
+def test_digest_matches_reference(oracle, golden_synth, order):
+    """The oracle's digest of every table of a scan (oracle/ref/tabledigest.h) equals the
+    digest of the reference's own combine / combine_and_popcnt tables (fixture)."""
+    ds = _synth_ds(golden_synth)
+    dg, cnt = oracle.table_digest(ds.data, ds.snps, ds.cases_words, ds.ctrls_words, order, threads=3)
+    assert cnt == int(golden_synth["o%d_digest_count" % order]) == math.comb(ds.snps, order)
+    assert dg == int(golden_synth["o%d_digest" % order])
+
+
+def test_digest_distribution_layer(oracle, golden_synth):
+    """Digest of the tables a Distribution(48, 2, 3, 2) layer owns, as the reference enumerates them."""
+    ds = _synth_ds(golden_synth)
+    dg, cnt = oracle.table_digest(ds.data, ds.snps, ds.cases_words, ds.ctrls_words, 3, threads=1,
+                                  dist=(ds.snps, 3, 2))
+    assert cnt == int(golden_synth["o3_step3_off2_digest_count"])
+    assert dg == int(golden_synth["o3_step3_off2_digest"])
+
+
+def test_digest_detects_one_wrong_cell(oracle, golden_synth):
+    """A single count changed by one in one cell of one combination changes the digest: the
+    mistake is planted in the oracle's input (one sample's genotype moved), on the CPU."""
+    from fiuncho_gb300.dataset import Dataset
+    g = golden_synth["geno"].copy()
+    g[5, 17] = (g[5, 17] + 1) % 3
+    ds = Dataset.from_genotypes(g, golden_synth["is_case"])
+    dg, _ = oracle.table_digest(ds.data, ds.snps, ds.cases_words, ds.ctrls_words, 2, threads=2)
+    assert dg != int(golden_synth["o2_digest"])
+
+
+def test_scale_fixture_layout():
+    """The full-size fixture holds, per workload, the data set's SHA-256, the reference's digest of
+    every table with its combination count C(snps, order), and its top-N."""
+    import os
+    from fiuncho_gb300 import synth
+    path = os.path.join(os.path.dirname(__file__), "golden", "reference_scale.npz")
+    g = dict(np.load(path))
+    names = sorted({k.rsplit("_", 1)[0] for k in g if k.endswith("_digest")})
+    assert names, "no workloads in the full-size fixture"
+    for name in names:
+        spec = synth.WORKLOADS[name]
+        assert int(g[name + "_count"]) == math.comb(spec.snps, spec.order)
+        c, v = g[name + "_combos"], g[name + "_vals"]
+        assert c.shape == (spec.outputs, spec.order)
+        assert_ascending_unique(c)
+        assert_sorted_desc(v)
+        assert len(str(g[name + "_sha256"])) == 64
