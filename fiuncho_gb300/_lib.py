@@ -52,7 +52,7 @@ class ServerStats_t(C.Structure):
                 ("active", C.c_uint64), ("rounds", C.c_uint64), ("bytes_in_use", C.c_uint64), ("p50_ms", C.c_double),
                 ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
                 ("combos_samples", C.c_double), ("solo", C.c_uint64),
-                ("overlapped", C.c_uint64)]
+                ("overlapped", C.c_uint64), ("peak_bytes", C.c_uint64)]
 
 
 _u64p = C.POINTER(C.c_uint64)

@@ -734,12 +734,18 @@ int fiu_mi_compute(fiu_ctx* ctx, const uint32_t* cases, const uint32_t* ctrls, s
                    unsigned n_cases, unsigned n_ctrls, int mode, float* out, double* out64) {
     if (!ctx) return FIU_ERR_INVALID;
     Scope scope(ctx);
-    if (!cases || !ctrls || !out || cells == 0 || (mode != 0 && mode != 1) || n_cases + n_ctrls == 0)
+    const long long tmax = (long long)n_cases + n_ctrls;  // no unsigned wrap
+    if (!cases || !ctrls || !out || cells == 0 || (mode != 0 && mode != 1) || tmax == 0)
         return fail(ctx, FIU_ERR_INVALID, "invalid mi_compute arguments");
+    if (tmax > 0x7fffffffll) return fail(ctx, FIU_ERR_UNSUPPORTED, "n_cases + n_ctrls above 2^31 - 1");
     if (count == 0) return FIU_OK;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
-    const long long tmax = (long long)n_cases + n_ctrls;
-    std::vector<long long> ftab(tmax + 1);
+    std::vector<long long> ftab;
+    try {
+        ftab.resize((size_t)tmax + 1);
+    } catch (const std::exception&) {
+        return fail(ctx, FIU_ERR_NOMEM, "host c ln c table");
+    }
     for (long long c = 0; c <= tmax; ++c)
         ftab[c] = c < 2 ? 0 : (long long)llround((double)c * std::log((double)c) * 4294967296.0);
     uint32_t *da = nullptr, *db = nullptr;

@@ -111,6 +111,7 @@ struct fiu_server {
     std::vector<int> free_slots;
     // statistics (under mu)
     uint64_t submitted = 0, completed = 0, failed = 0, rounds = 0, bytes_in_use = 0, solo = 0, overlapped = 0;
+    uint64_t peak_bytes = 0;
     std::vector<double> lat_ms;
     double combos_samples = 0;
     int init_status = FIU_OK;
@@ -161,6 +162,7 @@ void finish(fiu_server* sv, ServeScan* s, int status, fiu_ctx* ctx = nullptr) {
         sv->failed++;
     }
     sv->cv_done.notify_all();
+    sv->cv_work.notify_all();  // memory freed: the worker may admit the next scan
 }
 
 // Uploads and plans an admitted scan; returns false when it finished right away.
@@ -370,9 +372,13 @@ void worker_main(fiu_server* sv) {
                 if (sv->stop) return;
                 if (sv->queue.empty() || sv->free_slots.empty()) break;
                 ServeScan* h = sv->queue.front();
-                if (sv->bytes_in_use + h->bytes > sv->budget && !sv->active.empty()) break;
+                // every admitted scan holds its footprint until it finishes, whether it runs
+                // in the rounds or waits for / runs on a solo lane; a scan larger than the
+                // budget left runs only when nothing else holds device memory
+                if (sv->bytes_in_use + h->bytes > sv->budget && sv->bytes_in_use > 0) break;
                 sv->queue.pop_front();
                 sv->bytes_in_use += h->bytes;
+                sv->peak_bytes = std::max(sv->peak_bytes, sv->bytes_in_use);
                 s = h;
             }
             if (admit(sv, s)) sv->active.push_back(s);
@@ -504,6 +510,7 @@ int fiu_server_stats(fiu_server* sv, fiu_serve_stats* out) {
     out->solo = sv->solo;
     out->overlapped = sv->overlapped;
     out->bytes_in_use = sv->bytes_in_use;
+    out->peak_bytes = sv->peak_bytes;
     out->combos_samples = sv->combos_samples;
     if (!sv->lat_ms.empty()) {
         std::vector<double> v = sv->lat_ms;

@@ -434,7 +434,9 @@ class MPIEngine:
             blobs = [blob]
         else:
             blobs = [None] * self.size if self.rank == 0 else None
-            self.dist.gather_object(blob, blobs, dst=0, group=self.group)
+            # gather_object's dst is a global rank: the group's rank 0 in global numbering
+            dst = self.dist.get_global_rank(self.group, 0) if self.group is not None else 0
+            self.dist.gather_object(blob, blobs, dst=dst, group=self.group)
             if self.rank != 0:
                 return []
         res = []

@@ -200,8 +200,13 @@ typedef struct {
                                      lane's own stream beside the rounds */
     uint64_t overlapped;          /* completed scans whose device work overlapped another
                                      scan's (either lane) */
+    uint64_t peak_bytes;          /* largest bytes_in_use so far (never above the budget, except
+                                     for one scan larger than the budget left, run alone) */
 } fiu_serve_stats;
-/* budget_bytes: device memory the admitted scans may hold (0 = 120 GB). */
+/* budget_bytes: device memory the admitted scans may hold (0 = 120 GB): a scan
+ * is admitted -- its data set uploaded -- when its footprint fits what the
+ * admitted scans leave, whichever lane then runs it; scans larger than the
+ * whole budget are rejected at submit. */
 int fiu_server_create(int device, uint64_t budget_bytes, fiu_server **out);
 /* Queues a scan of the whole data set (Distribution(snps, order-1, 1, 0)). */
 int fiu_server_submit(fiu_server *srv, const fiu_dataset *dataset, unsigned order, unsigned outputs,

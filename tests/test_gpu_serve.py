@@ -65,17 +65,32 @@ def test_server_alone_and_in_mix_identical():
         srv.close()
 
 
-def test_server_budget_admits_one_at_a_time():
-    """A budget that fits one scan at a time still completes everything, in order."""
-    from fiuncho_gb300 import Distribution, GpuSearch, Server
+@pytest.mark.parametrize("one_hot", [True, False])
+def test_server_budget_admits_one_at_a_time(one_hot):
+    """A budget that fits one scan at a time still completes everything, and the
+    admitted scans never hold more than the budget, whether they run on the solo
+    lanes (one-hot: tensor-core kernels) or in the rounds (not one-hot)."""
+    from fiuncho_gb300 import Distribution, FiunchoError, GpuSearch, Server
     gs = GpuSearch(0)
-    data = [_ds(20 + i, 200, 1000, 1000) for i in range(4)]
-    srv = Server(0, budget_bytes=8 * 1024 * 1024)
+    data = [_ds(20 + i, 200, 1000, 1000, one_hot) for i in range(4)]
+    budget = 8 * 1024 * 1024
+    srv = Server(0, budget_bytes=budget)
     try:
         tickets = [srv.submit(ds, 3, 20) for ds in data]
-        for ds, t in zip(data, tickets):
-            _same(srv.result(t), gs.run(ds, 3, Distribution(ds.snps, 2), 20, with_fp64=True))
-        from fiuncho_gb300 import FiunchoError
+        seen = []
+        pending = list(zip(data, tickets))
+        while pending:
+            seen.append(srv.stats()["bytes_in_use"])
+            ds, t = pending[0]
+            r = srv.result(t, 1)
+            if r is None:
+                continue
+            _same(r, gs.run(ds, 3, Distribution(ds.snps, 2), 20, with_fp64=True))
+            pending.pop(0)
+        st = srv.stats()
+        assert max(seen) <= budget and 0 < st["peak_bytes"] <= budget
+        assert st["completed"] == 4 and st["bytes_in_use"] == 0
+        assert st["solo"] == (4 if one_hot else 0)
         with pytest.raises(FiunchoError):
             srv.submit(_ds(30, 3000, 4000, 4000), 3, 10)  # larger than the whole budget
     finally:
@@ -99,9 +114,9 @@ def test_server_concurrent_submitters():
         t.join(timeout=120)
     try:
         assert len(out) == 6 and all(len(r[0]) == 15 for r in out.values())
-        assert srv.result(123456789, 0) is None or True
-    except KeyError:
-        pass
+        # an unknown (or already collected) ticket is an invalid argument
+        from fiuncho_gb300 import _lib
+        assert srv.lib.fiu_server_poll(srv.h, 123456789, 0, None, None, None, None, None) == _lib.FIU_ERR_INVALID
     finally:
         srv.close()
 

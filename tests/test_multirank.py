@@ -108,3 +108,59 @@ def test_two_rank_gather_equals_single_rank(tmp_path, sharded):
     full = OracleSearch().run(ds, 3, Distribution(snps, 2), 25)
     assert [list(map(int, r[:3])) for r in got0] == [r.combination for r in full]
     assert np.allclose(got0[:, 3], [r.val for r in full], rtol=1e-12)
+
+
+def _rank_main_subgroup(rank, world, port, data_path, out_path):
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import torch.distributed as dist
+
+    from fiuncho_gb300 import Dataset, MPIEngine
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sub = dist.new_group([1, 2])  # every rank takes part in creating it
+        if rank in (1, 2):
+            z = np.load(data_path)
+            ds = Dataset.from_genotypes(z["geno"], z["is_case"])
+            res = MPIEngine(group=sub).run(OracleSearch, None, 3, 25, dataset=ds)
+            np.save(out_path % rank, np.array([r.combination + [r.val] for r in res], np.float64).reshape(-1, 4))
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_subgroup_gather_goes_to_the_groups_first_rank(tmp_path):
+    """An engine over a process subgroup that leaves out global rank 0 gathers on the
+    group's own rank 0 (global rank 1) and returns the whole search there."""
+    import multiprocessing as mp
+
+    from fiuncho_gb300 import Dataset, Distribution
+    rng = np.random.default_rng(12)
+    snps, n_case, n_ctrl = 30, 250, 260
+    maf = rng.uniform(0.05, 0.5, snps)[:, None]
+    u = rng.random((snps, n_case + n_ctrl))
+    geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
+    is_case = np.r_[np.ones(n_case, np.uint8), np.zeros(n_ctrl, np.uint8)]
+    data_path = str(tmp_path / "data.npz")
+    np.savez(data_path, geno=geno, is_case=is_case)
+    out_path = str(tmp_path / "rank%d.npy")
+    port = _free_port()
+    ctx = mp.get_context("spawn")
+    procs = [ctx.Process(target=_rank_main_subgroup, args=(r, 3, port, data_path, out_path)) for r in range(3)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+    for p in procs:
+        if p.is_alive():
+            p.kill()
+            p.join()
+    assert all(p.exitcode == 0 for p in procs), [p.exitcode for p in procs]
+    got1, got2 = np.load(out_path % 1), np.load(out_path % 2)
+    assert got2.shape[0] == 0
+    ds = Dataset.from_genotypes(geno, is_case)
+    full = OracleSearch().run(ds, 3, Distribution(snps, 2), 25)
+    assert [list(map(int, r[:3])) for r in got1] == [r.combination for r in full]
