@@ -171,12 +171,15 @@ struct T3Plan {
     double item_combos = 0;  // combinations per work item, about 32 x L / 2
     int pitch = 0;        // bytes per plane row
     int k_cases = 0;      // padded case samples (= byte offset of the control region)
+    bool pair3 = false;   // order 3, packed classes: pair items (i, 64 j, 128 l) of the CTA-pair kernel
     long long* item_begin = nullptr;
     long long total = 0;  // work items
     CUtensorMap map_l;    // box 128 B x 192 rows (256 when packed), 128-byte swizzle (l operand)
     CUtensorMap map_j;    // box 128 B x 64 rows, 128-byte swizzle (j rows of the (i,j) operand)
     CUtensorMap map_i;    // box 128 B x 2 rows, 128-byte swizzle (i rows)
-    // order 2: work items (64 i, 128 j) over i-tiles
+    // order 2: work items (64 i, 128 j) over i-tiles, or pair items (2 x 64 i, 128 j) of the
+    // CTA-pair kernel (pair2)
+    bool pair2 = false;
     long long* item2_begin = nullptr;
     long long total2 = 0;
     int n_itiles = 0;

@@ -1,4 +1,8 @@
-// Order-3 contingency tables on the 5th-generation tensor cores (tcgen05).
+// Order-3 and order-2 contingency tables on the 5th-generation tensor cores
+// (tcgen05).  Kernels: tensor3x_kernel (order 3, classes that pack into one
+// accumulator, CTA pairs), tensor3_kernel (order 3, one accumulator per
+// class, described first below), tensor2x_kernel (order 2, classes that
+// pack, CTA pairs) and tensor2_kernel (order 2, per class).
 //
 // For one-hot data the 8 core cells of a combination (i, j, l) -- genotypes
 // x, y, z in {0, 1} -- are dot products over the samples of one class:
@@ -558,60 +562,110 @@ __global__ void __launch_bounds__(kT3Threads, 1)
 }
 
 // ---------------------------------------------------------------------------
-// Packed-class kernel.  When both classes fit one FP32 accumulator -- control
+// Packed classes.  When both classes fit one FP32 accumulator -- control
 // samples weighted by W = 4^h: the operand planes hold 2^h instead of 1.0 in
 // the control region, every control product is 2^h * 2^h = W, and an
 // accumulator holds cases + W * controls, exact while n_cases < W and
 // n_cases + W * n_ctrls < 2^24 -- an item needs one tensor-memory region of
-// N columns instead of two.  N = 256 (128 l per item; the M 128 x K 32 MMA
-// costs the same for every N up to 256) and two regions alternate between
-// items, so the next item's GEMM runs while the epilogue reads the last one.
-// A is built in shared memory (tensor memory is full) by six producer warps,
-// 3 stages.
+// N columns instead of two.  N = 256 (128 l per item; the MMA costs the same
+// for every N up to 256) and two regions alternate between items, so the next
+// item's GEMM runs while the epilogue reads the last one.  A is built in
+// shared memory (tensor memory is full) by six producer warps.
 constexpr int kPL = 128, kPN = 2 * kPL;                  // 128 l, N 256
 constexpr int kPBuildWarps = 6;                           // producer warps (the A build is on the critical path)
 constexpr int kPThreads = 32 * (2 + kPBuildWarps + kT3EpiWarps);  // 512: 128 registers fill the register file
-constexpr int kPStages = 3;
-constexpr int kPSB = kPN * kT3KB;                         // 32 KB  l rows
 constexpr int kPSA = kT3M * kT3KB;                        // 16 KB  (i,j) rows, 128-byte swizzle
-constexpr int kPStage = kPSB + kPSA + kT3SJ + kT3SI;      // 57 KB, a multiple of 1 KB
-constexpr size_t kPSmem = 1024 + (size_t)kPStages * kPStage + (size_t)kT3EpiWarps * kT3Ebuf + 2 * kPL * 16;
-constexpr uint32_t kPIdesc = (1u << 4) | ((uint32_t)(kPN >> 3) << 17) | ((uint32_t)(kT3M >> 4) << 24);
-static_assert(kPSmem <= 227 * 1024 - 256, "packed tensor kernel shared memory");
 static_assert(2 * kPN <= 512, "packed tensor kernel tensor memory");
 
-__global__ void __launch_bounds__(kPThreads, 1)
-    tensor3p_kernel(const __grid_constant__ T3Maps maps, ScanWork w, const long long* __restrict__ item_begin,
-                    long long g0, long long g1, int k_cases, int pack, CandSink sink, float thr_f, uint32_t* dump,
-                    const uint32_t* __restrict__ single, const uint4* __restrict__ pairs, int* status) {
+// ---------------------------------------------------------------------------
+// Packed-class order-3 kernel on CTA pairs.  A cluster of two CTAs (the two
+// SMs of a TPC) runs one GEMM of M 256 x N 256 per work item (i, 64 j, 128 l)
+// with tcgen05.mma.cta_group::2: CTA r builds the A tile of its 32 j
+// (j0 + 32 r ..) in its own shared memory and stages half r of the l rows
+// (64 l x 2 rows); CTA 0 issues the MMAs, which read both CTAs' shared memory
+// and leave each CTA's 128 accumulator rows -- its own (j, x, y) rows x the
+// item's 256 (l, z) columns -- in its own tensor memory.  The shared memory
+// of an SM then takes 82 instead of 114 KB per 128-sample stage (the l-row
+// TMA writes and MMA operand reads halve; the single-CTA kernel keeps the
+// SM's shared memory at its bank limit), and 4 stages of 41 KB fit.  (Split
+// into a 5-slot TMA ring and a 3-slot A ring it ran 18 % slower: the A build
+// then has too little slack.)
+// Handover: each CTA's TMA completes on its own `full_t`; its producer warps
+// build A once their rows landed and arrive on CTA 0's `full_a` (12 arrivals:
+// both CTAs' rows and A tiles are then in place); the MMA commits go to both
+// CTAs' `empty`, `acc_full` and `done`; both CTAs' epilogue warps arrive on
+// CTA 0's `acc_empty` (16 arrivals).  Every wait is bounded; both CTAs meet
+// at a cluster barrier before tensor memory is released.
+constexpr int kPxJ = 2 * kT3J;                                     // 64 j per pair item
+constexpr int kPxStages = 4;
+constexpr int kPxBRows = kPN / 2;                                  // this CTA's l rows (64 l x 2)
+constexpr int kPxSB = kPxBRows * kT3KB;                            // 16 KB
+constexpr int kPxStage = kPxSB + kPSA + kT3SJ + kT3SI;             // 41 KB, a multiple of 1 KB
+constexpr size_t kPxSmem = 1024 + (size_t)kPxStages * kPxStage + (size_t)kT3EpiWarps * kT3Ebuf + 2 * kPL * 16;
+constexpr uint32_t kPxIdesc = (1u << 4) | ((uint32_t)(kPN >> 3) << 17) | ((uint32_t)((2 * kT3M) >> 4) << 24);
+static_assert(kPxSmem <= 227 * 1024 - 256, "paired order-3 tensor kernel shared memory");
+
+// Pair items of one i: J-tile a starts at j0 = i+1+64a and has
+// ceil((n-1-j0)/128) L-tiles starting at l0 = j0+1+128b.
+__device__ __forceinline__ void t3x_decode(const long long* __restrict__ item_begin, int n, long long g, int& i,
+                                           int& j0, int& l0) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (item_begin[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    i = lo;
+    long long q = g - item_begin[i];
+    for (int a = 0;; ++a) {
+        const int j = i + 1 + kPxJ * a;
+        const long long nl = (n - 1 - j + kPL - 1) / kPL;
+        if (q < nl) {
+            j0 = j;
+            l0 = j + 1 + kPL * (int)q;
+            return;
+        }
+        q -= nl;
+    }
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
+    tensor3x_kernel(const __grid_constant__ T3Maps maps, const __grid_constant__ CUtensorMap map_lh, ScanWork w,
+                    const long long* __restrict__ item_begin, long long g0, long long g1, int k_cases, int pack,
+                    CandSink sink, float thr_f, uint32_t* dump, const uint32_t* __restrict__ single,
+                    const uint4* __restrict__ pairs, int* status) {
     extern __shared__ uint8_t smraw[];
-    __shared__ __align__(8) uint64_t full_t[kPStages], full_a[kPStages], empty[kPStages];
+    __shared__ __align__(8) uint64_t full_t[kPxStages], full_a[kPxStages], empty[kPxStages];
     __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);  // stages: B | A | j rows | i rows
-    uint32_t* ebuf_all = reinterpret_cast<uint32_t*>(sm + kPStages * kPStage);
+    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);  // stages: B half | A | j | i
+    uint32_t* ebuf_all = reinterpret_cast<uint32_t*>(sm + kPxStages * kPxStage);
     volatile int* abort = &abort_flag;
     const DevData& d = w.d;
     const int n = d.snps;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ks_c = k_cases / kT3KB;
     const int ksteps = ks_c + (d.tw + 1) / 2;
+    const uint32_t rank = cluster_rank();  // 0 issues the MMAs
+    const long long cid = cluster_id(), ncl = cluster_count();
 
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(512));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
     }
     if (tid == 0) {
-        for (int s = 0; s < kPStages; ++s) {
+        for (int s = 0; s < kPxStages; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full_t[s])));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_a[s])), "r"(kPBuildWarps));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full_a[s])),
+                         "r"(2 * kPBuildWarps));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
         }
         for (int b = 0; b < 2; ++b) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[b])), "r"(kT3EpiWarps));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[b])),
+                         "r"(2 * kT3EpiWarps));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
         asm volatile("fence.mbarrier_init.release.cluster;");
@@ -619,105 +673,106 @@ __global__ void __launch_bounds__(kPThreads, 1)
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+    cluster_sync_all();  // both CTAs' barriers exist before either signals the other
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
     bool ok = true;
 
     if (warp == 0) {
-        // ---------------------------------------------------------------- TMA producer
+        // ---------------------------------------------------------------- TMA producer (both CTAs)
         if (lane == 0) {
             long long step = 0;
-            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+            for (long long g = g0 + cid; g < g1 && ok; g += ncl) {
                 int i, j0, l0;
-                t3_decode<kPL>(item_begin, n, g, i, j0, l0);
+                t3x_decode(item_begin, n, g, i, j0, l0);
                 for (int ks = 0; ks < ksteps; ++ks) {
-                    const int s = (int)(step % kPStages);
-                    const long long u = step / kPStages;
-                    if (u > 0 && !t3_wait(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
+                    const int s = (int)(step % kPxStages);
+                    const long long u = step / kPxStages;
+                    if (u > 0 && !t3_wait_cl(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
                         ok = false;
                         break;
                     }
                     const int k0 = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
-                    uint8_t* st = sm + s * kPStage;
+                    uint8_t* st = sm + s * kPxStage;
                     const uint32_t bar = smem_u32(&full_t[s]);
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                                 "r"((uint32_t)(kPSB + kT3SJ + 2 * kT3KB))
+                                 "r"((uint32_t)(kPxSB + kT3SJ + 2 * kT3KB))
                                  : "memory");
-                    t3_tma(smem_u32(st), &maps.l, k0, 2 * l0, bar);
-                    t3_tma(smem_u32(st + kPSB + kPSA), &maps.j, k0, 2 * j0, bar);
-                    t3_tma(smem_u32(st + kPSB + kPSA + kT3SJ), &maps.i, k0, 2 * i, bar);
+                    t3_tma(smem_u32(st), &map_lh, k0, 2 * l0 + kPxBRows * (int)rank, bar);
+                    t3_tma(smem_u32(st + kPxSB + kPSA), &maps.j, k0, 2 * (j0 + kT3J * (int)rank), bar);
+                    t3_tma(smem_u32(st + kPxSB + kPSA + kT3SJ), &maps.i, k0, 2 * i, bar);
                     ++step;
                 }
             }
-            for (int s = 0; s < kPStages; ++s) {
+            for (int s = 0; s < kPxStages; ++s) {
                 if (step <= s) continue;
-                const long long last = s + ((step - 1 - s) / kPStages) * kPStages;
-                if (!t3_drain(smem_u32(&full_t[s]), (uint32_t)((last / kPStages) & 1))) ok = false;
+                const long long last = s + ((step - 1 - s) / kPxStages) * kPxStages;
+                if (!t3_drain(smem_u32(&full_t[s]), (uint32_t)((last / kPxStages) & 1))) ok = false;
             }
         }
     } else if (warp == 1) {
-        // ---------------------------------------------------------------- MMA issuer
-        if (lane == 0) {
+        // ---------------------------------------------------------------- MMA issuer (CTA 0)
+        if (lane == 0 && rank == 0) {
             long long step = 0, item = 0;
-            for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+            for (long long g = g0 + cid; g < g1 && ok; g += ncl, ++item) {
                 const int buf = (int)(item & 1);
-                if (item >= 2 && !t3_wait(smem_u32(&acc_empty[buf]), (uint32_t)(((item >> 1) - 1) & 1), abort)) {
+                if (item >= 2 && !t3_wait_cl(smem_u32(&acc_empty[buf]), (uint32_t)(((item >> 1) - 1) & 1), abort)) {
                     ok = false;
                     break;
                 }
                 const uint32_t dcol = tmem + (uint32_t)(kPN * buf);
                 for (int ks = 0; ks < ksteps; ++ks, ++step) {
-                    const int s = (int)(step % kPStages);
-                    if (!t3_wait(smem_u32(&full_a[s]), (uint32_t)((step / kPStages) & 1), abort)) {
+                    const int s = (int)(step % kPxStages);
+                    // both CTAs' rows landed and both A tiles are built
+                    if (!t3_wait_cl(smem_u32(&full_a[s]), (uint32_t)((step / kPxStages) & 1), abort)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const uint32_t sb = smem_u32(sm + s * kPStage), sa = sb + kPSB;
+                    const uint32_t sb = smem_u32(sm + s * kPxStage), sa = sb + kPxSB;
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk) {
                         const uint64_t ad = t3_desc(sa + 32 * kk), bd = t3_desc(sb + 32 * kk);
                         const uint32_t acc = (ks == 0 && kk == 0) ? 0u : 1u;
                         asm volatile(
                             "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
-                            "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
-                            "l"(ad), "l"(bd), "r"(kPIdesc), "r"(acc));
+                            "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
+                            "l"(ad), "l"(bd), "r"(kPxIdesc), "r"(acc));
                     }
-                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                        smem_u32(&empty[s])));
+                    commit_pair(smem_u32(&empty[s]));
                 }
                 if (!ok) break;
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                    smem_u32(&acc_full[buf])));
+                commit_pair(smem_u32(&acc_full[buf]));
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_u32(&done)));
-            if (!t3_drain(smem_u32(&done), 0)) ok = false;
+            commit_pair(smem_u32(&done));
         }
+        // neither CTA releases shared or tensor memory before the pair's MMAs are done
+        if (lane == 0 && !t3_drain_cl(smem_u32(&done), 0)) ok = false;
     } else if (warp < 2 + kPBuildWarps) {
-        // ---------------------------------------------------------------- A builders (shared memory)
-        const int t = tid - 64;  // 0 .. 32 * kPBuildWarps - 1
-        const int c = t & 7;     // 16-byte chunk; 8 consecutive threads cover one 128-byte row
+        // ---------------------------------------------------------------- A builders (both CTAs)
+        const int t = tid - 64;
+        const int c = t & 7;
+        uint32_t full_a0[kPxStages];
+#pragma unroll
+        for (int s = 0; s < kPxStages; ++s) full_a0[s] = cluster_addr(smem_u32(&full_a[s]), 0);
         long long step = 0;
-        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
+        for (long long g = g0 + cid; g < g1 && ok; g += ncl) {
             for (int ks = 0; ks < ksteps; ++ks, ++step) {
-                const int s = (int)(step % kPStages);
-                if (!t3_wait(smem_u32(&full_t[s]), (uint32_t)((step / kPStages) & 1), abort)) {
+                const int s = (int)(step % kPxStages);
+                if (!t3_wait(smem_u32(&full_t[s]), (uint32_t)((step / kPxStages) & 1), abort)) {
                     ok = false;
                     break;
                 }
-                uint8_t* st = sm + s * kPStage;
-                uint8_t* sA = st + kPSB;
+                uint8_t* st = sm + s * kPxStage;
+                uint8_t* sA = st + kPxSB;
                 const uint8_t* sJ = sA + kPSA;
                 const uint8_t* sI = sJ + kT3SJ;
-                // every load of the stage first, then the ANDs and stores: the loads
-                // overlap instead of waiting one by one behind the stores
                 const uint4 i0 = *reinterpret_cast<const uint4*>(sI + (c << 4));
                 const uint4 i1 = *reinterpret_cast<const uint4*>(sI + 128 + ((c ^ 1) << 4));
                 constexpr int kRows = (2 * kT3J + 4 * kPBuildWarps - 1) / (4 * kPBuildWarps);
                 uint4 jrow[kRows];
 #pragma unroll
-                for (int u = 0; u < kRows; ++u) {  // j row r = (jj, y)
+                for (int u = 0; u < kRows; ++u) {
                     const int r = (t >> 3) + 4 * kPBuildWarps * u;
                     if (r < 2 * kT3J) jrow[u] = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((c ^ (r & 7)) << 4));
                 }
@@ -726,7 +781,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
                     const int r = (t >> 3) + 4 * kPBuildWarps * u;
                     if (r >= 2 * kT3J) break;
                     const uint4 jv = jrow[u];
-                    const int m0 = 4 * (r >> 1) + (r & 1), m1 = m0 + 2;  // A rows (jj, x, y), x = 0, 1
+                    const int m0 = 4 * (r >> 1) + (r & 1), m1 = m0 + 2;
                     uint4 v;
                     v.x = jv.x & i0.x;
                     v.y = jv.y & i0.y;
@@ -741,28 +796,29 @@ __global__ void __launch_bounds__(kPThreads, 1)
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
-                if (lane == 0)
-                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full_a[s])) : "memory");
+                if (lane == 0) arrive_cl(full_a0[s]);
             }
         }
     } else {
-        // ---------------------------------------------------------------- epilogue
-        const int e = warp - (2 + kPBuildWarps);  // 0..7
-        const int q = warp & 3;                    // tensor-memory lane quarter this warp may access
-        const int hh = e >> 2;                     // column groups 2 cc + hh (see the loop below)
+        // ---------------------------------------------------------------- epilogue (both CTAs)
+        const int e = warp - (2 + kPBuildWarps);
+        const int q = warp & 3;
+        const int hh = e >> 2;
         uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
         const uint32_t wmask = (1u << pack) - 1u;
         const int jl = lane >> 2, xy = lane & 3, kp = lane & 3;
-        const int et = tid - 32 * (2 + kPBuildWarps);  // 0 .. 255
-        // the item's pair cores (i, l) and single cores of l, staged once per item
+        const int et = tid - 32 * (2 + kPBuildWarps);
+        const uint32_t acc_empty0[2] = {cluster_addr(smem_u32(&acc_empty[0]), 0),
+                                        cluster_addr(smem_u32(&acc_empty[1]), 0)};
         uint4* stage = reinterpret_cast<uint4*>(ebuf_all + kT3EpiWarps * (kT3Ebuf / 4));
         long long item = 0;
-        for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
+        for (long long g = g0 + cid; g < g1 && ok; g += ncl, ++item) {
             int i, j0, l0;
-            t3_decode<kPL>(item_begin, n, g, i, j0, l0);
+            t3x_decode(item_begin, n, g, i, j0, l0);
+            j0 += kT3J * (int)rank;
             const int buf = (int)(item & 1);
-            asm volatile("bar.sync 1, %0;" ::"n"(32 * kT3EpiWarps) : "memory");  // last item's readers done
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * kT3EpiWarps) : "memory");
             {
                 const int ll = et & (kPL - 1), l = l0 + ll;
                 if (l < n) {
@@ -776,24 +832,19 @@ __global__ void __launch_bounds__(kPThreads, 1)
             uint4 pij;
             float si[2][2], sj[2][2];
             t3_item_consts(single, pairs, i, j, n, j_ok, pij, si, sj);
-            if (!t3_wait(smem_u32(&acc_full[buf]), (uint32_t)((item >> 1) & 1), abort)) {
+            if (!t3_wait_cl(smem_u32(&acc_full[buf]), (uint32_t)((item >> 1) & 1), abort)) {
                 ok = false;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
             for (int cc = 0; cc < 8; ++cc) {
-                // column group 2 cc + hh: l offsets 16 cc + 8 hh + [0, 8) (the two warps of a
-                // lane quarter interleave over the item's l range); a group without a valid
-                // combination for this warp is skipped, the region still released
                 const int lg = l0 + 16 * cc + 8 * hh;
                 if (!__any_sync(0xffffffffu, j_ok && lg + 7 > j && lg < n)) {
                     if (cc == 7) {
                         asm volatile("tcgen05.fence::before_thread_sync;");
                         __syncwarp();
-                        if (lane == 0)
-                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
-                                         : "memory");
+                        if (lane == 0) arrive_cl(acc_empty0[buf]);
                     }
                     continue;
                 }
@@ -808,12 +859,10 @@ __global__ void __launch_bounds__(kPThreads, 1)
                           "=r"(v[14]), "=r"(v[15])
                         : "r"(lane_base + col));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    if (cc == 7) {  // last read of this item's accumulators: the region is free
+                    if (cc == 7) {
                         asm volatile("tcgen05.fence::before_thread_sync;");
                         __syncwarp();
-                        if (lane == 0)
-                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
-                                         : "memory");
+                        if (lane == 0) arrive_cl(acc_empty0[buf]);
                     }
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
@@ -835,8 +884,10 @@ __global__ void __launch_bounds__(kPThreads, 1)
     if (!ok) *abort = 1;
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+    cluster_sync_all();  // the other CTA is done with this CTA's shared and tensor memory
+    asm volatile("tcgen05.fence::after_thread_sync;");
     if (tid == 0 && abort_flag) atomicOr(status, 1);
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
 // ---------------------------------------------------------------------------
@@ -1211,6 +1262,274 @@ __global__ void __launch_bounds__(kT2Threads, 1)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
+// ---------------------------------------------------------------------------
+// Order 2 on CTA pairs.  A cluster of two CTAs (the two SMs of a TPC) runs one
+// GEMM D[(i,x), (j,y)] of M 256 x N 256 per work item with
+// tcgen05.mma.cta_group::2: CTA r stages its own A tile (64 i x 2 rows, i-tile
+// 2p + r of the band) and half r of the B tile (64 j x 2 rows); CTA 0 issues
+// the MMAs, which read both CTAs' shared memory and leave each CTA's 128
+// accumulator rows in its own tensor memory.  Per SM a stage then moves 32
+// instead of 48 KB through shared memory (TMA writes and MMA operand reads of
+// B halve), which is what bounded the single-CTA kernel.
+// Handover: CTA 0's `full` barriers take one arrival with the transaction
+// bytes of both CTAs' copies (CTA 1's copies complete on them through the
+// .cta_group::2 TMA form); the MMA commits go to both CTAs' `empty`,
+// `acc_full` and `done`; both CTAs' epilogue warps arrive on CTA 0's
+// `acc_empty` (16 arrivals).  Every wait is bounded as in the other kernels;
+// both CTAs meet at a cluster barrier before tensor memory is released.
+constexpr int kT2xStages = 5;
+constexpr int kT2xSA = kT2M * kT3KB;        // 16 KB: this CTA's 64 i x 2 rows
+constexpr int kT2xSB = kT2M * kT3KB;        // 16 KB: this CTA's half of the 128 j x 2 rows
+constexpr int kT2xStage = kT2xSA + kT2xSB;  // 32 KB
+constexpr size_t kT2xSmem = 1024 + (size_t)kT2xStages * kT2xStage + (size_t)kT3EpiWarps * kT3Ebuf;
+constexpr uint32_t kT2xIdesc = (1u << 4) | ((uint32_t)(kT2N >> 3) << 17) | ((uint32_t)((2 * kT2M) >> 4) << 24);
+static_assert(kT2xSmem <= 227 * 1024 - 256, "paired order-2 tensor kernel shared memory");
+
+// Pair items: band r (i-tiles [8 r, 8 r + 8), j-tiles b >= 4 r) lists, j-tile by
+// j-tile, its i-tile pairs (2 p, 2 p + 1); i0 = first i of the pair.
+__device__ __forceinline__ void t2x_decode(const long long* __restrict__ item_begin, int n_itiles, long long g,
+                                           int& i0, int& j0) {
+    const int n_bands = (n_itiles + kT2Band - 1) / kT2Band;
+    int lo = 0, hi = n_bands - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (item_begin[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    const int ca = min(kT2Band, n_itiles - kT2Band * lo);
+    const int cp = (ca + 1) >> 1;  // i-tile pairs in the band
+    const long long idx = g - item_begin[lo];
+    const int b = kT2Band * kT2I / kT2L * lo + (int)(idx / cp);
+    i0 = kT2I * (kT2Band * lo + 2 * (int)(idx % cp));
+    j0 = kT2L * b;
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kT2Threads, 1)
+    tensor2x_kernel(const __grid_constant__ T2Maps maps, ScanWork w, const long long* __restrict__ item_begin,
+                    int n_itiles, long long g0, long long g1, int k_cases, int pack, CandSink sink, float thr_f,
+                    uint32_t* dump, const uint32_t* __restrict__ single, int* status) {
+    extern __shared__ uint8_t smraw[];
+    __shared__ __align__(8) uint64_t full[kT2xStages], empty[kT2xStages];
+    __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);  // stages: A | B half
+    uint32_t* ebuf_all = reinterpret_cast<uint32_t*>(sm + kT2xStages * kT2xStage);
+    volatile int* abort = &abort_flag;
+    const DevData& d = w.d;
+    const int n = d.snps;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ks_c = k_cases / kT3KB;
+    const int ksteps = ks_c + (d.tw + 1) / 2;
+    const int nbuf = pack ? 2 : 1;
+    const uint32_t rank = cluster_rank();  // 0 issues the MMAs
+    const long long cid = cluster_id(), ncl = cluster_count();
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kT2xStages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[b])),
+                         "r"(2 * kT3EpiWarps));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        abort_flag = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    cluster_sync_all();  // both CTAs' barriers exist before either signals the other
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+
+    if (warp == 0) {
+        // ---------------------------------------------------------------- TMA producer (both CTAs)
+        if (lane == 0) {
+            long long step = 0;
+            for (long long g = g0 + cid; g < g1 && ok; g += ncl) {
+                int i0, j0;
+                t2x_decode(item_begin, n_itiles, g, i0, j0);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const int s = (int)(step % kT2xStages);
+                    const long long u = step / kT2xStages;
+                    if (u > 0 && !t3_wait_cl(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    const int k0 = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
+                    uint8_t* st = sm + s * kT2xStage;
+                    const uint32_t bar = cluster_addr(smem_u32(&full[s]), 0);
+                    if (rank == 0)
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&full[s])),
+                                     "r"((uint32_t)(2 * kT2xStage))
+                                     : "memory");
+                    t3_tma_pair(smem_u32(st), &maps.a, k0, 2 * (i0 + kT2I * (int)rank), bar);
+                    t3_tma_pair(smem_u32(st + kT2xSA), &maps.a, k0, 2 * j0 + kT2M * (int)rank, bar);
+                    ++step;
+                }
+            }
+            // copies in flight land before the pair is released: CTA 0 sees every copy of
+            // both CTAs complete on its `full` barriers, CTA 1 sees its stages consumed
+            for (int s = 0; s < kT2xStages; ++s) {
+                if (step <= s) continue;
+                const long long last = s + ((step - 1 - s) / kT2xStages) * kT2xStages;
+                const uint32_t par = (uint32_t)((last / kT2xStages) & 1);
+                if (!(rank == 0 ? t3_drain_cl(smem_u32(&full[s]), par) : t3_drain_cl(smem_u32(&empty[s]), par)))
+                    ok = false;
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------------------------------------------------------- MMA issuer (CTA 0)
+        if (lane == 0 && rank == 0) {
+            long long step = 0, item = 0;
+            for (long long g = g0 + cid; g < g1 && ok; g += ncl, ++item) {
+                const int buf = (int)(item % nbuf);
+                if (item >= nbuf &&
+                    !t3_wait_cl(smem_u32(&acc_empty[buf]), (uint32_t)(((item / nbuf) - 1) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                for (int ks = 0; ks < ksteps; ++ks, ++step) {
+                    const int s = (int)(step % kT2xStages);
+                    if (!t3_wait_cl(smem_u32(&full[s]), (uint32_t)((step / kT2xStages) & 1), abort)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t sa = smem_u32(sm + s * kT2xStage), sb = sa + kT2xSA;
+                    const int cls = ks >= ks_c;
+                    const uint32_t dcol = tmem + (uint32_t)(pack ? kT2N * buf : kT2N * cls);
+                    const bool first = pack ? ks == 0 : (ks == 0 || ks == ks_c);
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint64_t ad = t3_desc(sa + 32 * kk), bd = t3_desc(sb + 32 * kk);
+                        const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+                        asm volatile(
+                            "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
+                            "l"(ad), "l"(bd), "r"(kT2xIdesc), "r"(acc));
+                    }
+                    commit_pair(smem_u32(&empty[s]));
+                }
+                if (!ok) break;
+                commit_pair(smem_u32(&acc_full[buf]));
+            }
+            commit_pair(smem_u32(&done));
+        }
+        // neither CTA releases shared or tensor memory before the pair's MMAs are done
+        if (lane == 0 && !t3_drain_cl(smem_u32(&done), 0)) ok = false;
+    } else {
+        // ---------------------------------------------------------------- epilogue (both CTAs)
+        const int e = warp - 2;
+        const int q = warp & 3;
+        const int hh = e >> 2;
+        uint32_t* ebuf = ebuf_all + e * (kT3Ebuf / 4);
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+        const uint32_t wmask = pack ? (1u << pack) - 1u : 0xffffffffu;
+        const int ii = lane >> 1, x = lane & 1, kh = lane & 1;
+        const uint32_t acc_empty0[2] = {cluster_addr(smem_u32(&acc_empty[0]), 0),
+                                        cluster_addr(smem_u32(&acc_empty[1]), 0)};
+        long long item = 0;
+        for (long long g = g0 + cid; g < g1 && ok; g += ncl, ++item) {
+            int i0, j0;
+            t2x_decode(item_begin, n_itiles, g, i0, j0);
+            i0 += kT2I * (int)rank;
+            const int buf = (int)(item % nbuf);
+            const int i = i0 + 16 * q + ii;
+            const bool i_ok = i < n;
+            float si[2][2];
+            {
+                uint4 a = make_uint4(0, 0, 0, 0);
+                if (i_ok) a = __ldg(reinterpret_cast<const uint4*>(single) + i);
+                si[0][0] = u2f(a.x);
+                si[0][1] = u2f(a.y);
+                si[1][0] = u2f(a.z);
+                si[1][1] = u2f(a.w);
+            }
+            if (!t3_wait_cl(smem_u32(&acc_full[buf]), (uint32_t)((item / nbuf) & 1), abort)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll 1
+            for (int cc = 0; cc < 8; ++cc) {
+                const int jg = j0 + 16 * cc + 8 * hh;
+                if (!__any_sync(0xffffffffu, i_ok && jg + 7 > i && jg < n)) {
+                    if (cc == 7) {
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0) arrive_cl(acc_empty0[buf]);
+                    }
+                    continue;
+                }
+                const int jl = jg + (lane & 7);
+                const uint4 sjp = jl < n ? __ldg(reinterpret_cast<const uint4*>(single) + jl) : make_uint4(0, 0, 0, 0);
+                {
+                    const uint32_t col = (uint32_t)((pack ? kT2N * buf : 0) + 32 * cc + 16 * hh);
+                    uint32_t v[16], vt[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
+                        "15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(lane_base + col));
+                    if (!pack)
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%"
+                            "14,%15}, [%16];"
+                            : "=r"(vt[0]), "=r"(vt[1]), "=r"(vt[2]), "=r"(vt[3]), "=r"(vt[4]), "=r"(vt[5]),
+                              "=r"(vt[6]), "=r"(vt[7]), "=r"(vt[8]), "=r"(vt[9]), "=r"(vt[10]), "=r"(vt[11]),
+                              "=r"(vt[12]), "=r"(vt[13]), "=r"(vt[14]), "=r"(vt[15])
+                            : "r"(lane_base + (uint32_t)kT2N + col));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (cc == 7) {
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncwarp();
+                        if (lane == 0) arrive_cl(acc_empty0[buf]);
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        uint4 c4;
+                        if (pack) {
+                            const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * k]));
+                            const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * k + 1]));
+                            c4 = make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                        } else {
+                            c4 = make_uint4(f2u(__uint_as_float(v[2 * k])), f2u(__uint_as_float(v[2 * k + 1])),
+                                            f2u(__uint_as_float(vt[2 * k])), f2u(__uint_as_float(vt[2 * k + 1])));
+                        }
+                        *reinterpret_cast<uint4*>(ebuf + 4 * t2_chunk(ii, k, x)) = c4;
+                    }
+                }
+                __syncwarp();
+#pragma unroll 1
+                for (int kk = 0; kk < 4; ++kk) {
+                    const int k = 4 * kh + kk;
+                    t2_eval(w, sink, thr_f, dump, sjp, ebuf, ii, k, i, jg + k, i_ok, si, lane);
+                }
+                __syncwarp();
+            }
+        }
+    }
+    if (!ok) *abort = 1;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    cluster_sync_all();  // the other CTA is done with this CTA's shared and tensor memory
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && abort_flag) atomicOr(status, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
 // Operand planes: one thread per 16 output bytes (16 samples of one row).
 __global__ void t3_planes_kernel(DevData d, uint8_t* planes, int pitch, int k_cases, uint32_t ctrl_byte) {
     const long long chunks = (long long)pitch / 16;
@@ -1259,13 +1578,31 @@ static long long t2_items(int n, std::vector<long long>& item_begin, int& n_itil
     return total;
 }
 
-// Items per i (host): prefix sums item_begin[0..n], item_begin[n] = total.
-static long long t3_items(int n, int L, std::vector<long long>& item_begin) {
+// Pair items of tensor2x_kernel (host): prefix sums over the bands of t2x_decode.
+static long long t2x_items(int n, std::vector<long long>& item_begin, int& n_itiles) {
+    n_itiles = std::max(1, (n - 1 + kT2I - 1) / kT2I);
+    const int n_bands = (n_itiles + kT2Band - 1) / kT2Band;
+    const int nb = (n + kT2L - 1) / kT2L;
+    item_begin.assign((size_t)n_bands + 1, 0);
+    long long total = 0;
+    for (int r = 0; r < n_bands; ++r) {
+        item_begin[r] = total;
+        const int ca = std::min(kT2Band, n_itiles - kT2Band * r);
+        const int b0 = kT2Band * kT2I / kT2L * r;
+        if (nb > b0) total += (long long)((ca + 1) / 2) * (nb - b0);
+    }
+    item_begin[n_bands] = total;
+    return total;
+}
+
+// Items per i (host): prefix sums item_begin[0..n], item_begin[n] = total;
+// J j per item (kT3J, or kPxJ for the pair items of tensor3x_kernel).
+static long long t3_items(int n, int L, std::vector<long long>& item_begin, int J = kT3J) {
     item_begin.assign((size_t)n + 1, 0);
     long long total = 0;
     for (int i = 0; i < n; ++i) {
         item_begin[i] = total;
-        for (int j = i + 1; j < n - 1; j += kT3J) total += (n - 1 - j + L - 1) / L;
+        for (int j = i + 1; j < n - 1; j += J) total += (n - 1 - j + L - 1) / L;
     }
     item_begin[n] = total;
     return total;
@@ -1312,11 +1649,14 @@ int tensor_pack(int n_cases, int n_ctrls) {
 cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
     plan.pack = tensor_pack(d.n_cases, d.n_ctrls);
     const int L = plan.pack ? kPL : kT3L;
-    plan.item_combos = kT3J * L / 2.0;
+    // packed classes: CTA-pair items
+    plan.pair3 = plan.pack != 0;
+    const int J = plan.pair3 ? kPxJ : kT3J;
+    plan.item_combos = J * L / 2.0;
     plan.k_cases = kT3KB * ((d.cw + 1) / 2);
     plan.pitch = plan.k_cases + kT3KB * ((d.tw + 1) / 2);
     std::vector<long long> ib;
-    plan.total = t3_items(d.snps, L, ib);
+    plan.total = t3_items(d.snps, L, ib, J);
     cudaError_t e = cudaMalloc((void**)&plan.item_begin, ib.size() * sizeof(long long));
     if (e == cudaSuccess) e = cudaMemcpy(plan.item_begin, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc((void**)&plan.planes, (size_t)2 * d.snps * plan.pitch);
@@ -1332,9 +1672,11 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
         return e;
     if ((e = t3_map(&plan.map_j, plan.planes, rows, plan.pitch, 2 * kT3J, true)) != cudaSuccess) return e;
     if ((e = t3_map(&plan.map_i, plan.planes, rows, plan.pitch, 2, true)) != cudaSuccess) return e;
-    // order 2
+    // order 2: CTA-pair items when the classes pack (per class the MMA waits for the epilogue between
+    // items, and the single-CTA kernel measured 2 % faster there)
     std::vector<long long> ib2;
-    plan.total2 = t2_items(d.snps, ib2, plan.n_itiles);
+    plan.pair2 = plan.pack != 0;
+    plan.total2 = plan.pair2 ? t2x_items(d.snps, ib2, plan.n_itiles) : t2_items(d.snps, ib2, plan.n_itiles);
     plan.item2_combos = (double)d.snps * (d.snps - 1) / 2 / std::max(1ll, plan.total2);
     e = cudaMalloc((void**)&plan.item2_begin, ib2.size() * sizeof(long long));
     if (e == cudaSuccess)
@@ -1469,6 +1811,29 @@ cudaError_t probe_lg2_error(unsigned max_c, double* max_abs_err, cudaStream_t s)
     return e;
 }
 
+// Clusters of two CTAs of a pair kernel that fit on the device at once (a TPC
+// each); 0 when the occupancy query is not available.
+template <class K>
+static int pair_clusters(K* kernel, int threads, size_t smem) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(2, 1, 1);
+    cfg.blockDim = dim3(threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int c = 0;
+    if (cudaOccupancyMaxActiveClusters(&c, kernel, &cfg) != cudaSuccess || c < 1) {
+        cudaGetLastError();
+        c = 0;
+    }
+    return c;
+}
+
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
                            uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
                            int* status, cudaStream_t s, int sms) {
@@ -1479,9 +1844,11 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     static const cudaError_t attr = [] {
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(tensor3p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPSmem);
-        if (e == cudaSuccess)
             e = cudaFuncSetAttribute(tensor2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2Smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tensor2x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2xSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tensor3x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPxSmem);
         return e;
     }();
     if (attr != cudaSuccess) return attr;
@@ -1491,6 +1858,16 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     const double thr = ((double)sink.thr - (double)w.base_key) * scale - t3_margin(w.d.n_cases + w.d.n_ctrls);
     const float thr_f = (float)std::max(-3.0e38, std::min(3.0e38, thr));
     const unsigned grid = (unsigned)(items < sms ? items : sms);
+    if (w.order == 2 && plan.pair2) {
+        static const int max_clusters = pair_clusters(tensor2x_kernel, kT2Threads, kT2xSmem);
+        const long long clusters = std::min<long long>(items, max_clusters > 0 ? max_clusters : sms / 2);
+        T2Maps maps2{plan.map_a2, plan.map_b2};
+        tensor2x_kernel<<<(unsigned)(2 * std::max(1ll, clusters)), kT2Threads, kT2xSmem, s>>>(
+            maps2, w, plan.item2_begin, plan.n_itiles, g0, g1, plan.k_cases, plan.pack, sink, thr_f, dump, single,
+            status);
+        count_launch();
+        return cudaGetLastError();
+    }
     if (w.order == 2) {
         T2Maps maps2{plan.map_a2, plan.map_b2};
         tensor2_kernel<<<grid, kT2Threads, kT2Smem, s>>>(maps2, w, plan.item2_begin, plan.n_itiles, g0, g1,
@@ -1499,12 +1876,17 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
         return cudaGetLastError();
     }
     T3Maps maps{plan.map_l, plan.map_j, plan.map_i};
-    if (plan.pack)
-        tensor3p_kernel<<<grid, kPThreads, kPSmem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, plan.pack,
-                                                          sink, thr_f, dump, single, pairs, status);
-    else
-        tensor3_kernel<<<grid, kT3Threads, kT3Smem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, sink, thr_f,
-                                                         dump, single, pairs, status);
+    if (plan.pair3) {
+        static const int max_clusters = pair_clusters(tensor3x_kernel, kPThreads, kPxSmem);
+        const long long clusters = std::min<long long>(items, max_clusters > 0 ? max_clusters : sms / 2);
+        tensor3x_kernel<<<(unsigned)(2 * std::max(1ll, clusters)), kPThreads, kPxSmem, s>>>(
+            maps, plan.map_a2, w, plan.item_begin, g0, g1, plan.k_cases, plan.pack, sink, thr_f, dump, single, pairs,
+            status);
+        count_launch();
+        return cudaGetLastError();
+    }
+    tensor3_kernel<<<grid, kT3Threads, kT3Smem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, sink, thr_f,
+                                                     dump, single, pairs, status);
     count_launch();
     return cudaGetLastError();
 }

@@ -52,6 +52,82 @@ __device__ __forceinline__ bool t3_drain(uint32_t bar, uint32_t parity) {
     }
 }
 
+// ---- CTA pairs (cluster of two CTAs, tcgen05 cta_group::2) ----------------
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_id() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_count() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+    return r;
+}
+// Shared::cluster address of the variable at shared address `a` in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t a, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+// Every thread of both CTAs (release / acquire at cluster scope).
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ bool t3_try_cl(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p;}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// t3_wait for a barrier that the other CTA of the pair (or its MMA commits) completes.
+__device__ __forceinline__ bool t3_wait_cl(uint32_t bar, uint32_t parity, volatile int* abort) {
+    const unsigned long long t0 = t3_now();
+    for (;;) {
+        if (t3_try_cl(bar, parity)) return true;
+        if (*abort) return false;
+        if (t3_now() - t0 > kT3LimitNs) {
+            *abort = 1;
+            return false;
+        }
+    }
+}
+__device__ __forceinline__ bool t3_drain_cl(uint32_t bar, uint32_t parity) {
+    const unsigned long long t0 = t3_now();
+    for (;;) {
+        if (t3_try_cl(bar, parity)) return true;
+        if (t3_now() - t0 > kT3LimitNs) return false;
+    }
+}
+// Arrival on an mbarrier of either CTA of the pair (cluster address).
+__device__ __forceinline__ void arrive_cl(uint32_t cluster_bar) {
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(cluster_bar) : "memory");
+}
+// TMA tile load into this CTA's shared memory whose completion is counted on an
+// mbarrier of either CTA of the pair (cluster address).
+__device__ __forceinline__ void t3_tma_pair(uint32_t dst, const CUtensorMap* m, int x, int y, uint32_t cluster_bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, "
+        "{%2, %3}], [%4];" ::"r"(dst),
+        "l"((uint64_t)m), "r"(x), "r"(y), "r"(cluster_bar)
+        : "memory");
+}
+// Arrival, once the MMAs issued so far by this thread completed, on the mbarrier
+// at shared address `bar` of both CTAs of the pair.
+__device__ __forceinline__ void commit_pair(uint32_t bar) {
+    const uint16_t both = 3;
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+        "h"(both));
+}
+
 __device__ __forceinline__ void t3_tma(uint32_t dst, const CUtensorMap* m, int x, int y, uint32_t bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
