@@ -326,6 +326,7 @@ def run_gpu(args, spec):
                     "note": "algorithmic bytes = the data set read once per scan; the kernel is integer-pipe "
                             "bound (int_roofline)"}
     top = out[0] if out else None
+    planted_rank = planted_ranks(gs, res, ds, spec, planted) if ws == 1 else None
     cpu = cpu_sample(spec, ds, seconds=args.cpu_seconds) if args.cpu_seconds > 0 and ws == 1 else None
     batch = None if (args.no_batch or ws > 1) else run_batch_and_serve(args, gs, ctx)
     line = {
@@ -337,7 +338,8 @@ def run_gpu(args, spec):
                    "parallelism": "work-unit shards over %d rank(s)" % ws,
                    "l2": "flushed between steps (512 MB write); data set %.1f MB is L2-resident by design"
                          % (ds_bytes / 1e6),
-                   "top1": (top.combination if top else None), "planted": [list(p) for p in planted]},
+                   "top1": (top.combination if top else None), "planted": [list(p) for p in planted],
+                   "planted_rank": planted_rank},
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ds_bytes,
                 "d2h_bytes_per_step": spec.outputs * (4 * spec.order + 4) + 8 * 2},
@@ -357,49 +359,114 @@ def run_gpu(args, spec):
     print(json.dumps(line), flush=True)
 
 
+def planted_ranks(gs, res, ds, spec, planted):
+    """Rank of each planted interaction (of the scan's order) among all combinations by
+    exact MI: its FP64 MI from its tables, against the search's top FIU_MAX_OUTPUTS
+    (outside the timed region)."""
+    from fiuncho_gb300 import Distribution, _lib
+    mine = [p for p in planted if len(p) == spec.order]
+    if not mine:
+        return None
+    _, v64 = gs.run(res, spec.order, Distribution(ds.snps, spec.order - 1), _lib.FIU_MAX_OUTPUTS, with_fp64=True)
+    out = []
+    for p in mine:
+        cc, tt = gs.tables(res, spec.order, np.array([p], np.int32))
+        _, mi = gs.mi(cc, tt, ds.cases, ds.ctrls, mode=1)
+        mi = float(mi[0])
+        rank = int(np.sum(v64 > mi)) + 1 if len(v64) and mi >= v64[-1] else None
+        out.append({"combination": list(p), "mi": mi, "rank": rank,
+                    "rank_note": None if rank else "below the top %d (MI of the %d-th: %.6g)"
+                    % (len(v64), len(v64), float(v64[-1]) if len(v64) else float("nan"))})
+    return out
+
+
 def run_batch_and_serve(args, gs, ctx):
-    """Batched vs plain on the scaled 64-scan batch, then a served Poisson stream."""
+    """Batched vs plain on the uneven 64-scan batch, then a served Poisson stream.
+
+    The batch is the configuration as stated (synth.batch_specs(): SNPs
+    log-uniform in [500, 20 000], order-4 scans capped at 400 SNPs, samples
+    log-uniform in [1 000, 32 000], case fraction U(0.3, 0.7), order U{2,3,4}),
+    with each scan's data set at full size.  The whole batch is ~1.2e16
+    combinations x samples (~90 s per pass, 64 % of it one scan), so every scan
+    is searched over a fixed leading range of its combinations: shard 0 of N_i
+    of its work units, N_i the smallest with at most `--batch-cap`
+    combinations x samples per shard.  Both arms run exactly those shards;
+    the combinations of each shard are counted by the library.  Timed passes:
+    `--batch-passes` per arm (alternating), median reported.
+
+    The served stream draws full-size scans (no truncation) from the same 64
+    at Poisson(`--serve-rate`) for `--serve-seconds` against a 120 GB device
+    budget; at the end of the arrival window the backlog is recorded and the
+    server is destroyed (scans still running are cancelled)."""
+    import ctypes as C
     import random
 
     import torch
 
     from fiuncho_gb300 import Dataset, Distribution, Resident, Server, synth
-    specs = synth.batch_specs(**synth.BATCH_BENCH)
+    lib = ctx.lib
+    specs = synth.batch_specs()
     t0 = time.perf_counter()
     data = []
     for sp in specs:
         g, c, _ = synth.simulate(sp)
         data.append(Dataset.from_genotypes(g, c))
+        del g
     gen_s = time.perf_counter() - t0
-    work = sum(sp.combos() * sp.samples for sp in specs)
+    full_work = sum(sp.combos() * sp.samples for sp in specs)
+    t0 = time.perf_counter()
     res = [Resident(ctx, ds) for ds in data]
-    reqs = [(r, sp.order, Distribution(sp.snps, sp.order - 1), sp.outputs) for r, sp in zip(res, specs)]
-    launches0 = ctx.launches
+    shards = [max(1, math.ceil(sp.combos() * sp.samples / args.batch_cap)) for sp in specs]
+    reqs = [(r, sp.order, Distribution(sp.snps, sp.order - 1), sp.outputs, 0, n)
+            for r, sp, n in zip(res, specs, shards)]
 
     def plain():
-        return [gs.run(r, o, d, n, with_fp64=True) for r, o, d, n in reqs]
+        return [gs.run_shard(r, o, sh, n, k, with_fp64=True) for r, o, _, k, sh, n in reqs]
 
     def batched():
         return gs.run_batch(reqs, use_graph=True)
 
-    # warm-up (also builds the core tables), then one timed pass of each
+    # first pass of the plain loop: builds each data set's device tables, and counts the
+    # combinations of each shard (the library's counter of evaluated combinations)
+    combos = []
+    for r, o, _, k, sh, n in reqs:
+        ctx.check(lib.fiu_set_kernel_timing(ctx.h, 1))
+        gs.run_shard(r, o, sh, n, k)
+        cnt = C.c_uint64(0)
+        ctx.check(lib.fiu_kernel_timing(ctx.h, None, None, C.byref(cnt)))
+        combos.append(int(cnt.value))
+    ctx.check(lib.fiu_set_kernel_timing(ctx.h, 0))
+    prep_s = time.perf_counter() - t0
+    work = sum(c * sp.samples for c, sp in zip(combos, specs))
     a, b = plain(), batched()
-    same = all([x.combination for x in p[0]] == [x.combination for x in q[0]] for p, q in zip(a, b))
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    plain()
-    t_plain = time.perf_counter() - t
-    t = time.perf_counter()
-    batched()
-    t_batch = time.perf_counter() - t
+    same = all([x.combination for x in p[0]] == [x.combination for x in q[0]] and np.array_equal(p[1], q[1])
+               for p, q in zip(a, b))
+    launches0 = ctx.launches
+    t_plain, t_batch = [], []
+    for _ in range(args.batch_passes):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        plain()
+        t_plain.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        batched()
+        t_batch.append(time.perf_counter() - t)
+    batch_launches = ctx.launches - launches0
+    mp, mb = statistics.median(t_plain), statistics.median(t_batch)
+    out = {"workload": "64 uneven scans as configured (synth.batch_specs): SNPs log-uniform [500, 20000], order-4 "
+                       "capped at 400, samples log-uniform [1000, 32000], case fraction U(0.3, 0.7), order U{2,3,4}, "
+                       "top-50 each; full-size data sets, each scan searched over shard 0 of N_i of its work units "
+                       "(<= %.0e combinations x samples per scan)" % args.batch_cap,
+           "combos_samples": work, "combos_samples_full_batch": full_work, "scans_truncated": sum(n > 1 for n in shards),
+           "plain_s": t_plain, "batched_s": t_batch, "plain_median_s": mp, "batched_median_s": mb,
+           "plain": work / mp, "batched": work / mb, "speedup": mp / mb, "passes": args.batch_passes,
+           "identical_results": bool(same), "graph": True, "data_gen_s": gen_s, "device_prep_s": prep_s,
+           "gpu_launches_timed": batch_launches, "unit": UNIT}
     for r in res:
         r.free()
-    out = {"workload": "64 uneven scans: SNPs log-uniform [200, 1200], order-4 capped at 150, samples "
-                       "log-uniform [1000, 32000], case fraction U(0.3, 0.7), order U{2,3,4}, top-50 each",
-           "combos_samples": work, "plain_s": t_plain, "batched_s": t_batch,
-           "plain": work / t_plain, "batched": work / t_batch, "speedup": t_plain / t_batch,
-           "identical_results": same, "graph": True, "data_gen_s": gen_s, "unit": UNIT}
-    # ---- served stream: Poisson arrivals drawn from the same 64 scans
+    del res
+    torch.cuda.empty_cache()
+    # ---- served stream: full-size scans drawn from the same 64, Poisson arrivals
     rng = random.Random(7)
     rate, duration = args.serve_rate, args.serve_seconds
     arrivals, tnow = [], 0.0
@@ -408,36 +475,70 @@ def run_batch_and_serve(args, gs, ctx):
         if tnow >= duration:
             break
         arrivals.append((tnow, rng.randrange(len(data))))
-    srv = Server(ctx.device)
+    srv = Server(ctx.device, budget_bytes=120 * 1000 ** 3)
+    lat, done_idx, pending = [], [], []
     try:
         t0 = time.perf_counter()
-        tickets = []
+
+        def collect():
+            keep = []
+            for tk, i in pending:
+                r = srv.result(tk, 0)
+                if r is None:
+                    keep.append((tk, i))
+                else:
+                    lat.append(r[2])
+                    done_idx.append((i, r))
+            pending[:] = keep
+
         for at, i in arrivals:
-            delay = t0 + at - time.perf_counter()
-            if delay > 0:
-                time.sleep(delay)
-            tickets.append((srv.submit(data[i], specs[i].order, specs[i].outputs), i))
-        lat, same_served = [], True
-        for tk, i in tickets:
-            r, v64, ms = srv.result(tk)
-            lat.append(ms)
-            # each served result equals the scan searched alone (the plain loop above)
-            same_served &= [x.combination for x in r] == [x.combination for x in a[i][0]] and \
-                np.array_equal(v64, a[i][1])
-        makespan = time.perf_counter() - t0
+            while True:
+                delay = t0 + at - time.perf_counter()
+                if delay <= 0:
+                    break
+                collect()
+                time.sleep(min(delay, 0.005))
+            pending.append((srv.submit(data[i], specs[i].order, specs[i].outputs), i))
+        while time.perf_counter() - t0 < duration:
+            collect()
+            time.sleep(0.005)
+        collect()
+        window = time.perf_counter() - t0
         st = srv.stats()
     finally:
+        t1 = time.perf_counter()
         srv.close()
-    served_work = sum(specs[i].combos() * specs[i].samples for _, i in arrivals)
+        close_s = time.perf_counter() - t1
+    # each completed served result equals the same scan searched alone
+    checked, same_served = 0, True
+    alone = {}
+    for i, (r, v64, _) in done_idx:
+        if i not in alone:
+            rr = Resident(ctx, data[i])
+            alone[i] = gs.run(rr, specs[i].order, Distribution(specs[i].snps, specs[i].order - 1), specs[i].outputs,
+                              with_fp64=True)
+            rr.free()
+        ar, av = alone[i]
+        same_served &= [x.combination for x in r] == [x.combination for x in ar] and np.array_equal(v64, av)
+        checked += 1
     lat.sort()
-    out["served"] = {"offered_scans_per_s": rate, "duration_s": duration, "requests": len(arrivals),
-                     "completed": int(st["completed"]), "scans_per_s": len(arrivals) / makespan,
-                     "makespan_s": makespan, "combos_samples_per_s": served_work / makespan,
-                     "p50_ms": lat[len(lat) // 2] if lat else None,
-                     "p99_ms": lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))] if lat else None,
-                     "rounds": int(st["rounds"]), "solo": int(st["solo"]), "overlapped": int(st["overlapped"]),
-                     "identical_to_alone": bool(same_served), "unit": UNIT}
-    out["gpu_launches"] = ctx.launches - launches0
+    offered_work = sum(specs[i].combos() * specs[i].samples for _, i in arrivals)
+    out["served"] = {
+        "workload": "Poisson arrivals of full-size scans drawn uniformly from the 64 above (configuration 5), "
+                    "120 GB device budget",
+        "offered_scans_per_s": rate, "duration_s": duration, "requests": len(arrivals),
+        "offered_combos_samples_per_s": offered_work / duration,
+        "completed": int(st["completed"]), "completed_scans_per_s": st["completed"] / window,
+        "completed_combos_samples_per_s": st["combos_samples"] / window,
+        "backlog_at_end": int(st["queued"] + st["active"]), "queued_at_end": int(st["queued"]),
+        "admitted_at_end": int(st["active"]), "peak_device_bytes": int(st["peak_bytes"]),
+        "p50_ms": lat[len(lat) // 2] if lat else None,
+        "p99_ms": lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))] if lat else None,
+        "latency_of": "completed scans (submit -> result)",
+        "rounds": int(st["rounds"]), "solo": int(st["solo"]), "overlapped": int(st["overlapped"]),
+        "rounds_note": "every scan of this distribution is one-hot over its whole data set, so each runs on a "
+                       "tensor-core (or pair-major order-4) kernel on a solo lane; the rounds serve the other scans",
+        "identical_to_alone": bool(same_served), "checked": checked, "destroy_s": close_s, "unit": UNIT}
     return out
 
 
@@ -455,6 +556,9 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=20.0, help="served stream: Poisson arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="served stream: arrival window (60 s, the served configuration's loop)")
+    ap.add_argument("--batch-cap", type=float, default=2e12,
+                    help="batched form: combinations x samples searched per scan (a leading shard of larger scans)")
+    ap.add_argument("--batch-passes", type=int, default=3, help="batched form: timed passes per arm (median)")
     args = ap.parse_args()
     import dataclasses
 

@@ -44,7 +44,8 @@ class Distribution_t(C.Structure):
 class Scan_t(C.Structure):
     _fields_ = [("res", C.c_void_p), ("order", C.c_uint), ("distribution", Distribution_t), ("outputs", C.c_uint),
                 ("out_combinations", C.POINTER(C.c_int32)), ("out_vals", C.POINTER(C.c_float)),
-                ("out_vals64", C.POINTER(C.c_double)), ("out_count", C.c_uint), ("status", C.c_int)]
+                ("out_vals64", C.POINTER(C.c_double)), ("out_count", C.c_uint), ("status", C.c_int),
+                ("shard", C.c_uint), ("n_shards", C.c_uint)]
 
 
 class ServerStats_t(C.Structure):
@@ -98,6 +99,8 @@ _SIGS = {
     "fiu_search_batch": (C.c_int, [_vp, C.POINTER(Scan_t), C.c_uint, C.c_int]),
     "fiu_server_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_vp)]),
     "fiu_server_submit": (C.c_int, [_vp, C.POINTER(Dataset_t), C.c_uint, C.c_uint, C.POINTER(C.c_uint64)]),
+    "fiu_server_submit_shard": (C.c_int, [_vp, C.POINTER(Dataset_t), C.c_uint, C.c_uint, C.c_uint, C.c_uint,
+                                          C.POINTER(C.c_uint64)]),
     "fiu_server_poll": (C.c_int, [_vp, C.c_uint64, C.c_int, _i32p, _f32p, _f64p, C.POINTER(C.c_uint),
                                   C.POINTER(C.c_double)]),
     "fiu_server_stats": (C.c_int, [_vp, C.POINTER(ServerStats_t)]),

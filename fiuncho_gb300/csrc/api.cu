@@ -1,6 +1,7 @@
 // C ABI of the library (include/fiuncho_gpu.h): contexts, resident data sets,
 // the search driver and the kernel-level entries.
 #include <algorithm>
+#include <chrono>
 #include <map>
 #include <cmath>
 #include <cstdio>
@@ -344,11 +345,22 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     const double per_unit = tensor       ? tensor_item_combos(*res->t3, (int)order)
                             : pair_major ? (double)binom(w.dist_n, 4) / std::max(1ll, res->e4_items)
                                          : per_prefix;
+    // Chunk schedule.  While fewer than `keep` candidates are held every
+    // combination is one; afterwards the threshold is the keep-th best key of
+    // the `seen` combinations so far, and about keep / seen of the next
+    // chunk's combinations pass it.  Chunks are sized for a quarter of the
+    // candidate buffer under that estimate (a chunk that overflows all the
+    // same is re-run in smaller pieces), so a scan takes a few launches.  A
+    // chunk also stays under about a quarter second (measured per unit on the
+    // previous chunk), so that a cancellation takes effect soon.
     long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_unit)));
+    double seen = 0, sec_per_unit = 0;
     long long m = units / n_shards * shard + std::min<long long>(shard, units % n_shards);
     const long long m_end = m + units / n_shards + (shard < units % n_shards ? 1 : 0);
     while (m < m_end) {
+        if (ctx->cancel.load(std::memory_order_relaxed)) return fail(ctx, FIU_ERR_CANCELLED, "search cancelled");
         const long long m1 = std::min(m_end, m + chunk);
+        const auto t_chunk = std::chrono::steady_clock::now();
         ctx->pinned[0] = have;
         ctx->pinned[1] = 0;
         CK(cudaMemcpyAsync(count, ctx->pinned, 2 * sizeof(unsigned), cudaMemcpyHostToDevice, s), "reset counters");
@@ -367,6 +379,8 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
         if (ctx->timing) CK(cudaEventRecord(ctx->ev1, s), "event");
         CK(cudaMemcpyAsync(ctx->pinned, count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read counters");
         CK(cudaStreamSynchronize(s), "count kernel");
+        sec_per_unit = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_chunk).count() /
+                       (double)(m1 - m);
         if (ctx->timing) {
             float ms = 0;
             CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
@@ -379,7 +393,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
             chunk = std::max<long long>(1, (m1 - m) / 4);
             continue;
         }
-        const unsigned fresh = M - have;
+        seen += (double)(m1 - m) * per_unit;
         if (M > keep) {
             CK(select_top(ctx->cand, M, keep, ctx->tmp, scratch, s), "top-N selection");
             Cand last;
@@ -391,11 +405,9 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
             have = M;
         }
         m = m1;
-        // grow fast while a chunk admits few candidates: every chunk costs a
-        // launch and a host round trip, which dominate small scans
-        if (fresh < cap / 64) chunk *= 16;
-        else if (fresh < cap / 8) chunk *= 4;
-        else if (fresh > cap / 2) chunk = std::max<long long>(1, chunk / 2);
+        const double next = have < keep ? (double)(cap - have) / (4.0 * std::max(1.0, per_unit))
+                                        : (double)cap / 4.0 * seen / ((double)keep * std::max(1.0, per_unit));
+        chunk = (long long)std::max(1.0, std::min({next, 0.25 / std::max(sec_per_unit, 1e-12), 4.0e18}));
     }
     if (tensor) {
         int st = 0;

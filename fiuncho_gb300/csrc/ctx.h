@@ -2,6 +2,7 @@
 // resident data set objects, error helpers and the single-scan driver.
 #pragma once
 
+#include <atomic>
 #include <map>
 #include <string>
 #include <utility>
@@ -42,6 +43,9 @@ struct fiu_ctx {
     size_t host_arena_cap = 0;
     // helper lanes of the batched search (own stream and scratch each), made on first use
     fiu_ctx* lanes[2] = {nullptr, nullptr};
+    // set by another thread to stop the search running on this context after
+    // its current chunk (FIU_ERR_CANCELLED)
+    std::atomic<int> cancel{0};
 };
 
 struct fiu_resident {

@@ -32,6 +32,7 @@ namespace {
 
 struct Plan {
     int idx;           // index in the caller's array
+    long long m_begin, m_end;  // owned prefix ordinals of the scan's shard
     ScanWork w;
     int kind, tp;
     unsigned keep, cap, outputs;
@@ -65,6 +66,12 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             sc.status = rc;
             continue;
         }
+        const unsigned ns = sc.n_shards ? sc.n_shards : 1;
+        if (sc.shard >= ns ||
+            (ns > 1 && (w.dist_step != 1 || w.dist_offset != 0 || w.dist_n != sc.res->d.snps))) {
+            sc.status = fail(ctx, FIU_ERR_INVALID, "shard out of range, or a shard of a distribution layer");
+            continue;
+        }
         if (sc.outputs == 0 || w.n_prefixes == 0) continue;
         int kind = 0, tp = 256;
         if ((rc = choose_tile(ctx, sc.res, w, ctx->kernel, kind, tp, true))) {
@@ -78,6 +85,8 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
         }
         Plan p;
         p.idx = (int)i;
+        p.m_begin = w.n_prefixes / ns * sc.shard + std::min<long long>(sc.shard, w.n_prefixes % ns);
+        p.m_end = p.m_begin + w.n_prefixes / ns + (sc.shard < w.n_prefixes % ns ? 1 : 0);
         p.w = w;
         p.kind = kind;
         p.tp = tp;
@@ -121,7 +130,8 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             for (unsigned i : alone[g]) {
                 fiu_scan& sc = scans[i];
                 sc.status = search_impl(lc, sc.res, sc.order, &sc.distribution, sc.outputs, sc.out_combinations,
-                                        sc.out_vals, sc.out_vals64, &sc.out_count, 0);
+                                        sc.out_vals, sc.out_vals64, &sc.out_count, 0, sc.shard,
+                                        sc.n_shards ? sc.n_shards : 1);
                 if (sc.status && lc != ctx) {
                     std::lock_guard<std::mutex> g2(err_mu);
                     lane_err = lc->err;
@@ -164,6 +174,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
         std::vector<long long> grp_total;   // items of group g
         std::vector<int> grp_family, grp_tp;
         std::vector<long long> cursor(n, 0), chunk(n);
+        for (int s = 0; s < n; ++s) cursor[s] = plans[s].m_begin;
         for (int s = 0; s < n; ++s) {
             const auto& w = plans[s].w;
             const double per = (double)binom(w.dist_n, w.order) / std::max(1.0, (double)binom(w.dist_n, w.order - 1));
@@ -174,7 +185,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             more = false;
             std::vector<long long> take(n, 0);
             for (int s = 0; s < n; ++s) {
-                const long long left = plans[s].w.n_prefixes - cursor[s];
+                const long long left = plans[s].m_end - cursor[s];
                 if (left > 0) take[s] = std::min(left, chunk[s]);
             }
             for (int fam = 0; fam < kRoundFamilies; ++fam)
@@ -194,7 +205,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             for (int s = 0; s < n; ++s) {
                 cursor[s] += take[s];
                 chunk[s] *= 4;
-                if (cursor[s] < plans[s].w.n_prefixes) more = true;
+                if (cursor[s] < plans[s].m_end) more = true;
             }
         }
         grp_first.push_back(ents.size());
@@ -307,7 +318,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
     for (unsigned i : single_path) {
         fiu_scan& sc = scans[i];
         sc.status = search_impl(ctx, sc.res, sc.order, &sc.distribution, sc.outputs, sc.out_combinations,
-                                sc.out_vals, sc.out_vals64, &sc.out_count, 0);
+                                sc.out_vals, sc.out_vals64, &sc.out_count, 0, sc.shard, sc.n_shards ? sc.n_shards : 1);
     }
     run_alone(ctx);
     for (std::thread& t : lane_threads) t.join();

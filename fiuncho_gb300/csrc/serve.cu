@@ -57,6 +57,8 @@ struct ServeScan {
     int kind = 0, tp = 256;
     unsigned keep = 0, cap = 0;
     long long cursor = 0, chunk = 1, max_chunk = 1;
+    unsigned shard = 0, n_shards = 1;  // shard of the scan's work units (fiu_server_submit_shard)
+    long long m_end = 0;               // end of the shard's prefix ordinals (round scans)
     size_t bytes = 0;
     char* buf = nullptr;
     size_t off_scored = 0, off_comb = 0, off_val = 0, off_val64 = 0;
@@ -157,7 +159,8 @@ void finish(fiu_server* sv, ServeScan* s, int status, fiu_ctx* ctx = nullptr) {
         sv->completed++;
         if (s->overlap) sv->overlapped++;
         sv->lat_ms.push_back(std::chrono::duration<double, std::milli>(s->done - s->submitted).count());
-        sv->combos_samples += (double)binom(s->host.snps, s->order) * (double)(s->host.cases + s->host.ctrls);
+        sv->combos_samples +=
+            (double)binom(s->host.snps, s->order) / s->n_shards * (double)(s->host.cases + s->host.ctrls);
     } else {
         sv->failed++;
     }
@@ -184,6 +187,11 @@ bool admit(fiu_server* sv, ServeScan* s) {
     if (s->outputs == 0 || s->w.n_prefixes == 0) {
         finish(sv, s, FIU_OK);
         return false;
+    }
+    {
+        const long long P = s->w.n_prefixes, N = s->n_shards;
+        s->cursor = P / N * s->shard + std::min<long long>(s->shard, P % N);
+        s->m_end = s->cursor + P / N + ((long long)s->shard < P % N ? 1 : 0);
     }
     if ((rc = choose_tile(ctx, s->res, s->w, ctx->kernel, s->kind, s->tp, true))) {
         finish(sv, s, rc);
@@ -261,7 +269,7 @@ int run_round(fiu_server* sv) {
     std::vector<long long> take(sv->active.size(), 0);
     for (size_t i = 0; i < sv->active.size(); ++i) {
         ServeScan* s = sv->active[i];
-        take[i] = std::min({s->w.n_prefixes - s->cursor, s->chunk, s->max_chunk});
+        take[i] = std::min({s->m_end - s->cursor, s->chunk, s->max_chunk});
     }
     std::vector<std::pair<int, int>> gkey;  // (family, tp) of each group
     for (int fam = 0; fam < kRoundFamilies; ++fam)
@@ -300,7 +308,7 @@ int run_round(fiu_server* sv) {
         ServeScan* s = sv->active[i];
         s->cursor += take[i];
         s->chunk *= 4;
-        (s->cursor >= s->w.n_prefixes ? done : still).push_back(s);
+        (s->cursor >= s->m_end ? done : still).push_back(s);
     }
     std::vector<ScanState> hs(done.size());
     for (size_t i = 0; i < done.size(); ++i) {
@@ -315,7 +323,7 @@ int run_round(fiu_server* sv) {
         if (hs[i].overflow) {  // candidate buffer overflowed: redo alone on the adaptive path
             fiu_distribution dist{(int)s->host.snps, (int)s->order - 1, 1, 0};
             rc = search_impl(ctx, s->res, s->order, &dist, s->outputs, s->comb.data(), s->vals.data(),
-                             s->vals64.data(), &s->count, 0);
+                             s->vals64.data(), &s->count, 0, s->shard, s->n_shards);
             finish(sv, s, rc);
             continue;
         }
@@ -352,7 +360,7 @@ void solo_main(fiu_server* sv, int lane) {
         }
         fiu_distribution dist{(int)s->host.snps, (int)s->order - 1, 1, 0};
         const int rc = search_impl(ctx, s->res, s->order, &dist, s->outputs, s->comb.data(), s->vals.data(),
-                                   s->vals64.data(), &s->count, 0);
+                                   s->vals64.data(), &s->count, 0, s->shard, s->n_shards);
         {
             std::lock_guard<std::mutex> g(sv->mu);
             sv->solo++;
@@ -448,9 +456,17 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
 }
 
 int fiu_server_submit(fiu_server* sv, const fiu_dataset* d, unsigned order, unsigned outputs, uint64_t* ticket) {
+    return fiu_server_submit_shard(sv, d, order, outputs, 0, 1, ticket);
+}
+
+int fiu_server_submit_shard(fiu_server* sv, const fiu_dataset* d, unsigned order, unsigned outputs, unsigned shard,
+                            unsigned n_shards, uint64_t* ticket) {
     if (!sv || !d || !d->data || !ticket) return FIU_ERR_INVALID;
     if (order < 2 || order > FIU_MAX_ORDER || outputs > FIU_MAX_OUTPUTS) return FIU_ERR_INVALID;
+    if (n_shards == 0 || shard >= n_shards) return FIU_ERR_INVALID;
     auto* s = new ServeScan;
+    s->shard = shard;
+    s->n_shards = n_shards;
     const size_t words = (size_t)d->snps * 3 * (d->cases_words + d->ctrls_words);
     s->data.assign(d->data, d->data + words);
     s->host = *d;
@@ -532,6 +548,8 @@ void fiu_server_destroy(fiu_server* sv) {
         std::lock_guard<std::mutex> g(sv->mu);
         sv->stop = true;
     }
+    for (fiu_ctx* c : sv->solo_ctx)  // scans running on the solo lanes stop after their current chunk
+        if (c) c->cancel.store(1);
     sv->cv_work.notify_all();
     sv->cv_solo.notify_all();
     if (sv->worker.joinable()) sv->worker.join();

@@ -240,21 +240,25 @@ class GpuSearch:
         return out
 
     def run_batch(self, requests, use_graph: bool = True):
-        """Many scans at once: requests = [(Resident, order, Distribution, outputs), ...].
-        Returns [(results, fp64 values)] in request order; raises if any scan failed."""
+        """Many scans at once: requests = [(Resident, order, Distribution, outputs), ...], or
+        (Resident, order, Distribution, outputs, shard, n_shards) for one shard of a whole
+        scan (as run_shard).  Returns [(results, fp64 values)] in request order; raises if
+        any scan failed."""
         lib, ctx = self.ctx.lib, self.ctx
         arr = (_lib.Scan_t * len(requests))()
         bufs = []
-        for i, (res, order, dist, outputs) in enumerate(requests):
+        for i, req in enumerate(requests):
+            res, order, dist, outputs = req[:4]
+            shard, n_shards = (req[4], req[5]) if len(req) > 4 else (0, 1)
             comb = np.zeros(max(outputs, 1) * order, np.int32)
             vals = np.zeros(max(outputs, 1), np.float32)
             v64 = np.zeros(max(outputs, 1), np.float64)
             bufs.append((comb, vals, v64))
             arr[i] = _lib.Scan_t(res.h, order, dist.c_struct(), outputs, _lib.ptr(comb, C.c_int32),
-                                 _lib.ptr(vals, C.c_float), _lib.ptr(v64, C.c_double), 0, 0)
+                                 _lib.ptr(vals, C.c_float), _lib.ptr(v64, C.c_double), 0, 0, shard, n_shards)
         ctx.check(lib.fiu_search_batch(ctx.h, arr, len(requests), 1 if use_graph else 0))
         out = []
-        for i, (res, order, dist, outputs) in enumerate(requests):
+        for i, (res, order, dist, outputs, *_) in enumerate(requests):
             if arr[i].status:
                 raise FiunchoError(arr[i].status, "scan %d: %s" % (i, lib.fiu_last_error(ctx.h).decode()))
             n = arr[i].out_count
@@ -351,10 +355,12 @@ class Server:
         self._orders = {}
         self._keep = {}
 
-    def submit(self, ds: Dataset, order: int, outputs: int) -> int:
+    def submit(self, ds: Dataset, order: int, outputs: int, shard: int = 0, n_shards: int = 1) -> int:
+        """Queues a whole-data-set scan, or shard `shard` of `n_shards` of it."""
         cds, data = _c_dataset(ds)
         t = C.c_uint64(0)
-        rc = self.lib.fiu_server_submit(self.h, C.byref(cds), int(order), int(outputs), C.byref(t))
+        rc = self.lib.fiu_server_submit_shard(self.h, C.byref(cds), int(order), int(outputs), int(shard),
+                                              int(n_shards), C.byref(t))
         if rc:
             raise FiunchoError(rc, "submit rejected")
         self._orders[t.value] = (order, outputs)

@@ -172,6 +172,10 @@ typedef struct {
     double *out_vals64;              /* out (host, optional): outputs */
     unsigned out_count;              /* out: results written */
     int status;                      /* out: FIU_OK or FIU_ERR_* of this scan */
+    unsigned shard, n_shards;        /* in: search shard `shard` of `n_shards` of the scan's work
+                                        units, as fiu_search_shard (n_shards 0 or 1: all of it;
+                                        with n_shards > 1 the distribution must be the whole
+                                        data set's) */
 } fiu_scan;
 /* use_graph: 1 = capture the rounds into a CUDA graph and launch it once.
  * Returns FIU_OK when every scan ran (see each scan's status). */
@@ -211,6 +215,9 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server **out);
 /* Queues a scan of the whole data set (Distribution(snps, order-1, 1, 0)). */
 int fiu_server_submit(fiu_server *srv, const fiu_dataset *dataset, unsigned order, unsigned outputs,
                       uint64_t *ticket);
+/* Queues shard `shard` of `n_shards` of such a scan (as fiu_search_shard). */
+int fiu_server_submit_shard(fiu_server *srv, const fiu_dataset *dataset, unsigned order, unsigned outputs,
+                            unsigned shard, unsigned n_shards, uint64_t *ticket);
 /* Waits up to wait_ms (0 = do not wait, < 0 = forever) for a ticket; FIU_OK and
  * the results once done (the ticket is then released), FIU_ERR_TIMEOUT if not
  * yet done, the scan's error code if it failed, FIU_ERR_INVALID for an unknown
@@ -218,7 +225,8 @@ int fiu_server_submit(fiu_server *srv, const fiu_dataset *dataset, unsigned orde
 int fiu_server_poll(fiu_server *srv, uint64_t ticket, int wait_ms, int32_t *out_combinations, float *out_vals,
                     double *out_vals64, unsigned *out_count, double *latency_ms);
 int fiu_server_stats(fiu_server *srv, fiu_serve_stats *out);
-/* Stops the worker after the current round; pending scans are dropped. */
+/* Stops the worker after the current round and cancels the scans running on
+ * the solo lanes after their current chunk; pending scans are dropped. */
 void fiu_server_destroy(fiu_server *srv);
 
 /* ---- kernel-level entries ------------------------------------------------------- */

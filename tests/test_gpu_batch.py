@@ -85,3 +85,34 @@ def test_batch_against_oracle(batch_setup, oracle):
         ex = lambda cs: exact_mi(oracle, ds.data, ds.cases_words, ds.ctrls_words, ds.cases, ds.ctrls, order, cs)
         assert_topn_equivalent(comb, c, ex, 1e-5 * abs(float(o64[-1])) + 1e-12)
         assert np.allclose(v, ex(comb), rtol=1e-9)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_batch_shards_identical_to_run_shard(batch_setup, use_graph):
+    """Shard r of N of a whole-data-set scan in the batch (round kernels, tensor-core and
+    pair-major lanes alike) gives the same list as run_shard on it alone, and the shards
+    of a scan merged by (MI desc, combination asc) give the whole scan's list."""
+    gs, reqs, alone = batch_setup
+    whole = [(i, q) for i, q in enumerate(reqs) if q[2].step == 1 and q[2].offset == 0]
+    sharded = []
+    for i, (res, order, dist, outputs) in whole:
+        for r in range(3):
+            sharded.append((i, (res, order, dist, outputs, r, 3)))
+    got = gs.run_batch([q for _, q in sharded], use_graph=use_graph)
+    merged = {}
+    for (i, (res, order, dist, outputs, r, n)), (rs, v) in zip(sharded, got):
+        want, wv = gs.run_shard(res, order, r, n, outputs, with_fp64=True)
+        assert [x.combination for x in rs] == [x.combination for x in want]
+        assert np.array_equal(v, wv)
+        merged.setdefault(i, []).extend(zip((-x for x in v), (x.combination for x in rs)))
+    for i, (res, order, dist, outputs) in whole:
+        m = sorted(merged[i])[:outputs]
+        assert [c for _, c in m] == [x.combination for x in alone[i][0]]
+
+
+def test_batch_rejects_shard_of_a_layer(batch_setup):
+    from fiuncho_gb300 import FiunchoError
+    gs, reqs, _ = batch_setup
+    res, order, dist, outputs = reqs[3]  # a Distribution(..., 3, 1) layer
+    with pytest.raises(FiunchoError):
+        gs.run_batch([(res, order, dist, outputs, 0, 2)])

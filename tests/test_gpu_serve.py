@@ -138,3 +138,41 @@ def test_server_solo_lanes_overlap():
         assert st["overlapped"] == 2
     finally:
         srv.close()
+
+
+def test_server_shards_identical_to_run_shard():
+    """Shards submitted to the server (solo lanes and rounds) give run_shard's lists."""
+    from fiuncho_gb300 import GpuSearch, Server
+    gs = GpuSearch(0)
+    cases = [(_ds(60, 700, 1500, 1500), 3, 30), (_ds(61, 90, 700, 650, one_hot=False), 3, 20),
+             (_ds(62, 60, 2000, 1900), 4, 25)]
+    srv = Server(0)
+    try:
+        tickets = [(srv.submit(ds, order, out, r, 4), ds, order, out, r) for ds, order, out in cases for r in range(4)]
+        for t, ds, order, out, r in tickets:
+            _same(srv.result(t), gs.run_shard(ds, order, r, 4, out, with_fp64=True))
+        st = srv.stats()
+        assert st["completed"] == len(tickets) and st["rounds"] > 0
+    finally:
+        srv.close()
+
+
+def test_server_destroy_cancels_running_scans():
+    """Destroying a server while a long scan runs on a solo lane returns once the scan's
+    current chunk is done (the scan is cancelled), not after the whole scan."""
+    from fiuncho_gb300 import Server
+    ds = _ds(70, 4000, 4000, 4000)  # order 3: about 1e10 combinations x 8 000 samples, ~0.6 s
+    srv = Server(0)
+    srv.submit(ds, 3, 10)
+    deadline = time.time() + 30
+    while time.time() < deadline:  # admitted (its data set uploaded), then on a solo lane
+        st = srv.stats()
+        if st["queued"] == 0 and st["active"] == 1:
+            break
+        time.sleep(0.002)
+    time.sleep(0.15)
+    st = srv.stats()
+    assert st["completed"] == 0, "the scan finished before the server was destroyed"
+    t0 = time.perf_counter()
+    srv.close()
+    assert time.perf_counter() - t0 < 0.6
