@@ -331,7 +331,8 @@ def run_gpu(args, spec):
     batch = None if (args.no_batch or ws > 1) else run_batch_and_serve(args, gs, ctx)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * my_time / args.steps, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * my_time / args.steps, "step_ms": [round(x, 3) for x in step_ms],
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": args.workload, "snps": spec.snps, "cases": spec.cases, "ctrls": spec.ctrls,
                    "order": spec.order, "outputs": spec.outputs, "combinations": total_combos,

@@ -721,6 +721,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
                     break;
                 }
                 const uint32_t dcol = tmem + (uint32_t)(kPN * buf);
+                // (N stays 256: with cta_group::2 each CTA supplies N / 2 of the B rows, so a
+                // narrower N would move the split point off the CTAs' l halves)
                 for (int ks = 0; ks < ksteps; ++ks, ++step) {
                     const int s = (int)(step % kPxStages);
                     // both CTAs' rows landed and both A tiles are built

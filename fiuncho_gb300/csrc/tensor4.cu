@@ -334,7 +334,6 @@ __global__ void __launch_bounds__(kT4Threads, 1)
     const int ksteps = ks_c + (d.tw + 1) / 2;
     constexpr int L = PACK ? kT4L : kT4L / 2;                     // l per item
     constexpr int NR = 2 * L;                                       // N of one accumulator region
-    constexpr uint32_t kIdesc = t4_idesc(NR);
     constexpr uint32_t kTx = NR * kT3KB + kT4SK + 2 * 2 * kT3KB;  // bytes the TMA brings per stage
     constexpr int NCC = L / 16;                                     // column groups of 8 l per epilogue warp
 
@@ -405,6 +404,13 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     ok = false;
                     break;
                 }
+                // the MMA costs in proportion to N (from N 64 up): an item whose l run is cut
+                // short by the last SNP multiplies only the columns of its valid l, rounded up
+                // to 8 l (the epilogue's column groups), N 64 at least
+                int ii, jj, kk0, l0;
+                t4_decode<L>(begin, per, n, g, ii, jj, kk0, l0);
+                const int vl = min(L, n - l0);
+                const uint32_t idesc = t4_idesc(min(NR, max(64, (2 * vl + 15) / 16 * 16)));
                 for (int ks = 0; ks < ksteps; ++ks, ++step) {
                     // packed: one region of N 256 per buffer; split: cases in the
                     // buffer's first N 128 columns, controls in its second
@@ -425,7 +431,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                         asm volatile(
                             "{.reg .pred p; setp.ne.b32 p, %4, 0;\n"
                             "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;}\n" ::"r"(dcol),
-                            "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc));
+                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
                     }
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                         smem_u32(&empty[s])));
