@@ -329,6 +329,7 @@ def run_gpu(args, spec):
     planted_rank = planted_ranks(gs, res, ds, spec, planted) if ws == 1 else None
     cpu = cpu_sample(spec, ds, seconds=args.cpu_seconds) if args.cpu_seconds > 0 and ws == 1 else None
     batch = None if (args.no_batch or ws > 1) else run_batch_and_serve(args, gs, ctx)
+    ingest_t = ingest_timing(ctx, os.cpu_count() or 1) if (not args.no_ingest and ws == 1) else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * my_time / args.steps, "step_ms": [round(x, 3) for x in step_ms],
@@ -356,8 +357,36 @@ def run_gpu(args, spec):
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
         "batched": batch,
+        "ingest": ingest_t,
     }
     print(json.dumps(line), flush=True)
+
+
+def ingest_timing(ctx, threads):
+    """Ingest of the 40 000 SNPs x 8 000 / 8 000 samples workload from PLINK text
+    files (.tped 2.6 GB + .tfam, written first, outside the timing): the
+    library's threaded parser to genotype codes, then packing on the device."""
+    import tempfile
+
+    from fiuncho_gb300 import ingest, synth
+    spec = synth.WORKLOADS["order2_40000x16000"]
+    g, c, _ = synth.simulate(spec)
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        tped, tfam = synth.write_tped(os.path.join(d, "x"), g, c)
+        write_s = time.perf_counter() - t0
+        del g, c
+        size = os.path.getsize(tped)
+        t0 = time.perf_counter()
+        geno, is_case = ingest.read_genotypes([tped, tfam], threads=threads, ctx=ctx)
+        parse_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    res = ingest.upload_genotypes(ctx, geno, is_case)
+    pack_s = time.perf_counter() - t0
+    res.free()
+    return {"workload": "order2_40000x16000 as .tped/.tfam", "file_bytes": size, "threads": threads,
+            "parse_s": parse_s, "parse_gb_per_s": size / parse_s / 1e9,
+            "device_pack_and_prepare_s": pack_s, "write_s_untimed": write_s}
 
 
 def planted_ranks(gs, res, ds, spec, planted):
@@ -554,6 +583,7 @@ def main():
     ap.add_argument("--snps", type=int, default=0, help="override the SNP count (small profiling cases)")
     ap.add_argument("--kernel", type=int, default=0, help="force a counting kernel (0 = automatic choice)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched / served measurements")
+    ap.add_argument("--no-ingest", action="store_true", help="skip the file ingest timing")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="served stream: Poisson arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="served stream: arrival window (60 s, the served configuration's loop)")

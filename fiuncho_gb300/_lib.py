@@ -108,6 +108,13 @@ _SIGS = {
     "fiu_tables": (C.c_int, [_vp, _vp, C.c_uint, _i32p, C.c_size_t, _u32p, _u32p]),
     "fiu_scan_tables": (C.c_int, [_vp, _vp, C.c_uint, C.POINTER(Distribution_t), C.c_int, _u32p, C.c_size_t]),
     "fiu_scan_digest": (C.c_int, [_vp, _vp, C.c_uint, C.POINTER(Distribution_t), C.c_int, _u64p, _u64p]),
+    "fiu_read_genotypes": (C.c_int, [_vp, C.c_char_p, C.c_char_p, C.c_int, C.POINTER(_vp)]),
+    "fiu_genotypes_info": (C.c_int, [_vp, _u64p, _u64p, C.POINTER(C.POINTER(C.c_uint8)),
+                                     C.POINTER(C.POINTER(C.c_uint8))]),
+    "fiu_genotypes_free": (None, [_vp]),
+    "fiu_dataset_upload_genotypes": (C.c_int, [_vp, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), C.c_uint64,
+                                               C.c_uint64, C.POINTER(_vp)]),
+    "fiu_dataset_packed": (C.c_int, [_vp, _vp, C.POINTER(Dataset_t), _u64p]),
 }
 
 _lib = None

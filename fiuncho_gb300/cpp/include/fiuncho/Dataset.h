@@ -10,6 +10,7 @@
 
 #include <fiuncho/GenotypeTable.h>
 #include <fiuncho/dataset/Readers.hpp>
+#include <fiuncho_gpu.h>
 
 #include <memory>
 #include <stdexcept>
@@ -22,22 +23,25 @@ template <class T> class Dataset
     Dataset(const Dataset<T> &) = delete;
     Dataset(Dataset<T> &&) = default;
 
-    static Dataset<T> read(const std::vector<std::string> &inputs)
+    /** Parses the inputs with the library's threaded reader (fiu_read_genotypes,
+     * `threads` host threads, 0 = all cores) and packs them; errors throw
+     * std::runtime_error with the reader's message, as the reference does. */
+    static Dataset<T> read(const std::vector<std::string> &inputs, int threads = 0)
     {
-        fiuncho_io::Genotypes g;
-        if (inputs.size() == 1) {
-            const std::string ext = fiuncho_io::extension(inputs[0]);
-            if (ext != ".raw") throw std::runtime_error("Unrecognized input file extension " + ext);
-            g = fiuncho_io::read_raw(inputs[0]);
-        } else if (inputs.size() == 2) {
-            const std::string e1 = fiuncho_io::extension(inputs[0]), e2 = fiuncho_io::extension(inputs[1]);
-            if (e1 != ".tped" && e1 != ".tfam") throw std::runtime_error("Unrecognized input file extension " + e1);
-            if (e1 == e2 || (e2 != ".tped" && e2 != ".tfam"))
-                throw std::runtime_error("Expecting a tfam file after \"" + inputs[0] + "\", but found a " + e2);
-            g = e1 == ".tped" ? fiuncho_io::read_tped(inputs[0], inputs[1]) : fiuncho_io::read_tped(inputs[1], inputs[0]);
-        } else {
+        if (inputs.size() != 1 && inputs.size() != 2)
             throw std::runtime_error("Unrecognized number of input files to Dataset factory constructor");
-        }
+        fiu_genotypes *h = nullptr;
+        if (fiu_read_genotypes(nullptr, inputs[0].c_str(), inputs.size() == 2 ? inputs[1].c_str() : nullptr, threads,
+                               &h) != FIU_OK)
+            throw std::runtime_error(fiu_last_error(nullptr));
+        uint64_t snps = 0, samples = 0;
+        const uint8_t *codes = nullptr, *cases = nullptr;
+        fiu_genotypes_info(h, &snps, &samples, &codes, &cases);
+        fiuncho_io::Genotypes g;
+        g.snps = snps;
+        g.geno.assign(codes, codes + snps * samples);
+        g.is_case.assign(cases, cases + samples);
+        fiu_genotypes_free(h);
         return from_genotypes(g);
     }
 

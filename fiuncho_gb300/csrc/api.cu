@@ -22,8 +22,12 @@ using namespace fiu;
 
 namespace fiu {
 
+// Message of the last failure of a call made without a context (this thread).
+static thread_local std::string g_free_err;
+
 int fail(fiu_ctx* ctx, int code, const std::string& msg) {
     if (ctx) ctx->err = msg;
+    else g_free_err = msg;
     return code;
 }
 
@@ -436,6 +440,70 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     return FIU_OK;
 }
 
+int check_sizes(fiu_ctx* ctx, uint64_t snps, uint64_t cases, uint64_t ctrls, uint64_t cw, uint64_t tw) {
+    if (snps < 1 || snps > 0x7fffffffull || cw > 0x7fffffffull / 8 || tw > 0x7fffffffull / 8)
+        return fail(ctx, FIU_ERR_INVALID, "data set sizes out of range");
+    if (cases > 64 * cw || ctrls > 64 * tw) return fail(ctx, FIU_ERR_INVALID, "more samples than the row words hold");
+    if (cases + ctrls == 0) return fail(ctx, FIU_ERR_INVALID, "empty data set");
+    if (cw + tw == 0) return fail(ctx, FIU_ERR_INVALID, "rows without words");
+    return FIU_OK;
+}
+
+// A resident data set with its reference-layout buffer allocated (not filled).
+int new_resident(fiu_ctx* ctx, uint64_t snps, uint64_t cases, uint64_t ctrls, uint64_t cw, uint64_t tw,
+                 fiu_resident** out) {
+    auto* r = new (std::nothrow) fiu_resident;
+    if (!r) return fail(ctx, FIU_ERR_NOMEM, "host allocation");
+    r->device = ctx->device;
+    r->d = DevData{nullptr, nullptr, nullptr, (int)snps, (int)cw, (int)tw, (int)cases, (int)ctrls};
+    const size_t words = (size_t)snps * 3 * (size_t)(cw + tw);
+    cudaError_t e = cudaMalloc((void**)&r->ref, words * 8);
+    if (e != cudaSuccess) {
+        delete r;
+        return cuda_fail(ctx, e, "data set upload");
+    }
+    *out = r;
+    return FIU_OK;
+}
+
+// Once r->ref holds the reference layout on the device (queued on the
+// context's stream): the transposed copy, the c ln c table and the one-hot
+// check.  Frees r on failure.
+int finish_resident(fiu_ctx* ctx, fiu_resident* r) {
+    const int snps = r->d.snps, cw = r->d.cw, tw = r->d.tw;
+    const size_t rows = 3 * (size_t)(cw + tw);
+    const size_t words = (size_t)snps * rows;
+    const long long tmax = 64ll * (cw + tw);
+    std::vector<long long> ftab;
+    try {
+        ftab.resize(tmax + 1);
+    } catch (const std::exception&) {
+        fiu_dataset_free(ctx, r);
+        return fail(ctx, FIU_ERR_NOMEM, "host c ln c table");
+    }
+    for (long long c = 0; c <= tmax; ++c)
+        ftab[c] = c < 2 ? 0 : (long long)llround((double)c * std::log((double)c) * 4294967296.0);
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaMalloc((void**)&r->tr, words * 8);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&r->ftab, ftab.size() * 8);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r->ftab, ftab.data(), ftab.size() * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_transpose(r->ref, r->tr, snps, (int)rows, s);
+    int* bad = (int*)(ctx->ctl + 300);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = launch_onehot_check(r->ref, snps, cw, tw, r->d.n_cases, r->d.n_ctrls, bad, s);
+    int hb = 1;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        fiu_dataset_free(ctx, r);
+        return cuda_fail(ctx, e, "data set upload");
+    }
+    r->one_hot = hb == 0;
+    r->ftab_max = tmax;
+    r->d = DevData{r->ref, r->tr, r->ftab, snps, cw, tw, r->d.n_cases, r->d.n_ctrls};
+    return FIU_OK;
+}
+
 }  // namespace fiu
 
 extern "C" {
@@ -486,7 +554,10 @@ void fiu_destroy(fiu_ctx* ctx) {
     delete ctx;
 }
 
-const char* fiu_last_error(const fiu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+const char* fiu_last_error(const fiu_ctx* ctx) {
+    if (ctx) return ctx->err.c_str();
+    return g_free_err.empty() ? "null context" : g_free_err.c_str();
+}
 
 uint64_t fiu_launch_count(const fiu_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
@@ -574,44 +645,18 @@ int fiu_dataset_upload(fiu_ctx* ctx, const fiu_dataset* h, fiu_resident** out) {
     Scope scope(ctx);
     *out = nullptr;
     if (!h || !h->data) return fail(ctx, FIU_ERR_INVALID, "null data set");
-    if (h->snps < 1 || h->snps > 0x7fffffffull || h->cases_words > 0x7fffffffull / 8 ||
-        h->ctrls_words > 0x7fffffffull / 8)
-        return fail(ctx, FIU_ERR_INVALID, "data set sizes out of range");
-    if (h->cases > 64 * h->cases_words || h->ctrls > 64 * h->ctrls_words)
-        return fail(ctx, FIU_ERR_INVALID, "more samples than the row words hold");
-    if (h->cases + h->ctrls == 0) return fail(ctx, FIU_ERR_INVALID, "empty data set");
-    if (h->cases_words + h->ctrls_words == 0) return fail(ctx, FIU_ERR_INVALID, "rows without words");
+    int rc = check_sizes(ctx, h->snps, h->cases, h->ctrls, h->cases_words, h->ctrls_words);
+    if (rc) return rc;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
-    auto* r = new (std::nothrow) fiu_resident;
-    if (!r) return fail(ctx, FIU_ERR_NOMEM, "host allocation");
-    r->device = ctx->device;
-    const int snps = (int)h->snps, cw = (int)h->cases_words, tw = (int)h->ctrls_words;
-    const size_t rows = 3 * (size_t)(cw + tw);
-    const size_t words = (size_t)snps * rows;
-    const long long tmax = 64ll * (cw + tw);
-    std::vector<long long> ftab(tmax + 1);
-    for (long long c = 0; c <= tmax; ++c)
-        ftab[c] = c < 2 ? 0 : (long long)llround((double)c * std::log((double)c) * 4294967296.0);
-    cudaStream_t s = ctx->stream;
-    cudaError_t e = cudaMalloc((void**)&r->ref, words * 8);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&r->tr, words * 8);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&r->ftab, ftab.size() * 8);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(r->ref, h->data, words * 8, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(r->ftab, ftab.data(), ftab.size() * 8, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = launch_transpose(r->ref, r->tr, snps, (int)rows, s);
-    int* bad = (int*)(ctx->ctl + 300);
-    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), s);
-    if (e == cudaSuccess) e = launch_onehot_check(r->ref, snps, cw, tw, (int)h->cases, (int)h->ctrls, bad, s);
-    int hb = 1;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    const size_t words = (size_t)h->snps * 3 * (size_t)(h->cases_words + h->ctrls_words);
+    fiu_resident* r = nullptr;
+    if ((rc = new_resident(ctx, h->snps, h->cases, h->ctrls, h->cases_words, h->ctrls_words, &r))) return rc;
+    cudaError_t e = cudaMemcpyAsync(r->ref, h->data, words * 8, cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) {
         fiu_dataset_free(ctx, r);
         return cuda_fail(ctx, e, "data set upload");
     }
-    r->one_hot = hb == 0;
-    r->ftab_max = tmax;
-    r->d = DevData{r->ref, r->tr, r->ftab, snps, cw, tw, (int)h->cases, (int)h->ctrls};
+    if ((rc = finish_resident(ctx, r))) return rc;
     *out = r;
     return FIU_OK;
 }

@@ -92,6 +92,12 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
 bool e4_pair_major(int kernel, const fiu_resident* res, const ScanWork& w);
 cudaError_t launch_kernel(int kernel, int tp, const fiu_resident* res, const ScanWork& w, long long m0, long long m1,
                           const CandSink& sink, uint32_t* dump, cudaStream_t s, int sms);
+// Data set upload in steps (api.cu): sizes check, allocation of the reference
+// layout, then the derived device layouts once the layout is filled.
+int check_sizes(fiu_ctx* ctx, uint64_t snps, uint64_t cases, uint64_t ctrls, uint64_t cw, uint64_t tw);
+int new_resident(fiu_ctx* ctx, uint64_t snps, uint64_t cases, uint64_t ctrls, uint64_t cw, uint64_t tw,
+                 fiu_resident** out);
+int finish_resident(fiu_ctx* ctx, fiu_resident* r);
 // shard / n_shards: the search covers the shard-th of n_shards contiguous
 // ranges of the serving kernel's work units (tensor work items, pair-major
 // items or prefix ordinals).

@@ -146,6 +146,16 @@ class Resident:
         self.snps, self.cases, self.ctrls = ds.snps, ds.cases, ds.ctrls
         self._keep = None
 
+    @classmethod
+    def adopt(cls, ctx: "Context", handle) -> "Resident":
+        """Wraps a resident data set made by the library (e.g. fiu_dataset_upload_genotypes)."""
+        r = cls.__new__(cls)
+        r.ctx, r.h, r._keep = ctx, handle, None
+        d = _lib.Dataset_t()
+        ctx.check(ctx.lib.fiu_dataset_packed(ctx.h, handle, C.byref(d), None))
+        r.snps, r.cases, r.ctrls = int(d.snps), int(d.cases), int(d.ctrls)
+        return r
+
     @property
     def one_hot(self) -> bool:
         return bool(self.ctx.lib.fiu_dataset_is_one_hot(self.h))

@@ -165,3 +165,65 @@ def simulate(spec: ScanSpec, chunk: int = 2048):
     is_case = np.zeros(spec.samples, np.uint8)
     is_case[: spec.cases] = 1
     return geno, is_case, planted
+
+
+# ---------------------------------------------------------------------------
+# Synthetic genotype files (PLINK .tped/.tfam and .raw) for the ingest path.
+
+_LETTERS = np.frombuffer(b"ACGT", np.uint8)
+
+
+def write_tped(prefix: str, geno: np.ndarray, is_case: np.ndarray, letters=None, chunk: int = 512):
+    """Writes prefix.tped / prefix.tfam: one line per SNP ("chr id 0 pos" then two
+    nucleotides per sample), genotype g written as g copies of the SNP's second
+    letter.  letters: per-SNP (first, second) indices into ACGT (default A, C).
+    Returns the two paths.  Which allele the reader takes as the minor follows
+    its own rule (the rarer, ties to the smaller letter), so a file's codes
+    are the written ones only where the second letter is the rarer."""
+    geno = np.ascontiguousarray(geno, np.uint8)
+    snps, n = geno.shape
+    tfam = prefix + ".tfam"
+    with open(tfam, "w") as f:
+        for s in range(n):
+            f.write("F%d I%d 0 0 1 %d\n" % (s, s, 2 if is_case[s] else 1))
+    tped = prefix + ".tped"
+    with open(tped, "wb") as f:
+        for s0 in range(0, snps, chunk):
+            s1 = min(snps, s0 + chunk)
+            if letters is None:
+                lut = np.array([b"A A ", b"A C ", b"C C "], dtype="S4").view(np.uint8).reshape(1, 3, 4)
+                body = lut[0][geno[s0:s1]]
+            else:
+                a, b = _LETTERS[letters[s0:s1, 0]], _LETTERS[letters[s0:s1, 1]]
+                sp = np.full(s1 - s0, ord(" "), np.uint8)
+                lut = np.stack([np.stack([a, sp, a, sp], 1), np.stack([a, sp, b, sp], 1), np.stack([b, sp, b, sp], 1)], 1)
+                body = lut[np.arange(s1 - s0)[:, None], geno[s0:s1]]
+            body = body.reshape(s1 - s0, 4 * n)
+            body[:, -1] = ord("\n")
+            for r in range(s1 - s0):
+                f.write(b"1 rs%d 0 %d " % (s0 + r, s0 + r))
+                f.write(body[r].tobytes())
+    return tped, tfam
+
+
+def write_raw(path: str, geno: np.ndarray, is_case: np.ndarray, gametes: bool = False):
+    """Writes a PLINK .raw (FID IID PAT MAT SEX PHENOTYPE rs<i>_A rs<i>_HET ...,
+    phenotype 1/2) or, with gametes, a GAMETES .raw (P<i> ... Class, class 0/1)."""
+    geno = np.ascontiguousarray(geno, np.uint8)
+    snps, n = geno.shape
+    with open(path, "w") as f:
+        if gametes:
+            f.write(" ".join(["P%d" % i for i in range(snps)] + ["Class"]) + "\n")
+            for s in range(n):
+                f.write(" ".join(map(str, geno[:, s].tolist())) + " %d\n" % (1 if is_case[s] else 0))
+        else:
+            cols = []
+            for i in range(snps):
+                cols += ["rs%d_A" % i, "rs%d_HET" % i]
+            f.write("FID IID PAT MAT SEX PHENOTYPE " + " ".join(cols) + "\n")
+            het = (geno == 1).astype(np.uint8)
+            for s in range(n):
+                v = np.empty(2 * snps, np.uint8)
+                v[0::2], v[1::2] = geno[:, s], het[:, s]
+                f.write("F%d I%d 0 0 1 %d " % (s, s, 2 if is_case[s] else 1) + " ".join(map(str, v.tolist())) + "\n")
+    return path

@@ -75,6 +75,8 @@ typedef struct {
 /* Creates a context on CUDA device `device` (its own stream and scratch). */
 int fiu_create(int device, fiu_ctx **out);
 void fiu_destroy(fiu_ctx *ctx);
+/* ctx NULL: the message of this thread's last failed call made without a
+ * context (fiu_read_genotypes). */
 const char *fiu_last_error(const fiu_ctx *ctx);
 /* Sum of the GPU-side launches made by this context since creation (kernels of
  * this library only); used to report how many launches a timed region made. */
@@ -124,6 +126,31 @@ int fiu_last_tile(const fiu_ctx *ctx, int *kernel, int *tp);
  * device buffers) and derives the device layouts the kernels read. */
 int fiu_dataset_upload(fiu_ctx *ctx, const fiu_dataset *host, fiu_resident **out);
 void fiu_dataset_free(fiu_ctx *ctx, fiu_resident *res);
+/* ---- ingest: genotype files -> codes -> packed on the device -----------------
+ * fiu_read_genotypes replaces Dataset<uint64_t>::read's parsing
+ * (include/fiuncho/Dataset.h:48-94 with TPEDFile.hpp:72-296 / RAWFile.hpp:18-313):
+ * one .raw file, or a .tped + .tfam pair in either order (f2 NULL for .raw),
+ * parsed by `threads` host threads (<= 0: all cores) into minor-allele
+ * counts (snps x samples, SNP-major) and per-sample case flags, with the
+ * reference's input rules and error messages (the first failing line of the
+ * file).  ctx may be NULL: the message is then fiu_last_error(NULL). */
+typedef struct fiu_genotypes fiu_genotypes;
+int fiu_read_genotypes(fiu_ctx *ctx, const char *f1, const char *f2, int threads, fiu_genotypes **out);
+/* Sizes and host arrays of parsed genotypes (valid until fiu_genotypes_free). */
+int fiu_genotypes_info(const fiu_genotypes *g, uint64_t *snps, uint64_t *samples, const uint8_t **codes,
+                       const uint8_t **is_case);
+void fiu_genotypes_free(fiu_genotypes *g);
+/* A resident data set from genotype codes (snps x samples, values 0..2; other
+ * values match no row) and case flags: the codes are copied to the device and
+ * packed there into the reference layout (TPEDFile.hpp:176-269: per class,
+ * samples in file order, most-significant bit first, the last word
+ * right-aligned, unaligned rows), then prepared as by fiu_dataset_upload. */
+int fiu_dataset_upload_genotypes(fiu_ctx *ctx, const uint8_t *codes, const uint8_t *is_case, uint64_t snps,
+                                 uint64_t samples, fiu_resident **out);
+/* Layout of a resident data set (desc, data pointer NULL) and, when data is
+ * not NULL, a copy of its packed words (snps * 3 * (cases_words + ctrls_words)). */
+int fiu_dataset_packed(fiu_ctx *ctx, const fiu_resident *res, fiu_dataset *desc, uint64_t *data);
+
 /* 1 when every SNP's three rows are disjoint, cover each class exactly and
  * padding words are zero (the reference's own invariant, tests/dataset.cpp:25-44). */
 int fiu_dataset_is_one_hot(const fiu_resident *res);
