@@ -200,8 +200,13 @@ static int ensure_e4_items(fiu_ctx* ctx, const fiu_resident* res_c) {
 }
 
 static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
-    const bool base = res->one_hot && whole_data_set(res, w) && res->d.n_cases >= 1 && res->d.n_ctrls >= 1 &&
-                      res->d.n_cases <= 65535 && res->d.n_ctrls <= 65535 && res->d.snps < (1 << 21);
+    const bool data_ok = res->one_hot && res->d.n_cases >= 1 && res->d.n_ctrls >= 1 && res->d.n_cases <= 65535 &&
+                         res->d.n_ctrls <= 65535 && res->d.snps < (1 << 21);
+    // a Distribution layer of an order-3 scan whose classes pack: the pair kernel's list mode
+    if (data_ok && w.order == 3 && !whole_data_set(res, w) && w.dist_n == res->d.snps &&
+        tensor_pack(res->d.n_cases, res->d.n_ctrls) != 0)
+        return true;
+    const bool base = data_ok && whole_data_set(res, w);
     if (w.order == 2 || w.order == 3) return base;
     // order 4: triple cores within their limit
     return base && w.order == 4 && res->d.snps >= 4 && triples_bytes(res->d.snps) <= kMaxTriplesBytes;
@@ -239,6 +244,10 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
                 return cuda_fail(ctx, e, "tensor operand planes");
             }
             r->t3 = plan;
+        }
+        if (!whole_data_set(res, w)) {
+            cudaError_t e = tensor3_layer(*r->t3, w);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor work items of a distribution layer");
         }
         kernel = FIU_KERNEL_TENSOR;
         // GEMM width N: order 3 uses 256 with one accumulator for both classes, 192 with one per class
@@ -330,7 +339,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     ctx->last_tp = tp;
     const bool tensor = kernel == FIU_KERNEL_TENSOR;
     const bool pair_major = e4_pair_major(kernel, res, w);
-    const long long units = tensor ? tensor_units(*res->t3, (int)order) : pair_major ? res->e4_items : w.n_prefixes;
+    const long long units = tensor ? tensor_units(*res->t3, w) : pair_major ? res->e4_items : w.n_prefixes;
     int* t_status = (int*)(ctx->ctl + 16);
     if (tensor) CK(cudaMemsetAsync(t_status, 0, sizeof(int), ctx->stream), "status reset");
     const unsigned keep = outputs + std::max(32u, outputs / 8);
@@ -346,7 +355,7 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     long long thr = (long long)0x8000000000000000ull;
     unsigned have = 0;
     const double per_prefix = (double)binom(w.dist_n, order) / std::max<double>(1.0, (double)binom(w.dist_n, order - 1));
-    const double per_unit = tensor       ? tensor_item_combos(*res->t3, (int)order)
+    const double per_unit = tensor       ? tensor_item_combos(*res->t3, w)
                             : pair_major ? (double)binom(w.dist_n, 4) / std::max(1ll, res->e4_items)
                                          : per_prefix;
     // Chunk schedule.  While fewer than `keep` candidates are held every
@@ -896,7 +905,7 @@ int fiu_scan_tables(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
     if (e == cudaSuccess && kernel == FIU_KERNEL_TENSOR) {
         e = cudaMemsetAsync(ctx->ctl + 16, 0, sizeof(int), s);
         if (e == cudaSuccess)
-            e = launch_tensor3(w, *res->t3, 0, tensor_units(*res->t3, (int)order), sink, d, res->single, res->pairs,
+            e = launch_tensor3(w, *res->t3, 0, tensor_units(*res->t3, w), sink, d, res->single, res->pairs,
                                res->triples, (int*)(ctx->ctl + 16), s, ctx->sms);
     } else if (e == cudaSuccess && e4_pair_major(kernel, res, w)) {
         if ((rc = ensure_e4_items(ctx, res))) {
@@ -938,7 +947,7 @@ int fiu_scan_digest(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const
         return fail(ctx, FIU_ERR_UNSUPPORTED, "the full-table kernel's digest covers orders 2-4");
     const bool tensor = kernel == FIU_KERNEL_TENSOR;
     const bool pair_major = e4_pair_major(kernel, res, w);
-    const long long units = tensor ? tensor_units(*res->t3, (int)order) : pair_major ? res->e4_items : w.n_prefixes;
+    const long long units = tensor ? tensor_units(*res->t3, w) : pair_major ? res->e4_items : w.n_prefixes;
     // order-4 and full-table kernels assemble each table in a per-thread row
     // (2 x 81 words) of scratch: room for every thread the launch can hold
     const bool scratch = order == 4 || kernel == FIU_KERNEL_FULL;

@@ -172,6 +172,7 @@ struct T3Plan {
     int pitch = 0;        // bytes per plane row
     int k_cases = 0;      // padded case samples (= byte offset of the control region)
     bool pair3 = false;   // order 3, packed classes: pair items (i, 64 j, 128 l) of the CTA-pair kernel
+    struct T3Layers* layers = nullptr;  // order 3, packed: work items of Distribution layers (tensor3.cu)
     long long* item_begin = nullptr;
     long long total = 0;  // work items
     CUtensorMap map_l;    // box 128 B x 192 rows (256 when packed), 128-byte swizzle (l operand)
@@ -197,8 +198,16 @@ struct T3Plan {
 // log2 of the control weight W = 4^h when both classes fit one FP32 accumulator
 // (n_cases < W, n_cases + W * n_ctrls < 2^24), else 0.
 int tensor_pack(int n_cases, int n_ctrls);
-long long tensor_units(const T3Plan& plan, int order);
-double tensor_item_combos(const T3Plan& plan, int order);
+// Work units of a request on the tensor kernels (w's order and Distribution
+// layer; a layer's items must have been made by tensor3_layer), and the
+// combinations of an average unit.
+long long tensor_units(const T3Plan& plan, const ScanWork& w);
+double tensor_item_combos(const T3Plan& plan, const ScanWork& w);
+// Whether the tensor kernels serve the Distribution layer of w (order 3,
+// classes that pack, the layer of all SNPs), and the layer's work items,
+// made on first use (host enumeration of the owned prefixes).
+bool tensor_layer_ok(const T3Plan& plan, const ScanWork& w);
+cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w);
 cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s);
 void tensor3_release(T3Plan& plan);
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,

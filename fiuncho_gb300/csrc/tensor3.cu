@@ -52,6 +52,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "tensor_common.cuh"
 
@@ -219,7 +221,9 @@ __device__ __forceinline__ void t3_eval(const ScanWork& w, const CandSink& sink,
         }
         pass = key >= sink.thr;
         if (dump) {
-            uint32_t* o = dump + ((size_t)pair_index(i, j, n) * n + l) * 54;
+            // owned prefix ordinal m of (i, j): rank offset + m * step
+            const size_t m = (size_t)((pair_index(i, j, n) - w.dist_offset) / w.dist_step);
+            uint32_t* o = dump + (m * n + l) * 54;
 #pragma unroll
             for (int c = 0; c < 27; ++c) {
                 o[c] = f2u(t[0][c]);
@@ -629,11 +633,51 @@ __device__ __forceinline__ void t3x_decode(const long long* __restrict__ item_be
     }
 }
 
+// List mode (a Distribution layer): the owned j of each i are listed in
+// jlist[jl_begin[i] .. jl_begin[i+1]); an item takes 64 consecutive entries
+// from p0 (= jl_begin[i] + 64 a) and an l-tile l0 = jlist[p0] + 1 + 128 b.
+__device__ __forceinline__ void t3l_decode(const long long* __restrict__ item_begin,
+                                           const long long* __restrict__ jl_begin, const int* __restrict__ jlist,
+                                           int n, long long g, int& i, long long& p0, int& l0) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (item_begin[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    i = lo;
+    long long q = g - item_begin[i];
+    for (long long p = jl_begin[i];; p += kPxJ) {
+        const int jf = jlist[p];
+        const long long nl = (n - 1 - jf + kPL - 1) / kPL;
+        if (q < nl) {
+            p0 = p;
+            l0 = jf + 1 + kPL * (int)q;
+            return;
+        }
+        q -= nl;
+    }
+}
+
+// The j of row jj (0..31) of this CTA's half of an item: the listed entry, or
+// n when the list of i ends before it.
+template <bool LIST>
+__device__ __forceinline__ int t3x_j(int j0, long long p0, long long p_end, const int* __restrict__ jlist, int jj,
+                                     int n) {
+    if (!LIST) return j0 + jj;
+    const long long p = p0 + jj;
+    return p < p_end ? __ldg(jlist + p) : n;
+}
+
+// LIST: the list mode above (the j rows are fetched row by row with bulk
+// copies, unswizzled, from the operand planes at `planes` with `pitch`).
+template <bool LIST>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
     tensor3x_kernel(const __grid_constant__ T3Maps maps, const __grid_constant__ CUtensorMap map_lh, ScanWork w,
                     const long long* __restrict__ item_begin, long long g0, long long g1, int k_cases, int pack,
                     CandSink sink, float thr_f, uint32_t* dump, const uint32_t* __restrict__ single,
-                    const uint4* __restrict__ pairs, int* status) {
+                    const uint4* __restrict__ pairs, int* status, const long long* __restrict__ jl_begin,
+                    const int* __restrict__ jlist, const uint8_t* __restrict__ planes, int pitch) {
     extern __shared__ uint8_t smraw[];
     __shared__ __align__(8) uint64_t full_t[kPxStages], full_a[kPxStages], empty[kPxStages];
     __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done;
@@ -680,35 +724,65 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
 
     if (warp == 0) {
         // ---------------------------------------------------------------- TMA producer (both CTAs)
-        if (lane == 0) {
+        // (list mode: the whole warp, each lane fetching the two plane rows of one j)
+        if (LIST || lane == 0) {
             long long step = 0;
             for (long long g = g0 + cid; g < g1 && ok; g += ncl) {
-                int i, j0, l0;
-                t3x_decode(item_begin, n, g, i, j0, l0);
+                int i, j0 = 0, l0;
+                long long p0 = 0, p_end = 0;
+                if (LIST) {
+                    t3l_decode(item_begin, jl_begin, jlist, n, g, i, p0, l0);
+                    p0 += kT3J * (int)rank;
+                    p_end = jl_begin[i + 1];
+                } else {
+                    t3x_decode(item_begin, n, g, i, j0, l0);
+                }
+                const int my_j = LIST ? t3x_j<true>(0, p0, p_end, jlist, lane, n) : 0;
+                const int n_j = LIST ? (int)max(0ll, min((long long)kT3J, p_end - p0)) : kT3J;
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const int s = (int)(step % kPxStages);
                     const long long u = step / kPxStages;
-                    if (u > 0 && !t3_wait_cl(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
+                    bool waited = true;
+                    if (lane == 0 && u > 0) waited = t3_wait_cl(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort);
+                    if (LIST) waited = __shfl_sync(0xffffffffu, waited, 0);
+                    if (!waited) {
                         ok = false;
                         break;
                     }
                     const int k0 = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
                     uint8_t* st = sm + s * kPxStage;
                     const uint32_t bar = smem_u32(&full_t[s]);
-                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                                 "r"((uint32_t)(kPxSB + kT3SJ + 2 * kT3KB))
-                                 : "memory");
-                    t3_tma(smem_u32(st), &map_lh, k0, 2 * l0 + kPxBRows * (int)rank, bar);
-                    t3_tma(smem_u32(st + kPxSB + kPSA), &maps.j, k0, 2 * (j0 + kT3J * (int)rank), bar);
-                    t3_tma(smem_u32(st + kPxSB + kPSA + kT3SJ), &maps.i, k0, 2 * i, bar);
+                    if (lane == 0) {
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                                     "r"((uint32_t)(kPxSB + 2 * kT3KB * n_j + 2 * kT3KB))
+                                     : "memory");
+                        t3_tma(smem_u32(st), &map_lh, k0, 2 * l0 + kPxBRows * (int)rank, bar);
+                        if (!LIST) t3_tma(smem_u32(st + kPxSB + kPSA), &maps.j, k0, 2 * (j0 + kT3J * (int)rank), bar);
+                        t3_tma(smem_u32(st + kPxSB + kPSA + kT3SJ), &maps.i, k0, 2 * i, bar);
+                    }
+                    if (LIST && lane < n_j) {
+                        const uint8_t* src = planes + (size_t)(2 * my_j) * pitch + k0;
+                        const uint32_t dst = smem_u32(st + kPxSB + kPSA + 2 * lane * kT3KB);
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                dst),
+                            "l"(src), "r"(kT3KB), "r"(bar)
+                            : "memory");
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                dst + kT3KB),
+                            "l"(src + pitch), "r"(kT3KB), "r"(bar)
+                            : "memory");
+                    }
                     ++step;
                 }
             }
-            for (int s = 0; s < kPxStages; ++s) {
-                if (step <= s) continue;
-                const long long last = s + ((step - 1 - s) / kPxStages) * kPxStages;
-                if (!t3_drain(smem_u32(&full_t[s]), (uint32_t)((last / kPxStages) & 1))) ok = false;
-            }
+            if (lane == 0)
+                for (int s = 0; s < kPxStages; ++s) {
+                    if (step <= s) continue;
+                    const long long last = s + ((step - 1 - s) / kPxStages) * kPxStages;
+                    if (!t3_drain(smem_u32(&full_t[s]), (uint32_t)((last / kPxStages) & 1))) ok = false;
+                }
         }
     } else if (warp == 1) {
         // ---------------------------------------------------------------- MMA issuer (CTA 0)
@@ -776,7 +850,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
 #pragma unroll
                 for (int u = 0; u < kRows; ++u) {
                     const int r = (t >> 3) + 4 * kPBuildWarps * u;
-                    if (r < 2 * kT3J) jrow[u] = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((c ^ (r & 7)) << 4));
+                    // list mode: rows copied row by row, not swizzled
+                    if (r < 2 * kT3J)
+                        jrow[u] = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((LIST ? c : (c ^ (r & 7))) << 4));
                 }
 #pragma unroll
                 for (int u = 0; u < kRows; ++u) {
@@ -816,9 +892,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
         uint4* stage = reinterpret_cast<uint4*>(ebuf_all + kT3EpiWarps * (kT3Ebuf / 4));
         long long item = 0;
         for (long long g = g0 + cid; g < g1 && ok; g += ncl, ++item) {
-            int i, j0, l0;
-            t3x_decode(item_begin, n, g, i, j0, l0);
-            j0 += kT3J * (int)rank;
+            int i, j0 = 0, l0;
+            long long p0 = 0, p_end = 0;
+            if (LIST) {
+                t3l_decode(item_begin, jl_begin, jlist, n, g, i, p0, l0);
+                p0 += kT3J * (int)rank;
+                p_end = jl_begin[i + 1];
+            } else {
+                t3x_decode(item_begin, n, g, i, j0, l0);
+                j0 += kT3J * (int)rank;
+            }
             const int buf = (int)(item & 1);
             asm volatile("bar.sync 1, %0;" ::"n"(32 * kT3EpiWarps) : "memory");
             {
@@ -829,7 +912,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
                 }
             }
             asm volatile("bar.sync 1, %0;" ::"n"(32 * kT3EpiWarps) : "memory");
-            const int j = j0 + 8 * q + jl;
+            const int j = t3x_j<LIST>(j0, p0, p_end, jlist, 8 * q + jl, n);
             const bool j_ok = j < n;
             uint4 pij;
             float si[2][2], sj[2][2];
@@ -1703,14 +1786,104 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
     return t3_map(&plan.map_k4, plan.planes, rows, plan.pitch, 32, true);
 }
 
-long long tensor_units(const T3Plan& plan, int order) {
-    return order == 2 ? plan.total2 : order == 4 ? plan.total4 : plan.total;
+// Work items of Distribution layers of order-3 scans (the pair kernel's list
+// mode), one entry per (step, offset) used on the data set.
+struct T3Layer {
+    long long* item_begin = nullptr;  // [n + 1] first item of each i
+    long long* jl_begin = nullptr;    // [n + 1] first listed j of each i
+    int* jlist = nullptr;             // owned j of each i, ascending
+    long long total = 0;
+    double item_combos = 0;
+};
+struct T3Layers {
+    std::mutex mu;
+    std::map<std::pair<int, int>, T3Layer> by;
+};
+
+static bool is_layer(const ScanWork& w) { return w.dist_step != 1 || w.dist_offset != 0; }
+
+bool tensor_layer_ok(const T3Plan& plan, const ScanWork& w) {
+    return w.order == 3 && plan.pair3 && w.dist_n == w.d.snps;
 }
-double tensor_item_combos(const T3Plan& plan, int order) {
-    return order == 2 ? plan.item2_combos : order == 4 ? plan.item4_combos : plan.item_combos;
+
+static const T3Layer* find_layer(const T3Plan& plan, const ScanWork& w) {
+    if (!plan.layers) return nullptr;
+    std::lock_guard<std::mutex> g(plan.layers->mu);
+    auto it = plan.layers->by.find({w.dist_step, w.dist_offset});
+    return it == plan.layers->by.end() ? nullptr : &it->second;
+}
+
+cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w) {
+    if (!tensor_layer_ok(plan, w)) return cudaErrorInvalidValue;
+    if (!plan.layers) plan.layers = new T3Layers;
+    std::lock_guard<std::mutex> g(plan.layers->mu);
+    if (plan.layers->by.count({w.dist_step, w.dist_offset})) return cudaSuccess;
+    // owned prefixes (i, j): lexicographic ranks offset + m * step; the pairs
+    // (i, j > i) have ranks base(i) + (j - i - 1), base(i) = i (n-1) - i (i-1) / 2
+    const int n = w.d.snps;
+    const long long step = w.dist_step, offset = w.dist_offset;
+    std::vector<long long> ib((size_t)n + 1), jb((size_t)n + 1);
+    std::vector<int> jl;
+    long long total = 0, combos = 0;
+    for (int i = 0; i < n; ++i) {
+        ib[i] = total;
+        jb[i] = (long long)jl.size();
+        const long long base = (long long)i * (n - 1) - (long long)i * (i - 1) / 2, cnt = n - 1 - i;
+        long long t = std::max(0ll, offset - base);
+        t += ((offset - base - t) % step + step) % step;  // first t with base + t = offset (mod step)
+        for (; t < cnt; t += step) {
+            jl.push_back(i + 1 + (int)t);
+            combos += n - 2 - i - t;
+        }
+        for (size_t a = (size_t)jb[i]; a < jl.size(); a += kPxJ) total += (n - 1 - jl[a] + kPL - 1) / kPL;
+    }
+    ib[n] = total;
+    jb[n] = (long long)jl.size();
+    T3Layer L;
+    L.total = total;
+    L.item_combos = (double)combos / std::max(1ll, total);
+    cudaError_t e = cudaMalloc((void**)&L.item_begin, ib.size() * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&L.jl_begin, jb.size() * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&L.jlist, std::max<size_t>(1, jl.size()) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(L.item_begin, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(L.jl_begin, jb.data(), jb.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !jl.empty())
+        e = cudaMemcpy(L.jlist, jl.data(), jl.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(L.item_begin);
+        cudaFree(L.jl_begin);
+        cudaFree(L.jlist);
+        return e;
+    }
+    plan.layers->by[{w.dist_step, w.dist_offset}] = L;
+    return cudaSuccess;
+}
+
+long long tensor_units(const T3Plan& plan, const ScanWork& w) {
+    if (w.order == 3 && is_layer(w)) {
+        const T3Layer* L = find_layer(plan, w);
+        return L ? L->total : 0;
+    }
+    return w.order == 2 ? plan.total2 : w.order == 4 ? plan.total4 : plan.total;
+}
+double tensor_item_combos(const T3Plan& plan, const ScanWork& w) {
+    if (w.order == 3 && is_layer(w)) {
+        const T3Layer* L = find_layer(plan, w);
+        return L ? L->item_combos : 1.0;
+    }
+    return w.order == 2 ? plan.item2_combos : w.order == 4 ? plan.item4_combos : plan.item_combos;
 }
 
 void tensor3_release(T3Plan& plan) {
+    if (plan.layers) {
+        for (auto& kv : plan.layers->by) {
+            cudaFree(kv.second.item_begin);
+            cudaFree(kv.second.jl_begin);
+            cudaFree(kv.second.jlist);
+        }
+        delete plan.layers;
+        plan.layers = nullptr;
+    }
     cudaFree(plan.planes);
     cudaFree(plan.item_begin);
     cudaFree(plan.item2_begin);
@@ -1850,7 +2023,9 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(tensor2x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2xSmem);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(tensor3x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPxSmem);
+            e = cudaFuncSetAttribute(tensor3x_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPxSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tensor3x_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPxSmem);
         return e;
     }();
     if (attr != cudaSuccess) return attr;
@@ -1879,11 +2054,22 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     }
     T3Maps maps{plan.map_l, plan.map_j, plan.map_i};
     if (plan.pair3) {
-        static const int max_clusters = pair_clusters(tensor3x_kernel, kPThreads, kPxSmem);
+        static const int max_clusters = pair_clusters(tensor3x_kernel<false>, kPThreads, kPxSmem);
         const long long clusters = std::min<long long>(items, max_clusters > 0 ? max_clusters : sms / 2);
-        tensor3x_kernel<<<(unsigned)(2 * std::max(1ll, clusters)), kPThreads, kPxSmem, s>>>(
-            maps, plan.map_a2, w, plan.item_begin, g0, g1, plan.k_cases, plan.pack, sink, thr_f, dump, single, pairs,
-            status);
+        const unsigned grid2 = (unsigned)(2 * std::max(1ll, clusters));
+        if (is_layer(w)) {
+            const T3Layer* L = find_layer(plan, w);
+            if (!L || !tensor_layer_ok(plan, w)) return cudaErrorInvalidValue;
+            tensor3x_kernel<true><<<grid2, kPThreads, kPxSmem, s>>>(maps, plan.map_a2, w, L->item_begin, g0, g1,
+                                                                    plan.k_cases, plan.pack, sink, thr_f, dump, single,
+                                                                    pairs, status, L->jl_begin, L->jlist, plan.planes,
+                                                                    plan.pitch);
+        } else {
+            tensor3x_kernel<false><<<grid2, kPThreads, kPxSmem, s>>>(maps, plan.map_a2, w, plan.item_begin, g0, g1,
+                                                                     plan.k_cases, plan.pack, sink, thr_f, dump,
+                                                                     single, pairs, status, nullptr, nullptr, nullptr,
+                                                                     plan.pitch);
+        }
         count_launch();
         return cudaGetLastError();
     }

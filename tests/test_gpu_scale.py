@@ -61,7 +61,7 @@ def test_digest_every_kernel(gs, golden_synth, order, kernel):
     assert dg == int(golden_synth["o%d_digest" % order])
 
 
-@pytest.mark.parametrize("kernel", [K_POPC, K_HS, K_FULL])
+@pytest.mark.parametrize("kernel", [K_TENSOR, K_AUTO, K_POPC, K_HS, K_FULL])
 def test_digest_distribution_layer(gs, golden_synth, kernel):
     """The tables of the combinations a Distribution(48, 2, 3, 2) layer owns."""
     from fiuncho_gb300 import Dataset, Distribution

@@ -414,9 +414,10 @@ def test_order4_reduced_work_is_automatic(gs, golden_synth):
 
 
 def test_tensor_kernel_scope(gs, golden_synth):
-    """The tcgen05 kernel serves one-hot order-3 searches of the whole data set by one
-    worker; a step > 1 distribution falls back to the reduced-work kernel automatically
-    and is refused when the tensor kernel is forced."""
+    """The tcgen05 kernels serve one-hot order-2/3/4 searches of the whole data set, and
+    order-3 Distribution layers of all SNPs when the classes pack (the pair kernel's
+    list mode); other layers fall back to the reduced-work kernel automatically and
+    are refused when the tensor kernel is forced."""
     from fiuncho_gb300 import Dataset, Distribution, FiunchoError, GpuSearch, Resident
     ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
     g = GpuSearch(0)
@@ -424,14 +425,46 @@ def test_tensor_kernel_scope(gs, golden_synth):
     g.run(res, 3, Distribution(ds.snps, 2), 10)
     assert g.last_tile()[0] == 4
     g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
+    assert g.last_tile()[0] == 4
+    g.run(res, 3, Distribution(ds.snps - 5, 2, 2, 1), 10)  # a layer of the first n - 5 SNPs
+    assert g.last_tile()[0] in (2, 3)
+    g.run(res, 2, Distribution(ds.snps, 1, 2, 0), 10)
     assert g.last_tile()[0] in (2, 3)
     g.run(res, 2, Distribution(ds.snps, 1), 10)
     assert g.last_tile()[0] == 4
     g.set_kernel(4)
+    g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
     with pytest.raises(FiunchoError):
-        g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
+        g.run(res, 2, Distribution(ds.snps, 1, 2, 1), 10)
     with pytest.raises(FiunchoError):
         g.run(res, 5, Distribution(ds.snps, 4), 10)
+
+
+@pytest.mark.parametrize("n_ranks", [2, 3, 4, 5, 6, 7])
+def test_rank_layers_on_the_tensor_kernel(oracle, n_ranks):
+    """MPIEngine gives rank r of N the strided share Distribution(snps, 2, N, r)
+    (MPIEngine.h:133-134, Distribution.h:172-176): on the tensor kernel (list mode),
+    forced and automatic, every rank's list equals the oracle's list of that rank,
+    and the ranks' lists merged as MPIEngine merges them give the whole search."""
+    from fiuncho_gb300 import Dataset, Distribution, GpuSearch, MPIEngine, Resident
+    rng = np.random.default_rng(100 + n_ranks)
+    snps, nc, nt = 170, 1300, 1217
+    maf = rng.uniform(0.05, 0.5, snps)[:, None]
+    u = rng.random((snps, nc + nt))
+    geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
+    ds = Dataset.from_genotypes(geno, np.r_[np.ones(nc, np.uint8), np.zeros(nt, np.uint8)])
+    parts = []
+    for kernel in (4, 0):
+        g = GpuSearch(0, kernel=kernel)
+        res = Resident(g.ctx, ds)
+        for r in range(n_ranks):
+            out, v64 = g.run(res, 3, Distribution(snps, 2, n_ranks, r), 30, with_fp64=True)
+            assert g.last_tile()[0] == 4
+            _check_topn(oracle, ds, 3, 30, out, v64, dist=(snps, n_ranks, r))
+            if kernel == 0:
+                parts += out
+    whole = GpuSearch(0).run(ds, 3, Distribution(snps, 2), 30)
+    assert [x.combination for x in MPIEngine().gather(parts, 30)] == [x.combination for x in whole]
 
 
 def test_elided_rejects_non_one_hot(gs):
