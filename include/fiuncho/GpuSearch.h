@@ -18,11 +18,14 @@
  * CPU fallback: without a usable GPU the constructor throws.
  *
  * Multi-GPU: MPIEngine gives rank r of N the strided prefix share
- * Distribution(snps, order-1, N, r), which the whole-data-set tensor-core
- * kernels cannot serve.  With shard_ranks = true such a rank share runs as
- * shard r of N of the whole search instead (fiu_search_shard: equal ranges of
- * the tensor-core work units); the rank's own list then differs from the
- * strided share's, but MPIEngine's gathered result is the same:
+ * Distribution(snps, order-1, N, r) (MPIEngine.h:133-134).  For order 3 with
+ * classes that share one accumulator the tensor-core kernel serves such a
+ * share itself (its list mode), with the reference's per-rank list; other
+ * shares run on the CUDA-core kernels.  With shard_ranks = true a rank share
+ * runs as shard r of N of the whole search instead (fiu_search_shard: equal
+ * ranges of the tensor-core work units, every order); the rank's own list
+ * then differs from the strided share's, but MPIEngine's gathered result is
+ * the same:
  *
  *     engine.run<GpuSearch>({tped, tfam}, order, outputs, local_rank, true);
  */
