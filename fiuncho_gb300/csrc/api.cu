@@ -246,7 +246,7 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
             r->t3 = plan;
         }
         if (!whole_data_set(res, w)) {
-            cudaError_t e = tensor3_layer(*r->t3, w);
+            cudaError_t e = tensor3_layer(*r->t3, w, ctx->stream);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor work items of a distribution layer");
         }
         kernel = FIU_KERNEL_TENSOR;
@@ -363,9 +363,10 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
     // the `seen` combinations so far, and about keep / seen of the next
     // chunk's combinations pass it.  Chunks are sized for a quarter of the
     // candidate buffer under that estimate (a chunk that overflows all the
-    // same is re-run in smaller pieces), so a scan takes a few launches.  A
-    // chunk also stays under about a quarter second (measured per unit on the
-    // previous chunk), so that a cancellation takes effect soon.
+    // same is re-run in smaller pieces), so a scan takes a few launches and
+    // the same launches on every run.  On a context whose searches can be
+    // cancelled a chunk also stays under about a quarter second (measured per
+    // unit on the previous chunk), so that a cancellation takes effect soon.
     long long chunk = std::max<long long>(1, (long long)(keep / std::max(1.0, per_unit)));
     double seen = 0, sec_per_unit = 0;
     long long m = units / n_shards * shard + std::min<long long>(shard, units % n_shards);
@@ -420,7 +421,8 @@ int search_impl(fiu_ctx* ctx, const fiu_resident* res, unsigned order, const fiu
         m = m1;
         const double next = have < keep ? (double)(cap - have) / (4.0 * std::max(1.0, per_unit))
                                         : (double)cap / 4.0 * seen / ((double)keep * std::max(1.0, per_unit));
-        chunk = (long long)std::max(1.0, std::min({next, 0.25 / std::max(sec_per_unit, 1e-12), 4.0e18}));
+        const double time_cap = ctx->cancellable ? 0.25 / std::max(sec_per_unit, 1e-12) : 4.0e18;
+        chunk = (long long)std::max(1.0, std::min({next, time_cap, 4.0e18}));
     }
     if (tensor) {
         int st = 0;

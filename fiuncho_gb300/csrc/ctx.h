@@ -46,6 +46,10 @@ struct fiu_ctx {
     // set by another thread to stop the search running on this context after
     // its current chunk (FIU_ERR_CANCELLED)
     std::atomic<int> cancel{0};
+    // searches on this context may be cancelled (the server's solo lanes):
+    // their chunks are also kept under about a quarter second, so a cancel
+    // takes effect soon.  Elsewhere the chunk schedule depends on the data only.
+    bool cancellable = false;
 };
 
 struct fiu_resident {

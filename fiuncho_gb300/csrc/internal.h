@@ -205,9 +205,10 @@ long long tensor_units(const T3Plan& plan, const ScanWork& w);
 double tensor_item_combos(const T3Plan& plan, const ScanWork& w);
 // Whether the tensor kernels serve the Distribution layer of w (order 3,
 // classes that pack, the layer of all SNPs), and the layer's work items,
-// made on first use (host enumeration of the owned prefixes).
+// made on first use (host enumeration of the owned prefixes; the operand
+// planes ordered by SNP residue mod the layer's step, copied on stream s).
 bool tensor_layer_ok(const T3Plan& plan, const ScanWork& w);
-cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w);
+cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s);
 cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s);
 void tensor3_release(T3Plan& plan);
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,

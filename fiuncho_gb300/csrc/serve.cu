@@ -425,6 +425,8 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
             fiu_destroy(sv->ctx);
             delete sv;
             return rc;
+        } else {
+            sv->solo_ctx[l]->cancellable = true;
         }
     cudaSetDevice(device);
     if (cudaMalloc((void**)&sv->d_desc, kSlots * sizeof(ScanDesc)) != cudaSuccess ||

@@ -633,6 +633,14 @@ __device__ __forceinline__ void t3x_decode(const long long* __restrict__ item_be
     }
 }
 
+// Row (SNP position) of SNP j in the operand planes ordered by residue mod
+// step (SNPs r, r + step, .. for r = 0, 1, ..; residue r holds
+// n / step + (r < n % step) SNPs).
+__host__ __device__ __forceinline__ int residue_row(int j, int step, int n) {
+    const int r = j % step;
+    return r * (n / step) + min(r, n % step) + j / step;
+}
+
 // List mode (a Distribution layer): the owned j of each i are listed in
 // jlist[jl_begin[i] .. jl_begin[i+1]); an item takes 64 consecutive entries
 // from p0 (= jl_begin[i] + 64 a) and an l-tile l0 = jlist[p0] + 1 + 128 b.
@@ -669,15 +677,15 @@ __device__ __forceinline__ int t3x_j(int j0, long long p0, long long p_end, cons
     return p < p_end ? __ldg(jlist + p) : n;
 }
 
-// LIST: the list mode above (the j rows are fetched row by row with bulk
-// copies, unswizzled, from the operand planes at `planes` with `pitch`).
+// LIST: the list mode above (maps.j then covers the residue-ordered planes,
+// where the listed j of one i are consecutive rows).
 template <bool LIST>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
     tensor3x_kernel(const __grid_constant__ T3Maps maps, const __grid_constant__ CUtensorMap map_lh, ScanWork w,
                     const long long* __restrict__ item_begin, long long g0, long long g1, int k_cases, int pack,
                     CandSink sink, float thr_f, uint32_t* dump, const uint32_t* __restrict__ single,
                     const uint4* __restrict__ pairs, int* status, const long long* __restrict__ jl_begin,
-                    const int* __restrict__ jlist, const uint8_t* __restrict__ planes, int pitch) {
+                    const int* __restrict__ jlist) {
     extern __shared__ uint8_t smraw[];
     __shared__ __align__(8) uint64_t full_t[kPxStages], full_a[kPxStages], empty[kPxStages];
     __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done;
@@ -724,56 +732,37 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
 
     if (warp == 0) {
         // ---------------------------------------------------------------- TMA producer (both CTAs)
-        // (list mode: the whole warp, each lane fetching the two plane rows of one j)
-        if (LIST || lane == 0) {
+        if (lane == 0) {
             long long step = 0;
             for (long long g = g0 + cid; g < g1 && ok; g += ncl) {
                 int i, j0 = 0, l0;
-                long long p0 = 0, p_end = 0;
                 if (LIST) {
+                    long long p0;
                     t3l_decode(item_begin, jl_begin, jlist, n, g, i, p0, l0);
+                    // this CTA's 32 listed j: consecutive residue-ordered rows from its first one (rows
+                    // past the end of i's list are loaded too and ignored by the epilogue)
                     p0 += kT3J * (int)rank;
-                    p_end = jl_begin[i + 1];
+                    j0 = p0 < jl_begin[i + 1] ? residue_row(jlist[p0], w.dist_step, n) : 0;
                 } else {
                     t3x_decode(item_begin, n, g, i, j0, l0);
+                    j0 += kT3J * (int)rank;
                 }
-                const int my_j = LIST ? t3x_j<true>(0, p0, p_end, jlist, lane, n) : 0;
-                const int n_j = LIST ? (int)max(0ll, min((long long)kT3J, p_end - p0)) : kT3J;
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const int s = (int)(step % kPxStages);
                     const long long u = step / kPxStages;
-                    bool waited = true;
-                    if (lane == 0 && u > 0) waited = t3_wait_cl(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort);
-                    if (LIST) waited = __shfl_sync(0xffffffffu, waited, 0);
-                    if (!waited) {
+                    if (u > 0 && !t3_wait_cl(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), abort)) {
                         ok = false;
                         break;
                     }
                     const int k0 = ks < ks_c ? ks * kT3KB : k_cases + (ks - ks_c) * kT3KB;
                     uint8_t* st = sm + s * kPxStage;
                     const uint32_t bar = smem_u32(&full_t[s]);
-                    if (lane == 0) {
-                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                                     "r"((uint32_t)(kPxSB + 2 * kT3KB * n_j + 2 * kT3KB))
-                                     : "memory");
-                        t3_tma(smem_u32(st), &map_lh, k0, 2 * l0 + kPxBRows * (int)rank, bar);
-                        if (!LIST) t3_tma(smem_u32(st + kPxSB + kPSA), &maps.j, k0, 2 * (j0 + kT3J * (int)rank), bar);
-                        t3_tma(smem_u32(st + kPxSB + kPSA + kT3SJ), &maps.i, k0, 2 * i, bar);
-                    }
-                    if (LIST && lane < n_j) {
-                        const uint8_t* src = planes + (size_t)(2 * my_j) * pitch + k0;
-                        const uint32_t dst = smem_u32(st + kPxSB + kPSA + 2 * lane * kT3KB);
-                        asm volatile(
-                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                                dst),
-                            "l"(src), "r"(kT3KB), "r"(bar)
-                            : "memory");
-                        asm volatile(
-                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                                dst + kT3KB),
-                            "l"(src + pitch), "r"(kT3KB), "r"(bar)
-                            : "memory");
-                    }
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                                 "r"((uint32_t)(kPxSB + kT3SJ + 2 * kT3KB))
+                                 : "memory");
+                    t3_tma(smem_u32(st), &map_lh, k0, 2 * l0 + kPxBRows * (int)rank, bar);
+                    t3_tma(smem_u32(st + kPxSB + kPSA), &maps.j, k0, 2 * j0, bar);
+                    t3_tma(smem_u32(st + kPxSB + kPSA + kT3SJ), &maps.i, k0, 2 * i, bar);
                     ++step;
                 }
             }
@@ -850,9 +839,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
 #pragma unroll
                 for (int u = 0; u < kRows; ++u) {
                     const int r = (t >> 3) + 4 * kPBuildWarps * u;
-                    // list mode: rows copied row by row, not swizzled
-                    if (r < 2 * kT3J)
-                        jrow[u] = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((LIST ? c : (c ^ (r & 7))) << 4));
+                    if (r < 2 * kT3J) jrow[u] = *reinterpret_cast<const uint4*>(sJ + r * 128 + ((c ^ (r & 7)) << 4));
                 }
 #pragma unroll
                 for (int u = 0; u < kRows; ++u) {
@@ -1787,18 +1774,26 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
 }
 
 // Work items of Distribution layers of order-3 scans (the pair kernel's list
-// mode), one entry per (step, offset) used on the data set.
+// mode), one entry per (step, offset) used on the data set.  The owned j of
+// one i are the j > i of one residue mod step (pair ranks base(i) + j - i - 1
+// step through the layer's offset class), so in a copy of the operand planes
+// ordered by residue -- SNPs r, r + step, r + 2 step, .. for r = 0, 1, .. --
+// they are consecutive rows, and one tiled TMA copy per stage loads an item's
+// j rows as in the scan of all prefixes.
 struct T3Layer {
     long long* item_begin = nullptr;  // [n + 1] first item of each i
     long long* jl_begin = nullptr;    // [n + 1] first listed j of each i
     int* jlist = nullptr;             // owned j of each i, ascending
     long long total = 0;
     double item_combos = 0;
+    CUtensorMap map_jr;               // box 128 B x 64 rows over the residue-ordered planes
 };
 struct T3Layers {
     std::mutex mu;
     std::map<std::pair<int, int>, T3Layer> by;
+    std::map<int, uint8_t*> by_residue;  // residue-ordered operand planes per step
 };
+
 
 static bool is_layer(const ScanWork& w) { return w.dist_step != 1 || w.dist_offset != 0; }
 
@@ -1813,11 +1808,28 @@ static const T3Layer* find_layer(const T3Plan& plan, const ScanWork& w) {
     return it == plan.layers->by.end() ? nullptr : &it->second;
 }
 
-cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w) {
+cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s) {
     if (!tensor_layer_ok(plan, w)) return cudaErrorInvalidValue;
     if (!plan.layers) plan.layers = new T3Layers;
     std::lock_guard<std::mutex> g(plan.layers->mu);
     if (plan.layers->by.count({w.dist_step, w.dist_offset})) return cudaSuccess;
+    uint8_t*& perm = plan.layers->by_residue[w.dist_step];
+    if (!perm) {
+        // residue class r holds SNPs r + step m, m < ceil((n - r) / step), each as its 2 plane rows
+        const int n = w.d.snps, step = w.dist_step;
+        const size_t row2 = (size_t)2 * plan.pitch;
+        cudaError_t e = cudaMalloc((void**)&perm, (size_t)n * row2);
+        for (int r = 0; r < step && r < n && e == cudaSuccess; ++r)
+            e = cudaMemcpy2DAsync(perm + (size_t)residue_row(r, step, n) * row2, row2, plan.planes + (size_t)r * row2,
+                                  (size_t)step * row2, row2, (size_t)((n - r + step - 1) / step),
+                                  cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            cudaFree(perm);
+            plan.layers->by_residue.erase(w.dist_step);
+            return e;
+        }
+    }
     // owned prefixes (i, j): lexicographic ranks offset + m * step; the pairs
     // (i, j > i) have ranks base(i) + (j - i - 1), base(i) = i (n-1) - i (i-1) / 2
     const int n = w.d.snps;
@@ -1842,7 +1854,8 @@ cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w) {
     T3Layer L;
     L.total = total;
     L.item_combos = (double)combos / std::max(1ll, total);
-    cudaError_t e = cudaMalloc((void**)&L.item_begin, ib.size() * sizeof(long long));
+    cudaError_t e = t3_map(&L.map_jr, perm, 2 * n, plan.pitch, 2 * kT3J, true);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&L.item_begin, ib.size() * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&L.jl_begin, jb.size() * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&L.jlist, std::max<size_t>(1, jl.size()) * sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(L.item_begin, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
@@ -1881,6 +1894,7 @@ void tensor3_release(T3Plan& plan) {
             cudaFree(kv.second.jl_begin);
             cudaFree(kv.second.jlist);
         }
+        for (auto& kv : plan.layers->by_residue) cudaFree(kv.second);
         delete plan.layers;
         plan.layers = nullptr;
     }
@@ -2060,15 +2074,14 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
         if (is_layer(w)) {
             const T3Layer* L = find_layer(plan, w);
             if (!L || !tensor_layer_ok(plan, w)) return cudaErrorInvalidValue;
-            tensor3x_kernel<true><<<grid2, kPThreads, kPxSmem, s>>>(maps, plan.map_a2, w, L->item_begin, g0, g1,
+            const T3Maps lmaps{plan.map_l, L->map_jr, plan.map_i};
+            tensor3x_kernel<true><<<grid2, kPThreads, kPxSmem, s>>>(lmaps, plan.map_a2, w, L->item_begin, g0, g1,
                                                                     plan.k_cases, plan.pack, sink, thr_f, dump, single,
-                                                                    pairs, status, L->jl_begin, L->jlist, plan.planes,
-                                                                    plan.pitch);
+                                                                    pairs, status, L->jl_begin, L->jlist);
         } else {
             tensor3x_kernel<false><<<grid2, kPThreads, kPxSmem, s>>>(maps, plan.map_a2, w, plan.item_begin, g0, g1,
                                                                      plan.k_cases, plan.pack, sink, thr_f, dump,
-                                                                     single, pairs, status, nullptr, nullptr, nullptr,
-                                                                     plan.pitch);
+                                                                     single, pairs, status, nullptr, nullptr);
         }
         count_launch();
         return cudaGetLastError();
