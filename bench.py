@@ -212,6 +212,18 @@ def run_gpu(args, spec):
 
     def search():
         return gs.run_shard(res, spec.order, rank, ws, spec.outputs)
+
+    if args.profile_layer:
+        # profiling case: two searches of one Distribution layer (the second one timed), no bench line
+        step, off = (int(x) for x in args.profile_layer.split(","))
+        layer = Distribution(ds.snps, spec.order - 1, step, off)
+        gs.run(res, spec.order, layer, spec.outputs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = gs.run(res, spec.order, layer, spec.outputs)
+        print(json.dumps({"profile_layer": [step, off], "workload": args.workload, "ms": 1e3 * (time.perf_counter() - t0),
+                          "top1": list(out[0].combination) if out else None}))
+        return
     stream = torch.cuda.ExternalStream(lib.fiu_stream(ctx.h), device=torch.device("cuda", local))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 512 MB > L2 (129 MB)
 
@@ -584,6 +596,8 @@ def main():
     ap.add_argument("--kernel", type=int, default=0, help="force a counting kernel (0 = automatic choice)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched / served measurements")
     ap.add_argument("--no-ingest", action="store_true", help="skip the file ingest timing")
+    ap.add_argument("--profile-layer", default="", metavar="STEP,OFFSET",
+                    help="profiling case: search Distribution(snps, order-1, STEP, OFFSET) twice and exit")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="served stream: Poisson arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="served stream: arrival window (60 s, the served configuration's loop)")

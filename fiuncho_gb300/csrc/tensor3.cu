@@ -811,8 +811,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
             }
             commit_pair(smem_u32(&done));
         }
-        // neither CTA releases shared or tensor memory before the pair's MMAs are done
-        if (lane == 0 && !t3_drain_cl(smem_u32(&done), 0)) ok = false;
+        // neither CTA releases shared or tensor memory before the pair's MMAs are
+        // done (CTA 1 waits once its own work is over, below: waiting here would
+        // span its whole launch, longer than the bound on a single wait)
+        if (lane == 0 && rank == 0 && !t3_drain_cl(smem_u32(&done), 0)) ok = false;
     } else if (warp < 2 + kPBuildWarps) {
         // ---------------------------------------------------------------- A builders (both CTAs)
         const int t = tid - 64;
@@ -956,6 +958,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
     if (!ok) *abort = 1;
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+    // CTA 1: its epilogue has read the last accumulators, so the pair's final
+    // commit to this CTA's `done` lands soon; it must land before the CTA exits
+    if (rank == 1 && warp == 1 && lane == 0 && !t3_drain_cl(smem_u32(&done), 0)) *abort = 1;
     cluster_sync_all();  // the other CTA is done with this CTA's shared and tensor memory
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (tid == 0 && abort_flag) atomicOr(status, 1);
@@ -1497,8 +1502,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kT2Threads, 1)
             }
             commit_pair(smem_u32(&done));
         }
-        // neither CTA releases shared or tensor memory before the pair's MMAs are done
-        if (lane == 0 && !t3_drain_cl(smem_u32(&done), 0)) ok = false;
+        // neither CTA releases shared or tensor memory before the pair's MMAs are
+        // done (CTA 1 waits once its own work is over, below: waiting here would
+        // span its whole launch, longer than the bound on a single wait)
+        if (lane == 0 && rank == 0 && !t3_drain_cl(smem_u32(&done), 0)) ok = false;
     } else {
         // ---------------------------------------------------------------- epilogue (both CTAs)
         const int e = warp - 2;
@@ -1596,6 +1603,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kT2Threads, 1)
     if (!ok) *abort = 1;
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+    // CTA 1: its epilogue has read the last accumulators, so the pair's final
+    // commit to this CTA's `done` lands soon; it must land before the CTA exits
+    if (rank == 1 && warp == 1 && lane == 0 && !t3_drain_cl(smem_u32(&done), 0)) *abort = 1;
     cluster_sync_all();  // the other CTA is done with this CTA's shared and tensor memory
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (tid == 0 && abort_flag) atomicOr(status, 1);

@@ -556,6 +556,23 @@ def test_bounded_wait_gives_up(gs):
     assert len(gs.run(ds, 3, Distribution(30, 2), 5)) == 5
 
 
+def test_pair_kernel_launch_longer_than_a_wait_bound(gs, oracle):
+    """An order-3 scan whose chunks run for seconds on the CTA-pair kernel
+    (10 000 SNPs x 2 000/2 000 samples, 1.7e11 combinations, ~5 s): no wait of
+    either CTA of a pair may span the launch, since every wait gives up after 2 s
+    (FIU_ERR_TIMEOUT).  The returned values are checked against the oracle."""
+    from fiuncho_gb300 import Distribution
+    from helpers import assert_sorted_desc, exact_mi
+    ds = _one_hot_dataset(17, 10000, 2000, 2000)
+    results, v64 = gs.run(ds, 3, Distribution(ds.snps, 2), 20, with_fp64=True)
+    assert gs.last_tile()[0] == 4  # the tensor kernel served it
+    got = np.array([r.combination for r in results], np.int32)
+    assert len(got) == 20
+    assert_sorted_desc(v64)
+    want = exact_mi(oracle, ds.data, ds.cases_words, ds.ctrls_words, ds.cases, ds.ctrls, 3, got)
+    assert np.allclose(v64, want, rtol=1e-5, atol=1e-12)
+
+
 def _one_hot_dataset(seed, snps, n_case, n_ctrl):
     from fiuncho_gb300 import Dataset
     rng = np.random.default_rng(seed)
