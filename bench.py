@@ -176,7 +176,7 @@ def run_reference(args, spec):
     value = done_all * spec.samples / total
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "scaling": "strong", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": args.workload, "snps": spec.snps, "cases": spec.cases, "ctrls": spec.ctrls,
                        "order": spec.order, "outputs": spec.outputs,
@@ -345,7 +345,7 @@ def run_gpu(args, spec):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * my_time / args.steps, "step_ms": [round(x, 3) for x in step_ms],
-        "higher_is_better": True, "scaling": "weak",
+        "higher_is_better": True, "scaling": "strong",  # the one scan's work units split over the ranks
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": args.workload, "snps": spec.snps, "cases": spec.cases, "ctrls": spec.ctrls,
                    "order": spec.order, "outputs": spec.outputs, "combinations": total_combos,
