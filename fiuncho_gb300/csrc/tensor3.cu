@@ -53,6 +53,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 
 #include "tensor_common.cuh"
@@ -1019,6 +1020,31 @@ __device__ __forceinline__ int t2_chunk(int ii, int k, int x) {
     return (((ii * 8 + k) * 2 + x) ^ ((ii & 3) << 1) ^ ((k >> 2) & 1));
 }
 
+// Distribution layers of order-2 scans: the owned prefixes are the SNPs
+// i = offset + step m, consecutive rows m of the operand planes ordered by
+// residue mod step (from row residue_row(offset)).  A layer tile is IT
+// consecutive owned i (positions p0 = IT a ..); tiles are grouped in bands of
+// BT (512 owned i), and a band lists its items j-tile by j-tile, tile fastest,
+// from the j-tile holding the band's first i + 1 (as the whole scan's bands:
+// the CTAs at work share a band's A tiles and each B tile in L2).
+// item_begin[r] = first item of band r.
+template <int IT, int BT>
+__device__ __forceinline__ void t2l_decode(const long long* __restrict__ item_begin, int n_tiles, const ScanWork& w,
+                                           long long g, int& p0, int& j0) {
+    const int n_bands = (n_tiles + BT - 1) / BT;
+    int lo = 0, hi = n_bands - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (item_begin[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    const int ca = min(BT, n_tiles - BT * lo);  // tiles in the band
+    const long long idx = g - item_begin[lo];
+    const int i_first = w.dist_offset + w.dist_step * (IT * BT * lo);
+    p0 = IT * (BT * lo + (int)(idx % ca));
+    j0 = kT2L * ((i_first + 1) / kT2L + (int)(idx / ca));
+}
+
 // Evaluates pair (i, j) from its transpose chunks: exact 9-cell tables from the
 // cores and the single cores, the bounded single-precision prefilter, the exact
 // fixed-point key for survivors, warp-aggregated append (every lane calls it).
@@ -1076,7 +1102,8 @@ __device__ __forceinline__ void t2_eval(const ScanWork& w, const CandSink& sink,
         }
         pass = key >= sink.thr;
         if (dump) {
-            uint32_t* o = dump + ((size_t)i * n + j) * 18;
+            // owned prefix ordinal m of i: rank offset + m * step
+            uint32_t* o = dump + ((size_t)((i - w.dist_offset) / w.dist_step) * n + j) * 18;
 #pragma unroll
             for (int c = 0; c < 9; ++c) {
                 o[c] = f2u(t[0][c]);
@@ -1117,6 +1144,9 @@ struct T2Maps {
     CUtensorMap a, b;
 };
 
+// LAYER: a Distribution layer (t2l_decode; maps.a covers the residue-ordered
+// planes, item_begin / n_itiles are the layer's tiles).
+template <bool LAYER>
 __global__ void __launch_bounds__(kT2Threads, 1)
     tensor2_kernel(const __grid_constant__ T2Maps maps, ScanWork w, const long long* __restrict__ item_begin,
                    int n_itiles, long long g0, long long g1, int k_cases, int pack, CandSink sink, float thr_f,
@@ -1165,8 +1195,14 @@ __global__ void __launch_bounds__(kT2Threads, 1)
         if (lane == 0) {
             long long step = 0;
             for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
-                int i0, j0;
-                t2_decode(item_begin, n_itiles, g, i0, j0);
+                int i0, j0;  // LAYER: i0 = the tile's first row in the residue-ordered planes
+                if (LAYER) {
+                    int p0;
+                    t2l_decode<kT2I, 8>(item_begin, n_itiles, w, g, p0, j0);
+                    i0 = residue_row(w.dist_offset, w.dist_step, n) + p0;
+                } else {
+                    t2_decode(item_begin, n_itiles, g, i0, j0);
+                }
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const int s = (int)(step % kT2Stages);
                     const long long u = step / kT2Stages;
@@ -1244,10 +1280,17 @@ __global__ void __launch_bounds__(kT2Threads, 1)
         const int ii = lane >> 1, x = lane & 1, kh = lane & 1;  // row (ii, x); pairs k = 4 kh + kk
         long long item = 0;
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
-            int i0, j0;
-            t2_decode(item_begin, n_itiles, g, i0, j0);
+            int i0, j0, istep = 1;
+            if (LAYER) {
+                int p0;
+                t2l_decode<kT2I, 8>(item_begin, n_itiles, w, g, p0, j0);
+                i0 = w.dist_offset + w.dist_step * p0;
+                istep = w.dist_step;
+            } else {
+                t2_decode(item_begin, n_itiles, g, i0, j0);
+            }
             const int buf = (int)(item % nbuf);
-            const int i = i0 + 16 * q + ii;
+            const int i = i0 + istep * (16 * q + ii);
             const bool i_ok = i < n;
             float si[2][2];
             {
@@ -1381,6 +1424,8 @@ __device__ __forceinline__ void t2x_decode(const long long* __restrict__ item_be
     j0 = kT2L * b;
 }
 
+// LAYER: a Distribution layer (t2l_decode over tile pairs, as tensor2_kernel).
+template <bool LAYER>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kT2Threads, 1)
     tensor2x_kernel(const __grid_constant__ T2Maps maps, ScanWork w, const long long* __restrict__ item_begin,
                     int n_itiles, long long g0, long long g1, int k_cases, int pack, CandSink sink, float thr_f,
@@ -1433,8 +1478,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kT2Threads, 1)
         if (lane == 0) {
             long long step = 0;
             for (long long g = g0 + cid; g < g1 && ok; g += ncl) {
-                int i0, j0;
-                t2x_decode(item_begin, n_itiles, g, i0, j0);
+                int i0, j0;  // LAYER: i0 = the pair's first row in the residue-ordered planes
+                if (LAYER) {
+                    int p0;
+                    t2l_decode<2 * kT2I, 4>(item_begin, n_itiles, w, g, p0, j0);
+                    i0 = residue_row(w.dist_offset, w.dist_step, n) + p0;
+                } else {
+                    t2x_decode(item_begin, n_itiles, g, i0, j0);
+                }
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const int s = (int)(step % kT2xStages);
                     const long long u = step / kT2xStages;
@@ -1450,7 +1501,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kT2Threads, 1)
                                      "r"((uint32_t)(2 * kT2xStage))
                                      : "memory");
                     t3_tma_pair(smem_u32(st), &maps.a, k0, 2 * (i0 + kT2I * (int)rank), bar);
-                    t3_tma_pair(smem_u32(st + kT2xSA), &maps.a, k0, 2 * j0 + kT2M * (int)rank, bar);
+                    t3_tma_pair(smem_u32(st + kT2xSA), &maps.b, k0, 2 * j0 + kT2M * (int)rank, bar);
                     ++step;
                 }
             }
@@ -1519,11 +1570,18 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kT2Threads, 1)
                                         cluster_addr(smem_u32(&acc_empty[1]), 0)};
         long long item = 0;
         for (long long g = g0 + cid; g < g1 && ok; g += ncl, ++item) {
-            int i0, j0;
-            t2x_decode(item_begin, n_itiles, g, i0, j0);
-            i0 += kT2I * (int)rank;
+            int i0, j0, istep = 1;
+            if (LAYER) {
+                int p0;
+                t2l_decode<2 * kT2I, 4>(item_begin, n_itiles, w, g, p0, j0);
+                i0 = w.dist_offset + w.dist_step * (p0 + kT2I * (int)rank);
+                istep = w.dist_step;
+            } else {
+                t2x_decode(item_begin, n_itiles, g, i0, j0);
+                i0 += kT2I * (int)rank;
+            }
             const int buf = (int)(item % nbuf);
-            const int i = i0 + 16 * q + ii;
+            const int i = i0 + istep * (16 * q + ii);
             const bool i_ok = i < n;
             float si[2][2];
             {
@@ -1791,30 +1849,32 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
 // they are consecutive rows, and one tiled TMA copy per stage loads an item's
 // j rows as in the scan of all prefixes.
 struct T3Layer {
-    long long* item_begin = nullptr;  // [n + 1] first item of each i
-    long long* jl_begin = nullptr;    // [n + 1] first listed j of each i
-    int* jlist = nullptr;             // owned j of each i, ascending
+    long long* item_begin = nullptr;  // order 3: [n + 1] first item of each i; order 2: [tiles + 1] of each tile
+    long long* jl_begin = nullptr;    // order 3: [n + 1] first listed j of each i
+    int* jlist = nullptr;             // order 3: owned j of each i, ascending
     long long total = 0;
     double item_combos = 0;
-    CUtensorMap map_jr;               // box 128 B x 64 rows over the residue-ordered planes
+    int n_tiles = 0;                  // order 2: tiles of owned i
+    CUtensorMap map_jr;               // order 3: box 128 B x 64 rows over the residue-ordered planes
+    CUtensorMap map_ar;               // order 2: box 128 B x 128 rows over the residue-ordered planes
 };
 struct T3Layers {
     std::mutex mu;
-    std::map<std::pair<int, int>, T3Layer> by;
-    std::map<int, uint8_t*> by_residue;  // residue-ordered operand planes per step
+    std::map<std::tuple<int, int, int>, T3Layer> by;  // (order, step, offset)
+    std::map<int, uint8_t*> by_residue;              // residue-ordered operand planes per step
 };
 
 
 static bool is_layer(const ScanWork& w) { return w.dist_step != 1 || w.dist_offset != 0; }
 
 bool tensor_layer_ok(const T3Plan& plan, const ScanWork& w) {
-    return w.order == 3 && plan.pair3 && w.dist_n == w.d.snps;
+    return (w.order == 2 || (w.order == 3 && plan.pair3)) && w.dist_n == w.d.snps;
 }
 
 static const T3Layer* find_layer(const T3Plan& plan, const ScanWork& w) {
     if (!plan.layers) return nullptr;
     std::lock_guard<std::mutex> g(plan.layers->mu);
-    auto it = plan.layers->by.find({w.dist_step, w.dist_offset});
+    auto it = plan.layers->by.find(std::make_tuple(w.order, w.dist_step, w.dist_offset));
     return it == plan.layers->by.end() ? nullptr : &it->second;
 }
 
@@ -1822,7 +1882,8 @@ cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s) {
     if (!tensor_layer_ok(plan, w)) return cudaErrorInvalidValue;
     if (!plan.layers) plan.layers = new T3Layers;
     std::lock_guard<std::mutex> g(plan.layers->mu);
-    if (plan.layers->by.count({w.dist_step, w.dist_offset})) return cudaSuccess;
+    const auto key = std::make_tuple(w.order, w.dist_step, w.dist_offset);
+    if (plan.layers->by.count(key)) return cudaSuccess;
     uint8_t*& perm = plan.layers->by_residue[w.dist_step];
     if (!perm) {
         // residue class r holds SNPs r + step m, m < ceil((n - r) / step), each as its 2 plane rows
@@ -1840,10 +1901,43 @@ cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s) {
             return e;
         }
     }
-    // owned prefixes (i, j): lexicographic ranks offset + m * step; the pairs
-    // (i, j > i) have ranks base(i) + (j - i - 1), base(i) = i (n-1) - i (i-1) / 2
     const int n = w.d.snps;
     const long long step = w.dist_step, offset = w.dist_offset;
+    if (w.order == 2) {
+        // owned prefixes: SNPs i = offset + m step; tiles of IT consecutive owned i (a CTA pair's two
+        // i-tiles when the classes pack) in bands of BT (t2l_decode)
+        const int IT = plan.pack ? 2 * kT2I : kT2I, BT = plan.pack ? 4 : 8;
+        const long long count = offset < n ? (n - offset + step - 1) / step : 0;
+        const int tiles = (int)((count + IT - 1) / IT);
+        const int bands = (tiles + BT - 1) / BT;
+        const int nb = (n + kT2L - 1) / kT2L;
+        std::vector<long long> tb((size_t)bands + 1);
+        long long total = 0, combos = 0;
+        for (int r = 0; r < bands; ++r) {
+            tb[r] = total;
+            const long long i_first = offset + step * (long long)IT * BT * r;
+            const int ca = std::min(BT, tiles - BT * r);
+            total += (long long)ca * std::max(0ll, (long long)nb - (i_first + 1) / kT2L);
+        }
+        tb[bands] = total;
+        for (long long i = offset; i < n; i += step) combos += n - 1 - i;
+        T3Layer L;
+        L.total = total;
+        L.n_tiles = tiles;
+        L.item_combos = (double)combos / std::max(1ll, total);
+        cudaError_t e = t3_map(&L.map_ar, perm, 2 * n, plan.pitch, kT2M, true);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&L.item_begin, tb.size() * sizeof(long long));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(L.item_begin, tb.data(), tb.size() * sizeof(long long), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(L.item_begin);
+            return e;
+        }
+        plan.layers->by[key] = L;
+        return cudaSuccess;
+    }
+    // order 3: owned prefixes (i, j): lexicographic ranks offset + m * step; the pairs
+    // (i, j > i) have ranks base(i) + (j - i - 1), base(i) = i (n-1) - i (i-1) / 2
     std::vector<long long> ib((size_t)n + 1), jb((size_t)n + 1);
     std::vector<int> jl;
     long long total = 0, combos = 0;
@@ -1878,19 +1972,19 @@ cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s) {
         cudaFree(L.jlist);
         return e;
     }
-    plan.layers->by[{w.dist_step, w.dist_offset}] = L;
+    plan.layers->by[key] = L;
     return cudaSuccess;
 }
 
 long long tensor_units(const T3Plan& plan, const ScanWork& w) {
-    if (w.order == 3 && is_layer(w)) {
+    if ((w.order == 2 || w.order == 3) && is_layer(w)) {
         const T3Layer* L = find_layer(plan, w);
         return L ? L->total : 0;
     }
     return w.order == 2 ? plan.total2 : w.order == 4 ? plan.total4 : plan.total;
 }
 double tensor_item_combos(const T3Plan& plan, const ScanWork& w) {
-    if (w.order == 3 && is_layer(w)) {
+    if ((w.order == 2 || w.order == 3) && is_layer(w)) {
         const T3Layer* L = find_layer(plan, w);
         return L ? L->item_combos : 1.0;
     }
@@ -2043,9 +2137,14 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     static const cudaError_t attr = [] {
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(tensor2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2Smem);
+            e = cudaFuncSetAttribute(tensor2_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2Smem);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(tensor2x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2xSmem);
+            e = cudaFuncSetAttribute(tensor2_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2Smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tensor2x_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kT2xSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tensor2x_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2xSmem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(tensor3x_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPxSmem);
         if (e == cudaSuccess)
@@ -2059,20 +2158,32 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     const double thr = ((double)sink.thr - (double)w.base_key) * scale - t3_margin(w.d.n_cases + w.d.n_ctrls);
     const float thr_f = (float)std::max(-3.0e38, std::min(3.0e38, thr));
     const unsigned grid = (unsigned)(items < sms ? items : sms);
-    if (w.order == 2 && plan.pair2) {
-        static const int max_clusters = pair_clusters(tensor2x_kernel, kT2Threads, kT2xSmem);
-        const long long clusters = std::min<long long>(items, max_clusters > 0 ? max_clusters : sms / 2);
-        T2Maps maps2{plan.map_a2, plan.map_b2};
-        tensor2x_kernel<<<(unsigned)(2 * std::max(1ll, clusters)), kT2Threads, kT2xSmem, s>>>(
-            maps2, w, plan.item2_begin, plan.n_itiles, g0, g1, plan.k_cases, plan.pack, sink, thr_f, dump, single,
-            status);
-        count_launch();
-        return cudaGetLastError();
-    }
     if (w.order == 2) {
-        T2Maps maps2{plan.map_a2, plan.map_b2};
-        tensor2_kernel<<<grid, kT2Threads, kT2Smem, s>>>(maps2, w, plan.item2_begin, plan.n_itiles, g0, g1,
-                                                         plan.k_cases, plan.pack, sink, thr_f, dump, single, status);
+        // a Distribution layer: A rows from the residue-ordered planes, the layer's tiles
+        const T3Layer* L = is_layer(w) ? find_layer(plan, w) : nullptr;
+        if (is_layer(w) && (!L || !tensor_layer_ok(plan, w))) return cudaErrorInvalidValue;
+        const long long* ib = L ? L->item_begin : plan.item2_begin;
+        const int nt = L ? L->n_tiles : plan.n_itiles;
+        if (plan.pair2) {
+            static const int max_clusters = pair_clusters(tensor2x_kernel<false>, kT2Threads, kT2xSmem);
+            const long long clusters = std::min<long long>(items, max_clusters > 0 ? max_clusters : sms / 2);
+            const unsigned grid2 = (unsigned)(2 * std::max(1ll, clusters));
+            const T2Maps maps2{L ? L->map_ar : plan.map_a2, plan.map_a2};  // both boxes 128 rows
+            if (L)
+                tensor2x_kernel<true><<<grid2, kT2Threads, kT2xSmem, s>>>(maps2, w, ib, nt, g0, g1, plan.k_cases,
+                                                                         plan.pack, sink, thr_f, dump, single, status);
+            else
+                tensor2x_kernel<false><<<grid2, kT2Threads, kT2xSmem, s>>>(maps2, w, ib, nt, g0, g1, plan.k_cases,
+                                                                          plan.pack, sink, thr_f, dump, single, status);
+        } else {
+            const T2Maps maps2{L ? L->map_ar : plan.map_a2, plan.map_b2};
+            if (L)
+                tensor2_kernel<true><<<grid, kT2Threads, kT2Smem, s>>>(maps2, w, ib, nt, g0, g1, plan.k_cases,
+                                                                       plan.pack, sink, thr_f, dump, single, status);
+            else
+                tensor2_kernel<false><<<grid, kT2Threads, kT2Smem, s>>>(maps2, w, ib, nt, g0, g1, plan.k_cases,
+                                                                        plan.pack, sink, thr_f, dump, single, status);
+        }
         count_launch();
         return cudaGetLastError();
     }

@@ -18,9 +18,9 @@
  * CPU fallback: without a usable GPU the constructor throws.
  *
  * Multi-GPU: MPIEngine gives rank r of N the strided prefix share
- * Distribution(snps, order-1, N, r) (MPIEngine.h:133-134).  For order 3 with
- * classes that share one accumulator the tensor-core kernel serves such a
- * share itself (its list mode), with the reference's per-rank list; other
+ * Distribution(snps, order-1, N, r) (MPIEngine.h:133-134).  The tensor-core
+ * kernels serve such a share themselves for order 2 and, when the classes
+ * share one accumulator, order 3, with the reference's per-rank list; other
  * shares run on the CUDA-core kernels.  With shard_ranks = true a rank share
  * runs as shard r of N of the whole search instead (fiu_search_shard: equal
  * ranges of the tensor-core work units, every order); the rank's own list

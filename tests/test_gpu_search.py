@@ -414,10 +414,11 @@ def test_order4_reduced_work_is_automatic(gs, golden_synth):
 
 
 def test_tensor_kernel_scope(gs, golden_synth):
-    """The tcgen05 kernels serve one-hot order-2/3/4 searches of the whole data set, and
-    order-3 Distribution layers of all SNPs when the classes pack (the pair kernel's
-    list mode); other layers fall back to the reduced-work kernel automatically and
-    are refused when the tensor kernel is forced."""
+    """The tcgen05 kernels serve one-hot order-2/3/4 searches of the whole data set,
+    order-2 Distribution layers of all SNPs, and order-3 layers of all SNPs when the
+    classes pack (the pair kernel's list mode); layers of fewer SNPs fall back to the
+    reduced-work kernel automatically and are refused when the tensor kernel is
+    forced."""
     from fiuncho_gb300 import Dataset, Distribution, FiunchoError, GpuSearch, Resident
     ds = Dataset.from_genotypes(golden_synth["geno"], golden_synth["is_case"])
     g = GpuSearch(0)
@@ -429,26 +430,32 @@ def test_tensor_kernel_scope(gs, golden_synth):
     g.run(res, 3, Distribution(ds.snps - 5, 2, 2, 1), 10)  # a layer of the first n - 5 SNPs
     assert g.last_tile()[0] in (2, 3)
     g.run(res, 2, Distribution(ds.snps, 1, 2, 0), 10)
+    assert g.last_tile()[0] == 4
+    g.run(res, 2, Distribution(ds.snps - 5, 1, 2, 0), 10)
     assert g.last_tile()[0] in (2, 3)
     g.run(res, 2, Distribution(ds.snps, 1), 10)
     assert g.last_tile()[0] == 4
     g.set_kernel(4)
     g.run(res, 3, Distribution(ds.snps, 2, 2, 1), 10)
+    g.run(res, 2, Distribution(ds.snps, 1, 2, 1), 10)
     with pytest.raises(FiunchoError):
-        g.run(res, 2, Distribution(ds.snps, 1, 2, 1), 10)
+        g.run(res, 2, Distribution(ds.snps - 5, 1, 2, 1), 10)
     with pytest.raises(FiunchoError):
         g.run(res, 5, Distribution(ds.snps, 4), 10)
 
 
-@pytest.mark.parametrize("n_ranks", [2, 3, 4, 5, 6, 7])
-def test_rank_layers_on_the_tensor_kernel(oracle, n_ranks):
-    """MPIEngine gives rank r of N the strided share Distribution(snps, 2, N, r)
-    (MPIEngine.h:133-134, Distribution.h:172-176): on the tensor kernel (list mode),
-    forced and automatic, every rank's list equals the oracle's list of that rank,
-    and the ranks' lists merged as MPIEngine merges them give the whole search."""
+@pytest.mark.parametrize("order,n_ranks,nc,nt", [(3, r, 1300, 1217) for r in (2, 3, 4, 5, 6, 7)] +
+                         [(2, r, 1300, 1217) for r in (2, 3, 5, 7)] + [(2, r, 9000, 9800) for r in (2, 3, 7)])
+def test_rank_layers_on_the_tensor_kernel(oracle, order, n_ranks, nc, nt):
+    """MPIEngine gives rank r of N the strided share Distribution(snps, order-1, N, r)
+    (MPIEngine.h:133-134, Distribution.h:172-176): on the tensor kernels (order 3: the
+    pair kernel's list mode; order 2: the owned SNPs of one residue mod N, with classes
+    that pack -- CTA pairs -- and classes that do not), forced and automatic, every
+    rank's list equals the oracle's list of that rank, and the ranks' lists merged as
+    MPIEngine merges them give the whole search."""
     from fiuncho_gb300 import Dataset, Distribution, GpuSearch, MPIEngine, Resident
-    rng = np.random.default_rng(100 + n_ranks)
-    snps, nc, nt = 170, 1300, 1217
+    rng = np.random.default_rng(100 + n_ranks + 10 * order)
+    snps = 170 if order == 3 else 700
     maf = rng.uniform(0.05, 0.5, snps)[:, None]
     u = rng.random((snps, nc + nt))
     geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
@@ -458,13 +465,29 @@ def test_rank_layers_on_the_tensor_kernel(oracle, n_ranks):
         g = GpuSearch(0, kernel=kernel)
         res = Resident(g.ctx, ds)
         for r in range(n_ranks):
-            out, v64 = g.run(res, 3, Distribution(snps, 2, n_ranks, r), 30, with_fp64=True)
+            out, v64 = g.run(res, order, Distribution(snps, order - 1, n_ranks, r), 30, with_fp64=True)
             assert g.last_tile()[0] == 4
-            _check_topn(oracle, ds, 3, 30, out, v64, dist=(snps, n_ranks, r))
+            _check_topn(oracle, ds, order, 30, out, v64, dist=(snps, n_ranks, r))
             if kernel == 0:
                 parts += out
-    whole = GpuSearch(0).run(ds, 3, Distribution(snps, 2), 30)
+    whole = GpuSearch(0).run(ds, order, Distribution(snps, order - 1), 30)
     assert [x.combination for x in MPIEngine().gather(parts, 30)] == [x.combination for x in whole]
+
+
+@pytest.mark.parametrize("nc,nt", [(999, 1001), (9000, 9800)])
+@pytest.mark.parametrize("step,offset", [(2, 1), (3, 0), (3, 2), (64, 5), (200, 0)])
+def test_order2_layer_tables(gs, oracle, nc, nt, step, offset):
+    """Every table of an order-2 Distribution layer on the tensor kernel (classes that
+    pack: CTA pairs; classes that do not: one CTA per tile) equals the oracle's: the
+    digest of all of them and their count (130 SNPs: tiles of 64 owned SNPs end inside
+    the residue class and past it)."""
+    from fiuncho_gb300 import Distribution
+    ds = _one_hot_dataset(7 + step, 130, nc, nt)
+    from fiuncho_gb300.search import Resident
+    res = Resident(gs.ctx, ds)
+    want = oracle.table_digest(ds.data, ds.snps, ds.cases_words, ds.ctrls_words, 2, dist=(ds.snps, step, offset))
+    got = gs.scan_digest(res, 2, Distribution(ds.snps, 1, step, offset), 4)
+    assert got == want
 
 
 def test_elided_rejects_non_one_hot(gs):
