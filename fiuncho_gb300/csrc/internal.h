@@ -214,13 +214,18 @@ void tensor3_release(T3Plan& plan);
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
                            uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
                            int* status, cudaStream_t s, int sms);
-// tensor4.cu -- order 4 on tcgen05 (one-hot data, whole data set, one worker).
+// tensor4.cu -- order 4 on tcgen05 (one-hot data, the whole data set or a Distribution layer of it).
 std::vector<long long> t4_item_table(int n, bool pack, std::vector<long long>& per);
+long long t4_layer_items(int n, int step, long long offset, bool pack, std::vector<long long>& pbegin,
+                         std::vector<int4>& pinfo, long long& combos);
+// pinfo / n_pairs: a layer's pair tables (begin = their first items, per unused; map_k over the
+// residue-ordered planes), else nullptr
 cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l256, const CUtensorMap& map_l128,
                            const CUtensorMap& map_k, const CUtensorMap& map_i, const long long* begin,
                            const long long* per, int k_cases, int pack, long long g0, long long g1,
                            const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
-                           const uint4* triples, int* status, cudaStream_t s, int sms);
+                           const uint4* triples, int* status, cudaStream_t s, int sms, const int4* pinfo = nullptr,
+                           int n_pairs = 0);
 // Largest absolute error of the kernel's single-precision log2 over all its inputs (counts <= max_c).
 cudaError_t probe_lg2_error(unsigned max_c, double* max_abs_err, cudaStream_t s);
 cudaError_t probe_wait_limit(unsigned limit_us, int arrive, int* completed, double* elapsed_ms, cudaStream_t s);

@@ -634,14 +634,6 @@ __device__ __forceinline__ void t3x_decode(const long long* __restrict__ item_be
     }
 }
 
-// Row (SNP position) of SNP j in the operand planes ordered by residue mod
-// step (SNPs r, r + step, .. for r = 0, 1, ..; residue r holds
-// n / step + (r < n % step) SNPs).
-__host__ __device__ __forceinline__ int residue_row(int j, int step, int n) {
-    const int r = j % step;
-    return r * (n / step) + min(r, n % step) + j / step;
-}
-
 // List mode (a Distribution layer): the owned j of each i are listed in
 // jlist[jl_begin[i] .. jl_begin[i+1]); an item takes 64 consecutive entries
 // from p0 (= jl_begin[i] + 64 a) and an l-tile l0 = jlist[p0] + 1 + 128 b.
@@ -1854,9 +1846,11 @@ struct T3Layer {
     int* jlist = nullptr;             // order 3: owned j of each i, ascending
     long long total = 0;
     double item_combos = 0;
-    int n_tiles = 0;                  // order 2: tiles of owned i
+    int n_tiles = 0;                  // order 2: tiles of owned i; order 4: listed pairs
+    int4* pinfo = nullptr;            // order 4: (i, j, first owned k) of each listed pair
     CUtensorMap map_jr;               // order 3: box 128 B x 64 rows over the residue-ordered planes
     CUtensorMap map_ar;               // order 2: box 128 B x 128 rows over the residue-ordered planes
+    CUtensorMap map_kr;               // order 4: box 128 B x 32 rows over the residue-ordered planes
 };
 struct T3Layers {
     std::mutex mu;
@@ -1868,7 +1862,8 @@ struct T3Layers {
 static bool is_layer(const ScanWork& w) { return w.dist_step != 1 || w.dist_offset != 0; }
 
 bool tensor_layer_ok(const T3Plan& plan, const ScanWork& w) {
-    return (w.order == 2 || (w.order == 3 && plan.pair3)) && w.dist_n == w.d.snps;
+    return (w.order == 2 || (w.order == 3 && plan.pair3) || (w.order == 4 && w.d.snps >= 4)) &&
+           w.dist_n == w.d.snps;
 }
 
 static const T3Layer* find_layer(const T3Plan& plan, const ScanWork& w) {
@@ -1903,6 +1898,30 @@ cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s) {
     }
     const int n = w.d.snps;
     const long long step = w.dist_step, offset = w.dist_offset;
+    if (w.order == 4) {
+        std::vector<long long> pb;
+        std::vector<int4> pi;
+        long long combos = 0;
+        const long long total = t4_layer_items(n, (int)step, offset, plan.pack != 0, pb, pi, combos);
+        T3Layer L;
+        L.total = total;
+        L.n_tiles = (int)pi.size();
+        L.item_combos = (double)combos / std::max(1ll, total);
+        cudaError_t e = t3_map(&L.map_kr, perm, 2 * n, plan.pitch, 32, true);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&L.item_begin, pb.size() * sizeof(long long));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&L.pinfo, std::max<size_t>(1, pi.size()) * sizeof(int4));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(L.item_begin, pb.data(), pb.size() * sizeof(long long), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && !pi.empty())
+            e = cudaMemcpy(L.pinfo, pi.data(), pi.size() * sizeof(int4), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(L.item_begin);
+            cudaFree(L.pinfo);
+            return e;
+        }
+        plan.layers->by[key] = L;
+        return cudaSuccess;
+    }
     if (w.order == 2) {
         // owned prefixes: SNPs i = offset + m step; tiles of IT consecutive owned i (a CTA pair's two
         // i-tiles when the classes pack) in bands of BT (t2l_decode)
@@ -1977,14 +1996,14 @@ cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s) {
 }
 
 long long tensor_units(const T3Plan& plan, const ScanWork& w) {
-    if ((w.order == 2 || w.order == 3) && is_layer(w)) {
+    if (is_layer(w)) {
         const T3Layer* L = find_layer(plan, w);
         return L ? L->total : 0;
     }
     return w.order == 2 ? plan.total2 : w.order == 4 ? plan.total4 : plan.total;
 }
 double tensor_item_combos(const T3Plan& plan, const ScanWork& w) {
-    if ((w.order == 2 || w.order == 3) && is_layer(w)) {
+    if (is_layer(w)) {
         const T3Layer* L = find_layer(plan, w);
         return L ? L->item_combos : 1.0;
     }
@@ -1997,6 +2016,7 @@ void tensor3_release(T3Plan& plan) {
             cudaFree(kv.second.item_begin);
             cudaFree(kv.second.jl_begin);
             cudaFree(kv.second.jlist);
+            cudaFree(kv.second.pinfo);
         }
         for (auto& kv : plan.layers->by_residue) cudaFree(kv.second);
         delete plan.layers;
@@ -2130,9 +2150,17 @@ static int pair_clusters(K* kernel, int threads, size_t smem) {
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
                            uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,
                            int* status, cudaStream_t s, int sms) {
-    if (w.order == 4)
+    if (w.order == 4) {
+        if (is_layer(w)) {
+            const T3Layer* L = find_layer(plan, w);
+            if (!L || !tensor_layer_ok(plan, w)) return cudaErrorInvalidValue;
+            return launch_tensor4(w, plan.map_l, plan.map_a2, L->map_kr, plan.map_i, L->item_begin, nullptr,
+                                  plan.k_cases, plan.pack, g0, g1, sink, dump, single, pairs, triples, status, s, sms,
+                                  L->pinfo, L->n_tiles);
+        }
         return launch_tensor4(w, plan.map_l, plan.map_a2, plan.map_k4, plan.map_i, plan.item4_begin, plan.item4_per,
                               plan.k_cases, plan.pack, g0, g1, sink, dump, single, pairs, triples, status, s, sms);
+    }
     // set once, by whichever host thread comes first (thread-safe static initialisation)
     static const cudaError_t attr = [] {
         cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);

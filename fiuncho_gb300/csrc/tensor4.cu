@@ -119,6 +119,46 @@ __device__ __forceinline__ void t4_decode(const long long* __restrict__ begin, c
     }
 }
 
+// Distribution layers of order-4 scans: the owned prefixes (i, j, k) of a pair
+// (i, j) are k = kf + step m (their ranks triple_index(i, j, j + 1) + k - j - 1
+// step through the layer's offset class), consecutive rows of the operand
+// planes ordered by residue mod step.  A layer item is (i, j, 16 owned k from
+// kf + 16 step a, L l from that first k + 1); pbegin[p] = first item of listed
+// pair p, pinfo[p] = (i, j, kf).
+template <int L>
+__device__ __forceinline__ void t4l_decode(const long long* __restrict__ pbegin, const int4* __restrict__ pinfo,
+                                           int n_pairs, int n, int step, long long g, int& i, int& j, int& k0,
+                                           int& l0) {
+    int lo = 0, hi = n_pairs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(pbegin + mid) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    const int4 f = __ldg(pinfo + lo);
+    i = f.x;
+    j = f.y;
+    long long q = g - __ldg(pbegin + lo);
+    for (int k = f.z;; k += kT4K * step) {
+        const long long nl = (n - 1 - k + L - 1) / L;
+        if (q < nl) {
+            k0 = k;
+            l0 = k + 1 + L * (int)q;
+            return;
+        }
+        q -= nl;
+    }
+}
+
+// Item g of a scan of the whole data set (t4_decode) or of a layer (t4l_decode).
+template <int L, bool LAYER>
+__device__ __forceinline__ void t4_item(const long long* __restrict__ begin, const long long* __restrict__ per,
+                                        const int4* __restrict__ pinfo, int n_pairs, const ScanWork& w, long long g,
+                                        int& i, int& j, int& k0, int& l0) {
+    if (LAYER) t4l_decode<L>(begin, pinfo, n_pairs, w.d.snps, w.dist_step, g, i, j, k0, l0);
+    else t4_decode<L>(begin, per, w.d.snps, g, i, j, k0, l0);
+}
+
 // 16-byte chunk of the epilogue transpose buffer holding (cases w0, w1,
 // controls w0, w1) of row (kk, xyz) for the column group ll; conflict-free for
 // the row-wise writes (fixed ll) and the combination-wise reads (fixed xyz).
@@ -184,12 +224,14 @@ __device__ __forceinline__ void t4_cp16(void* dst, const void* src) {
 
 // Copies item g's k-only and l-only sources into it (epilogue thread et of
 // 256), then commits this thread's copy group.
-template <int L>
+template <int L, bool LAYER>
 __device__ __forceinline__ void t4_stage(T4Item& it, long long g, int et, const long long* __restrict__ begin,
-                                         const long long* __restrict__ per, int n, const uint32_t* __restrict__ single,
+                                         const long long* __restrict__ per, const int4* __restrict__ pinfo,
+                                         int n_pairs, const ScanWork& w, const uint32_t* __restrict__ single,
                                          const uint4* __restrict__ pairs, const uint4* __restrict__ triples) {
+    const int n = w.d.snps, kstep = LAYER ? w.dist_step : 1;
     int i, j, k0, l0;
-    t4_decode<L>(begin, per, n, g, i, j, k0, l0);
+    t4_item<L, LAYER>(begin, per, pinfo, n_pairs, w, g, i, j, k0, l0);
     const uint4* single4 = reinterpret_cast<const uint4*>(single);
     if (et < L) {
         const int l = l0 + et;
@@ -202,7 +244,7 @@ __device__ __forceinline__ void t4_stage(T4Item& it, long long g, int et, const 
             t4_cp16(&it.sl[et], single4 + l);
         }
     } else if (et >= kT4L && et < kT4L + kT4K) {
-        const int kk = et - kT4L, k = k0 + kk;
+        const int kk = et - kT4L, k = k0 + kstep * kk;
         if (k < n) {
             const uint4* t = triples + 2 * triple_index(i, j, k, n);
             t4_cp16(&it.tijk[0][kk], t);
@@ -253,7 +295,7 @@ template <bool DIGEST>
 __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink, long long thr_q, uint32_t* dump,
                                         const uint32_t* __restrict__ single, const uint4* __restrict__ pairs,
                                         const uint4* __restrict__ triples, const T4Item& it,
-                                        const uint32_t (&cp)[2][8], const T4KL& kl, int i, int j, int k0, int l0,
+                                        const uint32_t (&cp)[2][8], const T4KL& kl, int i, int j, int kk, int l0,
                                         int k, int l, bool valid, int lane) {
     const DevData& d = w.d;
     const int n = d.snps;
@@ -263,12 +305,14 @@ __device__ __forceinline__ void t4_eval(const ScanWork& w, const CandSink& sink,
     if (valid) {
         bool cand = DIGEST || dump != nullptr;
         if (!cand) {
-            const int kk = k - k0, ll = l - l0;
+            const int ll = l - l0;
             const long long est = t4_estimate(cp, it, kk, ll, kl, d.n_cases | d.n_ctrls << 16);
             cand = est >= thr_q;
         }
         if (cand) {
-            uint32_t* o = dump ? dump + ((size_t)triple_index(i, j, k, n) * n + l) * 2 * 81 : nullptr;
+            // owned prefix ordinal of (i, j, k): rank offset + m * step
+            const size_t m = (size_t)((triple_index(i, j, k, n) - w.dist_offset) / w.dist_step);
+            uint32_t* o = dump ? dump + (m * n + l) * 2 * 81 : nullptr;
             const unsigned gt = blockIdx.x * blockDim.x + threadIdx.x;
             if (DIGEST && gt < sink.dscratch_threads) o = sink.dscratch + (size_t)gt * 2 * 81;
             key += t4_exact(w, cp, i, j, k, l, single, pairs, triples, o);
@@ -313,12 +357,15 @@ __device__ __forceinline__ void t4_ld16(uint32_t taddr, uint32_t (&v)[16]) {
 
 // DIGEST: the digest mode of fiu_scan_digest (every valid combination's tables hashed), compiled
 // separately so that the search's instantiation carries none of its code.
-template <bool PACK, bool DIGEST>
+// LAYER: a Distribution layer (t4l_decode; maps.k then covers the residue-ordered planes, begin /
+// pinfo / n_pairs are the layer's pair tables).
+template <bool PACK, bool DIGEST, bool LAYER>
 __global__ void __launch_bounds__(kT4Threads, 1)
     tensor4p_kernel(const __grid_constant__ T4Maps maps, ScanWork w, const long long* __restrict__ begin,
                     const long long* __restrict__ per, long long g0, long long g1, int k_cases, int pack,
                     CandSink sink, long long thr_q, uint32_t* dump, const uint32_t* __restrict__ single,
-                    const uint4* __restrict__ pairs, const uint4* __restrict__ triples, int* status) {
+                    const uint4* __restrict__ pairs, const uint4* __restrict__ triples, int* status,
+                    const int4* __restrict__ pinfo, int n_pairs) {
     extern __shared__ uint8_t smraw[];
     __shared__ __align__(8) uint64_t full_t[kT4Stages], full_a[kT4Stages], empty[kT4Stages];
     __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done;
@@ -368,7 +415,8 @@ __global__ void __launch_bounds__(kT4Threads, 1)
             long long step = 0;
             for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
                 int i, j, k0, l0;
-                t4_decode<L>(begin, per, n, g, i, j, k0, l0);
+                t4_item<L, LAYER>(begin, per, pinfo, n_pairs, w, g, i, j, k0, l0);
+                const int krow = LAYER ? residue_row(k0, w.dist_step, n) : k0;  // first row of the k tile
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const int s = (int)(step % kT4Stages);
                     const long long u = step / kT4Stages;
@@ -382,7 +430,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kTx)
                                  : "memory");
                     t3_tma(smem_u32(st), &maps.l, kb, 2 * l0, bar);
-                    t3_tma(smem_u32(st + kT4SB + kT4SA), &maps.k, kb, 2 * k0, bar);
+                    t3_tma(smem_u32(st + kT4SB + kT4SA), &maps.k, kb, 2 * krow, bar);
                     t3_tma(smem_u32(st + kT4SB + kT4SA + kT4SK), &maps.i, kb, 2 * i, bar);
                     t3_tma(smem_u32(st + kT4SB + kT4SA + kT4SK + kT4SI), &maps.i, kb, 2 * j, bar);
                     ++step;
@@ -408,7 +456,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                 // short by the last SNP multiplies only the columns of its valid l, rounded up
                 // to 8 l (the epilogue's column groups), N 64 at least
                 int ii, jj, kk0, l0;
-                t4_decode<L>(begin, per, n, g, ii, jj, kk0, l0);
+                t4_item<L, LAYER>(begin, per, pinfo, n_pairs, w, g, ii, jj, kk0, l0);
                 const int vl = min(L, n - l0);
                 const uint32_t idesc = t4_idesc(min(NR, max(64, (2 * vl + 15) / 16 * 16)));
                 for (int ks = 0; ks < ksteps; ++ks, ++step) {
@@ -511,19 +559,20 @@ __global__ void __launch_bounds__(kT4Threads, 1)
         T4Item* items = reinterpret_cast<T4Item*>(ebuf_all + kT4EpiWarps * (kT4Ebuf / 4));  // two buffers
         long long item = 0;
         if (g0 + blockIdx.x < g1)
-            t4_stage<L>(items[0], g0 + blockIdx.x, et, begin, per, n, single, pairs, triples);
+            t4_stage<L, LAYER>(items[0], g0 + blockIdx.x, et, begin, per, pinfo, n_pairs, w, single, pairs, triples);
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
             int i, j, k0, l0;
-            t4_decode<L>(begin, per, n, g, i, j, k0, l0);
+            t4_item<L, LAYER>(begin, per, pinfo, n_pairs, w, g, i, j, k0, l0);
             const int buf = (int)(item & 1);
-            const int k = k0 + 4 * q + kkc;
+            const int k = k0 + (LAYER ? w.dist_step : 1) * (4 * q + kkc);
             // this thread's copies of the item's sources have landed; the named
             // barrier (the 256 epilogue threads) makes everyone's visible and
             // frees the other buffer (every thread is done with the previous item)
             asm volatile("cp.async.wait_group 0;" ::: "memory");
             asm volatile("bar.sync 1, %0;" ::"n"(32 * kT4EpiWarps) : "memory");
             if (g + gridDim.x < g1)
-                t4_stage<L>(items[buf ^ 1], g + gridDim.x, et, begin, per, n, single, pairs, triples);
+                t4_stage<L, LAYER>(items[buf ^ 1], g + gridDim.x, et, begin, per, pinfo, n_pairs, w, single, pairs,
+                                   triples);
             const T4Item& it = items[buf];
             if (!t3_wait(smem_u32(&acc_full[buf]), (uint32_t)((item >> 1) & 1), abort)) {
                 ok = false;
@@ -584,7 +633,8 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     cp[1][r] = c4.z | (c4.w << 16);
                 }
                 __syncwarp();
-                t4_eval<DIGEST>(w, sink, thr_q, dump, single, pairs, triples, it, cp, kl, i, j, k0, l0, valid ? k : 2,
+                t4_eval<DIGEST>(w, sink, thr_q, dump, single, pairs, triples, it, cp, kl, i, j, 4 * q + kkc, l0,
+                                valid ? k : 2,
                         valid ? l : 3, valid, lane);
             }
         }
@@ -627,18 +677,53 @@ std::vector<long long> t4_item_table(int n, bool pack, std::vector<long long>& p
     return begin;
 }
 
+// Pair tables of a Distribution layer of an order-4 scan (host): the listed pairs (i, j) with at
+// least one item, their first owned k and first item.  Returns the items; combos = combinations.
+long long t4_layer_items(int n, int step, long long offset, bool pack, std::vector<long long>& pbegin,
+                         std::vector<int4>& pinfo, long long& combos) {
+    const int L = pack ? kT4L : kT4L / 2;
+    pbegin.clear();
+    pinfo.clear();
+    combos = 0;
+    long long total = 0;
+    for (int i = 0; i + 3 < n; ++i)
+        for (int j = i + 1; j + 2 < n; ++j) {
+            const long long base = triple_index(i, j, j + 1, n), cnt = n - 1 - j;  // ranks base .. base + cnt - 1
+            long long t = std::max(0ll, offset - base);
+            t += ((offset - base - t) % step + step) % step;  // first t with base + t = offset (mod step)
+            if (t >= cnt) continue;
+            const int kf = j + 1 + (int)t;
+            long long items = 0;
+            for (long long k = kf; k <= n - 2; k += (long long)kT4K * step) items += (n - 1 - k + L - 1) / L;
+            for (long long k = kf; k < n; k += step) combos += n - 1 - k;
+            if (items == 0) continue;
+            pbegin.push_back(total);
+            pinfo.push_back(make_int4(i, j, kf, 0));
+            total += items;
+        }
+    pbegin.push_back(total);
+    return total;
+}
+
 cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l256, const CUtensorMap& map_l128,
                            const CUtensorMap& map_k, const CUtensorMap& map_i, const long long* begin,
                            const long long* per, int k_cases, int pack, long long g0, long long g1,
                            const CandSink& sink, uint32_t* dump, const uint32_t* single, const uint4* pairs,
-                           const uint4* triples, int* status, cudaStream_t s, int sms) {
-    if (!triples || !pairs || !single || !begin || !per) return cudaErrorInvalidValue;
-    static LaunchCache cache[4];
+                           const uint4* triples, int* status, cudaStream_t s, int sms, const int4* pinfo,
+                           int n_pairs) {
+    const bool layer = pinfo != nullptr;
+    if (!triples || !pairs || !single || !begin || (!per && !layer)) return cudaErrorInvalidValue;
+    static LaunchCache cache[8];
     const bool dg = sink.digest != nullptr;
-    auto fn = pack ? (dg ? tensor4p_kernel<true, true> : tensor4p_kernel<true, false>)
-                   : (dg ? tensor4p_kernel<false, true> : tensor4p_kernel<false, false>);
+    using Fn = decltype(&tensor4p_kernel<true, true, true>);
+    static const Fn fns[8] = {tensor4p_kernel<false, false, false>, tensor4p_kernel<false, true, false>,
+                              tensor4p_kernel<true, false, false>,  tensor4p_kernel<true, true, false>,
+                              tensor4p_kernel<false, false, true>,  tensor4p_kernel<false, true, true>,
+                              tensor4p_kernel<true, false, true>,   tensor4p_kernel<true, true, true>};
+    const int v = (layer ? 4 : 0) + (pack ? 2 : 0) + (dg ? 1 : 0);
+    const Fn fn = fns[v];
     int per_sm = 1;
-    cudaError_t e = blocks_per_sm(cache[(pack ? 2 : 0) + (dg ? 1 : 0)], fn, kT4Threads, kT4Smem, per_sm);
+    cudaError_t e = blocks_per_sm(cache[v], fn, kT4Threads, kT4Smem, per_sm);
     if (e != cudaSuccess) return e;
     const long long items = g1 - g0;
     if (items <= 0) return cudaSuccess;
@@ -649,7 +734,7 @@ cudaError_t launch_tensor4(const ScanWork& w, const CUtensorMap& map_l256, const
     const unsigned grid = (unsigned)(items < sms ? items : sms);
     const T4Maps maps{pack ? map_l256 : map_l128, map_k, map_i};
     fn<<<grid, kT4Threads, kT4Smem, s>>>(maps, w, begin, per, g0, g1, k_cases, pack, sink, thr_q, dump, single, pairs,
-                                         triples, status);
+                                         triples, status, pinfo, n_pairs);
     count_launch();
     return cudaGetLastError();
 }

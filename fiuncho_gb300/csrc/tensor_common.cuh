@@ -154,6 +154,14 @@ __device__ __forceinline__ uint32_t f2u(float f) {  // f an exact integer in [0,
     return __float_as_uint(f + 8388608.0f) & 0x7FFFFFu;
 }
 
+// Row (SNP position) of SNP j in the operand planes ordered by residue mod
+// step (SNPs r, r + step, .. for r = 0, 1, ..; residue r holds
+// n / step + (r < n % step) SNPs).
+__host__ __device__ __forceinline__ int residue_row(int j, int step, int n) {
+    const int r = j % step;
+    return r * (n / step) + min(r, n % step) + j / step;
+}
+
 __device__ __forceinline__ float t3_lg2(float x) {
     float r;
     asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
