@@ -202,10 +202,10 @@ static int ensure_e4_items(fiu_ctx* ctx, const fiu_resident* res_c) {
 static bool tensor_ok(const fiu_resident* res, const ScanWork& w) {
     const bool data_ok = res->one_hot && res->d.n_cases >= 1 && res->d.n_ctrls >= 1 && res->d.n_cases <= 65535 &&
                          res->d.n_ctrls <= 65535 && res->d.snps < (1 << 21);
-    // a Distribution layer of the whole data set: order 2 (the owned SNPs of one residue), order 3 when
-    // the classes pack (the pair kernel's list mode), order 4 (the owned k of each pair)
+    // a Distribution layer of the whole data set: order 2 (the owned SNPs of one residue), order 3 (the
+    // owned j of each i: list mode), order 4 (the owned k of each pair)
     if (data_ok && !whole_data_set(res, w) && w.dist_n == res->d.snps &&
-        (w.order == 2 || (w.order == 3 && tensor_pack(res->d.n_cases, res->d.n_ctrls) != 0) ||
+        (w.order == 2 || w.order == 3 ||
          (w.order == 4 && res->d.snps >= 4 && triples_bytes(res->d.snps) <= kMaxTriplesBytes)))
         return true;
     const bool base = data_ok && whole_data_set(res, w);

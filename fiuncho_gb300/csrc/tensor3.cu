@@ -104,6 +104,43 @@ __device__ __forceinline__ void t3_decode(const long long* __restrict__ item_beg
     }
 }
 
+// List mode (a Distribution layer): the owned j of each i are listed in
+// jlist[jl_begin[i] .. jl_begin[i+1]); an item takes J consecutive entries
+// from p0 (= jl_begin[i] + J a) and an l-tile l0 = jlist[p0] + 1 + L b.
+template <int J, int L>
+__device__ __forceinline__ void t3l_decode(const long long* __restrict__ item_begin,
+                                           const long long* __restrict__ jl_begin, const int* __restrict__ jlist,
+                                           int n, long long g, int& i, long long& p0, int& l0) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (item_begin[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    i = lo;
+    long long q = g - item_begin[i];
+    for (long long p = jl_begin[i];; p += J) {
+        const int jf = jlist[p];
+        const long long nl = (n - 1 - jf + L - 1) / L;
+        if (q < nl) {
+            p0 = p;
+            l0 = jf + 1 + L * (int)q;
+            return;
+        }
+        q -= nl;
+    }
+}
+
+// The j of row jj (0..31) of a CTA's 32 j of an item: j0 + jj, or in list mode
+// the listed entry p0 + jj (n when the list of i ends before it).
+template <bool LIST>
+__device__ __forceinline__ int t3x_j(int j0, long long p0, long long p_end, const int* __restrict__ jlist, int jj,
+                                     int n) {
+    if (!LIST) return j0 + jj;
+    const long long p = p0 + jj;
+    return p < p_end ? __ldg(jlist + p) : n;
+}
+
 // 16-byte chunk of the epilogue transpose buffer holding the 4 counts
 // (cases z0, z1, controls z0, z1) of row (jl, xy) and column group k; the XOR
 // makes both the row-wise writes and the combination-wise reads free of bank
@@ -286,10 +323,14 @@ struct T3Maps {
     CUtensorMap l, j, i;
 };
 
+// LIST: a Distribution layer (t3l_decode; maps.j covers the residue-ordered planes, where the
+// listed j of one i are consecutive rows).
+template <bool LIST>
 __global__ void __launch_bounds__(kT3Threads, 1)
     tensor3_kernel(const __grid_constant__ T3Maps maps, ScanWork w, const long long* __restrict__ item_begin,
                    long long g0, long long g1, int k_cases, CandSink sink, float thr_f, uint32_t* dump,
-                   const uint32_t* __restrict__ single, const uint4* __restrict__ pairs, int* status) {
+                   const uint32_t* __restrict__ single, const uint4* __restrict__ pairs, int* status,
+                   const long long* __restrict__ jl_begin, const int* __restrict__ jlist) {
     extern __shared__ uint8_t smraw[];
     __shared__ __align__(8) uint64_t full_t[kT3Stages], full_a[kT3Stages], empty[kT3Stages];
     __shared__ __align__(8) uint64_t case_full, case_empty, ctrl_full, ctrl_empty, done;
@@ -338,8 +379,14 @@ __global__ void __launch_bounds__(kT3Threads, 1)
         if (lane == 0) {
             long long step = 0;
             for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x) {
-                int i, j0, l0;
-                t3_decode<kT3L>(item_begin, n, g, i, j0, l0);
+                int i, j0, l0;  // LIST: j0 = the first listed j's row in the residue-ordered planes
+                if (LIST) {
+                    long long p0;
+                    t3l_decode<kT3J, kT3L>(item_begin, jl_begin, jlist, n, g, i, p0, l0);
+                    j0 = residue_row(jlist[p0], w.dist_step, n);
+                } else {
+                    t3_decode<kT3L>(item_begin, n, g, i, j0, l0);
+                }
                 for (int ks = 0; ks < ksteps; ++ks) {
                     const int s = (int)(step % kT3Stages);
                     const long long u = step / kT3Stages;
@@ -463,8 +510,14 @@ __global__ void __launch_bounds__(kT3Threads, 1)
         const int jl = lane >> 2, xy = lane & 3, kp = lane & 3;
         long long item = 0;
         for (long long g = g0 + blockIdx.x; g < g1 && ok; g += gridDim.x, ++item) {
-            int i, j0, l0;
-            t3_decode<kT3L>(item_begin, n, g, i, j0, l0);
+            int i, j0 = 0, l0;
+            long long p0 = 0, p_end = 0;
+            if (LIST) {
+                t3l_decode<kT3J, kT3L>(item_begin, jl_begin, jlist, n, g, i, p0, l0);
+                p_end = jl_begin[i + 1];
+            } else {
+                t3_decode<kT3L>(item_begin, n, g, i, j0, l0);
+            }
             // ---- phase 1: case counts -> 16-bit stash, case columns free for the next item
             if (!t3_wait(smem_u32(&case_full), (uint32_t)(item & 1), abort)) {
                 ok = false;
@@ -494,7 +547,7 @@ __global__ void __launch_bounds__(kT3Threads, 1)
             if (lane == 0)
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&case_empty)) : "memory");
             // ---- per-item constants of this thread's j
-            const int j = j0 + 8 * q + jl;
+            const int j = t3x_j<LIST>(j0, p0, p_end, jlist, 8 * q + jl, n);
             const bool j_ok = j < n;
             uint4 pij;
             float si[2][2], sj[2][2];
@@ -634,42 +687,6 @@ __device__ __forceinline__ void t3x_decode(const long long* __restrict__ item_be
     }
 }
 
-// List mode (a Distribution layer): the owned j of each i are listed in
-// jlist[jl_begin[i] .. jl_begin[i+1]); an item takes 64 consecutive entries
-// from p0 (= jl_begin[i] + 64 a) and an l-tile l0 = jlist[p0] + 1 + 128 b.
-__device__ __forceinline__ void t3l_decode(const long long* __restrict__ item_begin,
-                                           const long long* __restrict__ jl_begin, const int* __restrict__ jlist,
-                                           int n, long long g, int& i, long long& p0, int& l0) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (item_begin[mid] <= g) lo = mid;
-        else hi = mid - 1;
-    }
-    i = lo;
-    long long q = g - item_begin[i];
-    for (long long p = jl_begin[i];; p += kPxJ) {
-        const int jf = jlist[p];
-        const long long nl = (n - 1 - jf + kPL - 1) / kPL;
-        if (q < nl) {
-            p0 = p;
-            l0 = jf + 1 + kPL * (int)q;
-            return;
-        }
-        q -= nl;
-    }
-}
-
-// The j of row jj (0..31) of this CTA's half of an item: the listed entry, or
-// n when the list of i ends before it.
-template <bool LIST>
-__device__ __forceinline__ int t3x_j(int j0, long long p0, long long p_end, const int* __restrict__ jlist, int jj,
-                                     int n) {
-    if (!LIST) return j0 + jj;
-    const long long p = p0 + jj;
-    return p < p_end ? __ldg(jlist + p) : n;
-}
-
 // LIST: the list mode above (maps.j then covers the residue-ordered planes,
 // where the listed j of one i are consecutive rows).
 template <bool LIST>
@@ -731,7 +748,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
                 int i, j0 = 0, l0;
                 if (LIST) {
                     long long p0;
-                    t3l_decode(item_begin, jl_begin, jlist, n, g, i, p0, l0);
+                    t3l_decode<kPxJ, kPL>(item_begin, jl_begin, jlist, n, g, i, p0, l0);
                     // this CTA's 32 listed j: consecutive residue-ordered rows from its first one (rows
                     // past the end of i's list are loaded too and ignored by the epilogue)
                     p0 += kT3J * (int)rank;
@@ -877,7 +894,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
             int i, j0 = 0, l0;
             long long p0 = 0, p_end = 0;
             if (LIST) {
-                t3l_decode(item_begin, jl_begin, jlist, n, g, i, p0, l0);
+                t3l_decode<kPxJ, kPL>(item_begin, jl_begin, jlist, n, g, i, p0, l0);
                 p0 += kT3J * (int)rank;
                 p_end = jl_begin[i + 1];
             } else {
@@ -1862,8 +1879,7 @@ struct T3Layers {
 static bool is_layer(const ScanWork& w) { return w.dist_step != 1 || w.dist_offset != 0; }
 
 bool tensor_layer_ok(const T3Plan& plan, const ScanWork& w) {
-    return (w.order == 2 || (w.order == 3 && plan.pair3) || (w.order == 4 && w.d.snps >= 4)) &&
-           w.dist_n == w.d.snps;
+    return (w.order == 2 || w.order == 3 || (w.order == 4 && w.d.snps >= 4)) && w.dist_n == w.d.snps;
 }
 
 static const T3Layer* find_layer(const T3Plan& plan, const ScanWork& w) {
@@ -1970,7 +1986,9 @@ cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s) {
             jl.push_back(i + 1 + (int)t);
             combos += n - 2 - i - t;
         }
-        for (size_t a = (size_t)jb[i]; a < jl.size(); a += kPxJ) total += (n - 1 - jl[a] + kPL - 1) / kPL;
+        // items of J listed j and L l: the pair kernel's (classes that pack) or the per-class kernel's
+        const int J = plan.pair3 ? kPxJ : kT3J, L = plan.pair3 ? kPL : kT3L;
+        for (size_t a = (size_t)jb[i]; a < jl.size(); a += J) total += (n - 1 - jl[a] + L - 1) / L;
     }
     ib[n] = total;
     jb[n] = (long long)jl.size();
@@ -2163,7 +2181,10 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
     }
     // set once, by whichever host thread comes first (thread-safe static initialisation)
     static const cudaError_t attr = [] {
-        cudaError_t e = cudaFuncSetAttribute(tensor3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);
+        cudaError_t e = cudaFuncSetAttribute(tensor3_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kT3Smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tensor3_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT3Smem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(tensor2_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kT2Smem);
         if (e == cudaSuccess)
@@ -2235,8 +2256,17 @@ cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, 
         count_launch();
         return cudaGetLastError();
     }
-    tensor3_kernel<<<grid, kT3Threads, kT3Smem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, sink, thr_f,
-                                                     dump, single, pairs, status);
+    if (is_layer(w)) {
+        const T3Layer* L = find_layer(plan, w);
+        if (!L || !tensor_layer_ok(plan, w)) return cudaErrorInvalidValue;
+        const T3Maps lmaps{plan.map_l, L->map_jr, plan.map_i};
+        tensor3_kernel<true><<<grid, kT3Threads, kT3Smem, s>>>(lmaps, w, L->item_begin, g0, g1, plan.k_cases, sink,
+                                                               thr_f, dump, single, pairs, status, L->jl_begin,
+                                                               L->jlist);
+    } else {
+        tensor3_kernel<false><<<grid, kT3Threads, kT3Smem, s>>>(maps, w, plan.item_begin, g0, g1, plan.k_cases, sink,
+                                                                thr_f, dump, single, pairs, status, nullptr, nullptr);
+    }
     count_launch();
     return cudaGetLastError();
 }

@@ -19,9 +19,9 @@
  *
  * Multi-GPU: MPIEngine gives rank r of N the strided prefix share
  * Distribution(snps, order-1, N, r) (MPIEngine.h:133-134).  The tensor-core
- * kernels serve such a share themselves at orders 2 and 4 and, when the
- * classes share one accumulator, at order 3, with the reference's per-rank
- * list; other shares run on the CUDA-core kernels.  With shard_ranks = true a rank share
+ * kernels serve such a share themselves at orders 2, 3 and 4 (one-hot data),
+ * with the reference's per-rank list; other shares run on the CUDA-core
+ * kernels.  With shard_ranks = true a rank share
  * runs as shard r of N of the whole search instead (fiu_search_shard: equal
  * ranges of the tensor-core work units, every order); the rank's own list
  * then differs from the strided share's, but MPIEngine's gathered result is

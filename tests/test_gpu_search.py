@@ -448,18 +448,20 @@ def test_tensor_kernel_scope(gs, golden_synth):
 
 
 @pytest.mark.parametrize("order,n_ranks,nc,nt", [(3, r, 1300, 1217) for r in (2, 3, 4, 5, 6, 7)] +
+                         [(3, r, 9000, 9800) for r in (2, 3, 5)] +
                          [(2, r, 1300, 1217) for r in (2, 3, 5, 7)] + [(2, r, 9000, 9800) for r in (2, 3, 7)] +
                          [(4, r, 1300, 1217) for r in (2, 3, 5, 7)] + [(4, r, 9000, 9800) for r in (2, 3)])
 def test_rank_layers_on_the_tensor_kernel(oracle, order, n_ranks, nc, nt):
     """MPIEngine gives rank r of N the strided share Distribution(snps, order-1, N, r)
     (MPIEngine.h:133-134, Distribution.h:172-176): on the tensor kernels (order 3: the
-    pair kernel's list mode; order 2: the owned SNPs of one residue mod N; order 4: the
-    owned k of each pair (i, j); classes that pack and classes that do not), forced and
+    list modes of the pair and the per-class kernels; order 2: the owned SNPs of one
+    residue mod N; order 4: the owned k of each pair (i, j); classes that pack and classes
+    that do not), forced and
     automatic, every rank's list equals the oracle's list of that rank, and the ranks'
     lists merged as MPIEngine merges them give the whole search."""
     from fiuncho_gb300 import Dataset, Distribution, GpuSearch, MPIEngine, Resident
     rng = np.random.default_rng(100 + n_ranks + 10 * order)
-    snps = {2: 700, 3: 170, 4: 60 if nc < 5000 else 40}[order]
+    snps = {2: 700, 3: 170 if nc < 5000 else 90, 4: 60 if nc < 5000 else 40}[order]
     maf = rng.uniform(0.05, 0.5, snps)[:, None]
     u = rng.random((snps, nc + nt))
     geno = ((u >= (1 - maf) ** 2).astype(np.uint8) + (u >= 1 - maf ** 2)).astype(np.uint8)
@@ -478,17 +480,17 @@ def test_rank_layers_on_the_tensor_kernel(oracle, order, n_ranks, nc, nt):
     assert [x.combination for x in MPIEngine().gather(parts, 30)] == [x.combination for x in whole]
 
 
-@pytest.mark.parametrize("order", [2, 4])
+@pytest.mark.parametrize("order", [2, 3, 4])
 @pytest.mark.parametrize("nc,nt", [(999, 1001), (9000, 9800)])
 @pytest.mark.parametrize("step,offset", [(2, 1), (3, 0), (3, 2), (64, 5), (200, 0)])
 def test_layer_tables(gs, oracle, order, nc, nt, step, offset):
-    """Every table of an order-2 or order-4 Distribution layer on the tensor kernel
-    (classes that pack and classes that do not) equals the oracle's: the digest of all
-    of them and their count (order 2, 130 SNPs: tiles of 64 owned SNPs end inside the
-    residue class and past it; order 4, 40 SNPs: tiles of 16 owned k)."""
+    """Every table of a Distribution layer on the tensor kernels (classes that pack and
+    classes that do not) equals the oracle's: the digest of all of them and their count
+    (order 2, 130 SNPs: tiles of 64 owned SNPs end inside the residue class and past it;
+    order 3, 70 SNPs: 32 or 64 listed j per item; order 4, 40 SNPs: tiles of 16 owned k)."""
     from fiuncho_gb300 import Distribution
     from fiuncho_gb300.search import Resident
-    ds = _one_hot_dataset(7 + step, 130 if order == 2 else 40, nc, nt)
+    ds = _one_hot_dataset(7 + step, {2: 130, 3: 70, 4: 40}[order], nc, nt)
     res = Resident(gs.ctx, ds)
     want = oracle.table_digest(ds.data, ds.snps, ds.cases_words, ds.ctrls_words, order,
                                dist=(ds.snps, step, offset))
