@@ -250,6 +250,9 @@ int choose_tile(fiu_ctx* ctx, const fiu_resident* res, const ScanWork& w, int re
         if (!whole_data_set(res, w)) {
             cudaError_t e = tensor3_layer(*r->t3, w, ctx->stream);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor work items of a distribution layer");
+        } else {
+            cudaError_t e = tensor3_order_items(*r->t3, r->d, w.order);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor work items");
         }
         kernel = FIU_KERNEL_TENSOR;
         // GEMM width N: order 3 uses 256 with one accumulator for both classes, 192 with one per class

@@ -166,6 +166,7 @@ cudaError_t launch_elided4p(const ScanWork& w, const long long* begin, long long
 // class padded to a multiple of 128 samples), their TMA descriptors and the
 // work-item prefix sums.
 struct T3Plan {
+    std::mutex items_mu;  // guards the order-3 / order-4 item tables made on first use
     uint8_t* planes = nullptr;
     int pack = 0;         // log2 of the control weight W when one accumulator holds both classes (else 0)
     double item_combos = 0;  // combinations per work item, about 32 x L / 2
@@ -210,6 +211,8 @@ double tensor_item_combos(const T3Plan& plan, const ScanWork& w);
 bool tensor_layer_ok(const T3Plan& plan, const ScanWork& w);
 cudaError_t tensor3_layer(T3Plan& plan, const ScanWork& w, cudaStream_t s);
 cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s);
+// The whole data set's work items at order 3 or 4, made on first use (thread-safe).
+cudaError_t tensor3_order_items(T3Plan& plan, const DevData& d, int order);
 void tensor3_release(T3Plan& plan);
 cudaError_t launch_tensor3(const ScanWork& w, const T3Plan& plan, long long g0, long long g1, const CandSink& sink,
                            uint32_t* dump, const uint32_t* single, const uint4* pairs, const uint4* triples,

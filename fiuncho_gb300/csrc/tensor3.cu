@@ -1804,11 +1804,8 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
     plan.item_combos = J * L / 2.0;
     plan.k_cases = kT3KB * ((d.cw + 1) / 2);
     plan.pitch = plan.k_cases + kT3KB * ((d.tw + 1) / 2);
-    std::vector<long long> ib;
-    plan.total = t3_items(d.snps, L, ib, J);
-    cudaError_t e = cudaMalloc((void**)&plan.item_begin, ib.size() * sizeof(long long));
-    if (e == cudaSuccess) e = cudaMemcpy(plan.item_begin, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&plan.planes, (size_t)2 * d.snps * plan.pitch);
+    (void)L;
+    cudaError_t e = cudaMalloc((void**)&plan.planes, (size_t)2 * d.snps * plan.pitch);
     if (e != cudaSuccess) return e;
     const long long total = 2ll * d.snps * (plan.pitch / 16);
     const int grid = (int)std::min<long long>((total + 255) / 256, 4096);
@@ -1832,22 +1829,50 @@ cudaError_t tensor3_prepare(const DevData& d, T3Plan& plan, cudaStream_t s) {
         e = cudaMemcpy(plan.item2_begin, ib2.data(), ib2.size() * sizeof(long long), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
     if ((e = t3_map(&plan.map_a2, plan.planes, rows, plan.pitch, kT2M, true)) != cudaSuccess) return e;
-    if ((e = t3_map(&plan.map_b2, plan.planes, rows, plan.pitch, kT2N, true)) != cudaSuccess) return e;
-    // order 4
-    if (d.snps < 4) return cudaSuccess;
-    std::vector<long long> per4;
-    const std::vector<long long> ib4 = t4_item_table(d.snps, plan.pack != 0, per4);
-    plan.total4 = ib4.back();
-    const double n = d.snps;
-    plan.item4_combos = n * (n - 1) * (n - 2) * (n - 3) / 24.0 / std::max(1ll, plan.total4);
-    e = cudaMalloc((void**)&plan.item4_begin, ib4.size() * sizeof(long long));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&plan.item4_per, per4.size() * sizeof(long long));
-    if (e == cudaSuccess)
-        e = cudaMemcpy(plan.item4_begin, ib4.data(), ib4.size() * sizeof(long long), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(plan.item4_per, per4.data(), per4.size() * sizeof(long long), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return e;
-    return t3_map(&plan.map_k4, plan.planes, rows, plan.pitch, 32, true);
+    return t3_map(&plan.map_b2, plan.planes, rows, plan.pitch, kT2N, true);
+}
+
+// The work items of the whole data set at order 3 or 4, made on the first
+// search of that order (the host enumeration grows as n^2 / 16 at order 4:
+// about 0.1 s at 40 000 SNPs, which a search of another order need not pay).
+cudaError_t tensor3_order_items(T3Plan& plan, const DevData& d, int order) {
+    std::lock_guard<std::mutex> g(plan.items_mu);
+    cudaError_t e = cudaSuccess;
+    if (order == 3 && !plan.item_begin) {
+        const int L = plan.pack ? kPL : kT3L, J = plan.pair3 ? kPxJ : kT3J;
+        std::vector<long long> ib;
+        const long long total = t3_items(d.snps, L, ib, J);
+        long long* p = nullptr;
+        e = cudaMalloc((void**)&p, ib.size() * sizeof(long long));
+        if (e == cudaSuccess) e = cudaMemcpy(p, ib.data(), ib.size() * sizeof(long long), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(p);
+            return e;
+        }
+        plan.total = total;
+        plan.item_begin = p;
+    }
+    if (order == 4 && !plan.item4_begin && d.snps >= 4) {
+        std::vector<long long> per4;
+        const std::vector<long long> ib4 = t4_item_table(d.snps, plan.pack != 0, per4);
+        long long *pb = nullptr, *pp = nullptr;
+        e = t3_map(&plan.map_k4, plan.planes, 2 * d.snps, plan.pitch, 32, true);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&pb, ib4.size() * sizeof(long long));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&pp, per4.size() * sizeof(long long));
+        if (e == cudaSuccess) e = cudaMemcpy(pb, ib4.data(), ib4.size() * sizeof(long long), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(pp, per4.data(), per4.size() * sizeof(long long), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(pb);
+            cudaFree(pp);
+            return e;
+        }
+        plan.total4 = ib4.back();
+        const double n = d.snps;
+        plan.item4_combos = n * (n - 1) * (n - 2) * (n - 3) / 24.0 / std::max(1ll, plan.total4);
+        plan.item4_per = pp;
+        plan.item4_begin = pb;
+    }
+    return e;
 }
 
 // Work items of Distribution layers of order-3 scans (the pair kernel's list
