@@ -1,8 +1,12 @@
 // Multi-scan kernels: many scans of different sizes, orders and sample counts
 // progress together in rounds.  A round is one persistent launch over the
-// union of every active scan's next chunk of prefixes (work items are
-// (scan, prefix ordinal) pairs found by binary search over the round's
-// entries, then unranked on the device), followed by one CTA per scan that
+// union of every active scan's next chunk of prefixes: work items are
+// (scan, prefix ordinal) pairs that the CTAs' groups pull from a device work
+// queue (one 64-bit cursor per launch, advanced with atomicAdd), locate by
+// binary search over the round's entries and unrank on the device.  A group
+// takes its next item when it finishes the last, so scans whose prefixes cost
+// more (more samples, more last SNPs) never leave a statically assigned tail.
+// Each round is followed by one CTA per scan that
 // selects its best candidates and raises its admission threshold on the
 // device -- so no host round trip is needed between rounds and a whole batch
 // can be captured as one CUDA graph.  The final pass re-scores every scan's
@@ -60,11 +64,24 @@ template <int FAMILY, int TP>
 __global__ void __launch_bounds__(kRoundThreads, 2) round_kernel(const ScanDesc* __restrict__ scans,
                                                                  ScanState* states,
                                                                  const RoundEntry* __restrict__ ents, int n_ents,
-                                                                 long long total, size_t stride) {
+                                                                 long long total, size_t stride,
+                                                                 unsigned long long* queue) {
     extern __shared__ uint64_t sm[];
     constexpr int G = kRoundThreads / TP;
+    __shared__ long long claim[2][G];  // double-buffered: one group barrier per claim
     const int grp = threadIdx.x / TP;
-    for (long long g = (long long)blockIdx.x * G + grp; g < total; g += (long long)gridDim.x * G) {
+    for (int it = 0;; ++it) {
+        long long g;
+        if (TP == 32) {
+            unsigned long long c = 0;
+            if ((threadIdx.x & 31) == 0) c = atomicAdd(queue, 1ull);
+            g = (long long)__shfl_sync(0xffffffffu, c, 0);
+        } else {
+            if (threadIdx.x % TP == 0) claim[it & 1][grp] = (long long)atomicAdd(queue, 1ull);
+            group_sync<TP>(grp);
+            g = claim[it & 1][grp];
+        }
+        if (g >= total) break;
         int lo = 0, hi = n_ents - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -136,14 +153,17 @@ cudaError_t prepare_round_kernels(size_t smem) {
 
 template <int FAMILY, int TP>
 static void launch_round_t(unsigned grid, size_t smem, const ScanDesc* scans, ScanState* states,
-                           const RoundEntry* ents, int n_ents, long long total, cudaStream_t s) {
+                           const RoundEntry* ents, int n_ents, long long total, unsigned long long* queue,
+                           cudaStream_t s) {
     const size_t stride = smem / sizeof(uint64_t) / (kRoundThreads / TP);
-    round_kernel<FAMILY, TP><<<grid, kRoundThreads, smem, s>>>(scans, states, ents, n_ents, total, stride);
+    round_kernel<FAMILY, TP><<<grid, kRoundThreads, smem, s>>>(scans, states, ents, n_ents, total, stride, queue);
 }
 
 cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* states, const RoundEntry* ents,
-                         int n_ents, long long total, size_t smem, int sms, cudaStream_t s) {
+                         int n_ents, long long total, size_t smem, int sms, unsigned long long* queue,
+                         cudaStream_t s) {
     if (total <= 0 || n_ents <= 0) return cudaSuccess;
+    if (!queue) return cudaErrorInvalidValue;
     const int ti = tp_index(tp);
     if (family < 0 || family > 2) return cudaErrorInvalidValue;
     size_t sm = 0;
@@ -159,24 +179,24 @@ cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* s
     const unsigned grid = (unsigned)(ctas < cap ? ctas : cap);
     if (family == 2) {
         switch (ti) {
-            case 0: launch_round_t<2, 32>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            case 1: launch_round_t<2, 64>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            case 2: launch_round_t<2, 128>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            default: launch_round_t<2, 256>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 0: launch_round_t<2, 32>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            case 1: launch_round_t<2, 64>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            case 2: launch_round_t<2, 128>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            default: launch_round_t<2, 256>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
         }
     } else if (family == 0) {
         switch (ti) {
-            case 0: launch_round_t<0, 32>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            case 1: launch_round_t<0, 64>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            case 2: launch_round_t<0, 128>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            default: launch_round_t<0, 256>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 0: launch_round_t<0, 32>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            case 1: launch_round_t<0, 64>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            case 2: launch_round_t<0, 128>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            default: launch_round_t<0, 256>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
         }
     } else {
         switch (ti) {
-            case 0: launch_round_t<1, 32>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            case 1: launch_round_t<1, 64>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            case 2: launch_round_t<1, 128>(grid, sm, scans, states, ents, n_ents, total, s); break;
-            default: launch_round_t<1, 256>(grid, sm, scans, states, ents, n_ents, total, s); break;
+            case 0: launch_round_t<1, 32>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            case 1: launch_round_t<1, 64>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            case 2: launch_round_t<1, 128>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
+            default: launch_round_t<1, 256>(grid, sm, scans, states, ents, n_ents, total, queue, s); break;
         }
     }
     count_launch();

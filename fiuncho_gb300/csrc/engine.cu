@@ -174,12 +174,19 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
         std::vector<long long> grp_total;   // items of group g
         std::vector<int> grp_family, grp_tp;
         std::vector<long long> cursor(n, 0), chunk(n);
+        std::vector<double> cost(n);  // work of one prefix: words x last SNPs per prefix
         for (int s = 0; s < n; ++s) cursor[s] = plans[s].m_begin;
         for (int s = 0; s < n; ++s) {
             const auto& w = plans[s].w;
             const double per = (double)binom(w.dist_n, w.order) / std::max(1.0, (double)binom(w.dist_n, w.order - 1));
             chunk[s] = std::max<long long>(1, (long long)(plans[s].keep / std::max(1.0, per)));
+            cost[s] = per * (double)(w.d.cw + w.d.tw);
         }
+        // entries of a launch in decreasing cost per prefix: the work queue hands
+        // out the long items first, the short ones fill the tail
+        std::vector<int> by_cost(n);
+        for (int s = 0; s < n; ++s) by_cost[s] = s;
+        std::stable_sort(by_cost.begin(), by_cost.end(), [&](int a, int b) { return cost[a] > cost[b]; });
         int rounds = 0;
         for (bool more = true; more; ++rounds) {
             more = false;
@@ -192,7 +199,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
                 for (int tp : {32, 64, 128, 256}) {
                     long long total = 0;
                     grp_first.push_back(ents.size());
-                    for (int s = 0; s < n; ++s) {
+                    for (int s : by_cost) {
                         if (!take[s] || round_family(plans[s].kind, plans[s].w.order) != fam || plans[s].tp != tp)
                             continue;
                         ents.push_back(RoundEntry{s, 0, cursor[s], total});
@@ -209,12 +216,14 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
             }
         }
         grp_first.push_back(ents.size());
-        // ---- device arena: [descs][states][slot_begin][entries][per-scan buffers]
+        // ---- device arena: [descs][states][slot_begin][entries][queue cursors][per-scan buffers]
+        const size_t n_groups = grp_first.size() - 1;
         const size_t off_desc = 0;
         const size_t off_state = align256(off_desc + n * sizeof(ScanDesc));
         const size_t off_slots = align256(off_state + n * sizeof(ScanState));
         const size_t off_ents = align256(off_slots + n * sizeof(unsigned));
-        const size_t off_bufs = align256(off_ents + ents.size() * sizeof(RoundEntry));
+        const size_t off_queue = align256(off_ents + ents.size() * sizeof(RoundEntry));
+        const size_t off_bufs = align256(off_queue + n_groups * sizeof(unsigned long long));
         int rc = grow_bytes(ctx, ctx->arena, ctx->arena_cap, off_bufs + bytes);
         if (rc) return rc;
         char* base = ctx->arena;
@@ -252,11 +261,13 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
            "upload");
         CK(cudaMemcpyAsync(base + off_ents, ents.data(), ents.size() * sizeof(RoundEntry), cudaMemcpyHostToDevice, st),
            "upload");
+        CK(cudaMemsetAsync(base + off_queue, 0, n_groups * sizeof(unsigned long long), st), "upload");
         CK(cudaStreamSynchronize(st), "upload");
         const ScanDesc* d_desc = (const ScanDesc*)(base + off_desc);
         ScanState* d_state = (ScanState*)(base + off_state);
         const unsigned* d_slots = (const unsigned*)(base + off_slots);
         const RoundEntry* d_ents = (const RoundEntry*)(base + off_ents);
+        unsigned long long* d_queue = (unsigned long long*)(base + off_queue);
         // host mirror of results (pinned, so the copies can live in a graph)
         rc = grow_host(ctx, bytes + n * sizeof(ScanState));
         if (rc) return rc;
@@ -267,7 +278,7 @@ extern "C" int fiu_search_batch(fiu_ctx* ctx, fiu_scan* scans, unsigned n_scans,
                 const int ne = (int)(grp_first[g + 1] - grp_first[g]);
                 if (ne)
                     e = launch_round(grp_family[g], grp_tp[g], d_desc, d_state, d_ents + grp_first[g], ne,
-                                     grp_total[g], smem, ctx->sms, st);
+                                     grp_total[g], smem, ctx->sms, d_queue + g, st);
                 if (e == cudaSuccess && g % 8 == 7) e = launch_select_scans(d_desc, d_state, n, 0, st);
             }
             if (e == cudaSuccess) e = launch_select_scans(d_desc, d_state, n, 1, st);

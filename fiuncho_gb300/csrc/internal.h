@@ -76,8 +76,10 @@ size_t round_smem(const ScanDesc& sd);
 // kernel at order 4; tp as in ScanDesc.
 constexpr int kRoundFamilies = 3;
 inline int round_family(int kind, int order) { return kind == FIU_KERNEL_FULL_ID ? 1 : order == 4 ? 2 : 0; }
+// queue: the launch's work-queue cursor (device, zero before the launch).
 cudaError_t launch_round(int family, int tp, const ScanDesc* scans, ScanState* states, const RoundEntry* ents,
-                         int n_ents, long long total, size_t smem, int sms, cudaStream_t s);
+                         int n_ents, long long total, size_t smem, int sms, unsigned long long* queue,
+                         cudaStream_t s);
 cudaError_t launch_select_scans(const ScanDesc* scans, ScanState* states, int n_scans, int final_pass,
                                 cudaStream_t s);
 cudaError_t launch_finish_scans(const ScanDesc* scans, ScanState* states, const unsigned* slot_begin, int n_scans,

@@ -108,6 +108,7 @@ struct fiu_server {
     ScanDesc* d_desc = nullptr;
     ScanState* d_state = nullptr;
     unsigned* d_zero = nullptr;
+    unsigned long long* d_queue = nullptr;  // one work-queue cursor per round launch (family x tile width)
     RoundEntry* d_ents = nullptr;
     size_t ents_cap = 0;
     std::vector<int> free_slots;
@@ -271,12 +272,22 @@ int run_round(fiu_server* sv) {
         ServeScan* s = sv->active[i];
         take[i] = std::min({s->m_end - s->cursor, s->chunk, s->max_chunk});
     }
+    // entries of a launch in decreasing work per prefix (words x last SNPs per
+    // prefix): the device work queue hands out the long items first
+    std::vector<size_t> by_cost(sv->active.size());
+    std::vector<double> cost(sv->active.size());
+    for (size_t i = 0; i < sv->active.size(); ++i) {
+        const ScanWork& w = sv->active[i]->w;
+        by_cost[i] = i;
+        cost[i] = (double)(w.dist_n - w.order + 2) / w.order * (double)(w.d.cw + w.d.tw);
+    }
+    std::stable_sort(by_cost.begin(), by_cost.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
     std::vector<std::pair<int, int>> gkey;  // (family, tp) of each group
     for (int fam = 0; fam < kRoundFamilies; ++fam)
         for (int tp : {32, 64, 128, 256}) {
             const size_t first = ents.size();
             long long total = 0;
-            for (size_t i = 0; i < sv->active.size(); ++i) {
+            for (size_t i : by_cost) {
                 ServeScan* s = sv->active[i];
                 if (!take[i] || round_family(s->kind, s->order) != fam || s->tp != tp) continue;
                 ents.push_back(RoundEntry{s->slot, 0, s->cursor, total});
@@ -296,11 +307,12 @@ int run_round(fiu_server* sv) {
     CK(prepare_round_kernels(smem), "kernel attributes");
     CK(cudaMemcpyAsync(sv->d_ents, ents.data(), ents.size() * sizeof(RoundEntry), cudaMemcpyHostToDevice, st),
        "round entries");
+    CK(cudaMemsetAsync(sv->d_queue, 0, kRoundFamilies * 4 * sizeof(unsigned long long), st), "work queue");
     for (size_t g = 0; g < groups.size(); ++g) {
         const size_t first = groups[g].first;
         const size_t ne = (g + 1 < groups.size() ? groups[g + 1].first : ents.size()) - first;
         if (ne) CK(launch_round(gkey[g].first, gkey[g].second, sv->d_desc, sv->d_state, sv->d_ents + first, (int)ne,
-                                groups[g].second, smem, ctx->sms, st), "round");
+                                groups[g].second, smem, ctx->sms, sv->d_queue + g, st), "round");
     }
     CK(launch_select_scans(sv->d_desc, sv->d_state, kSlots, 0, st), "selection");
     std::vector<ServeScan*> done, still;
@@ -432,12 +444,14 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
     if (cudaMalloc((void**)&sv->d_desc, kSlots * sizeof(ScanDesc)) != cudaSuccess ||
         cudaMalloc((void**)&sv->d_state, kSlots * sizeof(ScanState)) != cudaSuccess ||
         cudaMalloc((void**)&sv->d_zero, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc((void**)&sv->d_queue, kRoundFamilies * 4 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMemset(sv->d_desc, 0, kSlots * sizeof(ScanDesc)) != cudaSuccess ||
         cudaMemset(sv->d_state, 0, kSlots * sizeof(ScanState)) != cudaSuccess ||
         cudaMemset(sv->d_zero, 0, sizeof(unsigned)) != cudaSuccess) {
         cudaFree(sv->d_desc);
         cudaFree(sv->d_state);
         cudaFree(sv->d_zero);
+        cudaFree(sv->d_queue);
         for (fiu_ctx* c : sv->solo_ctx) fiu_destroy(c);
         fiu_destroy(sv->ctx);
         delete sv;
@@ -566,6 +580,7 @@ void fiu_server_destroy(fiu_server* sv) {
     cudaFree(sv->d_desc);
     cudaFree(sv->d_state);
     cudaFree(sv->d_zero);
+    cudaFree(sv->d_queue);
     cudaFree(sv->d_ents);
     for (fiu_ctx* c : sv->solo_ctx) fiu_destroy(c);
     fiu_destroy(sv->ctx);
