@@ -43,11 +43,16 @@ namespace fiu {
 constexpr int kT4K = 16, kT4L = 128;                // k and l SNPs per work item (64 l in the split form)
 constexpr int kT4M = 8 * kT4K, kT4N = 2 * kT4L;     // 128 x 256 GEMM tile
 // Two A builders keep pace with the MMA (about 130 instructions per builder
-// thread and k-step against ~640 tensor cycles); 12 warps (three per SM
-// sub-partition) leave 168 registers a thread, which the epilogue's
-// derivation needs (128 at 16 warps made it spill ~1 KB a thread).
+// thread and k-step against ~640 tensor cycles).  The epilogue warps (a
+// multiple of 4: each reads the tensor-memory lane quarter warp % 4) share an
+// item's column groups of 8 l round-robin within their quarter.  12 warps in
+// all (three per SM sub-partition) leave 168 registers a thread, which the
+// epilogue's derivation needs: 12 epilogue warps (16 in all, 128 registers,
+// ~100 bytes of spills) took 137 instead of 82 ms for 300 SNPs x 4 000/4 000
+// and 173 instead of 166 ms for 400 SNPs x 558/1 012.
 constexpr int kT4BuildWarps = 2, kT4EpiWarps = 8;
-constexpr int kT4Threads = 32 * (2 + kT4BuildWarps + kT4EpiWarps);  // 384
+constexpr int kT4Threads = 32 * (2 + kT4BuildWarps + kT4EpiWarps);
+static_assert(kT4EpiWarps % 4 == 0, "epilogue warps cover the four lane quarters evenly");
 constexpr int kT4BuildRows = 2 * kT4K / (4 * kT4BuildWarps);          // k rows per builder thread and stage
 static_assert(2 * kT4K % (4 * kT4BuildWarps) == 0, "builder threads split the k rows evenly");
 constexpr int kT4Stages = 3;
@@ -57,7 +62,7 @@ constexpr int kT4SK = 2 * kT4K * kT3KB;             //  4 KB  k rows
 constexpr int kT4SI = 1024;                         // i rows (2 x 128 B) in a 1 KB slot
 constexpr int kT4SJ = 1024;                         // j rows
 constexpr int kT4Stage = kT4SB + kT4SA + kT4SK + kT4SI + kT4SJ;  // 54 KB, a multiple of 1 KB
-constexpr int kT4Ebuf = 4096;                       // per epilogue warp: 32 combinations x 8 (x,y,z) x 16 B
+constexpr int kT4Ebuf = 2048;                       // per epilogue warp: 32 combinations x 8 (x,y,z) x 8 B
 
 // Sources of the epilogue that depend on one of k or l only, copied into
 // shared memory by the epilogue threads (cp.async: global to shared without
@@ -159,10 +164,11 @@ __device__ __forceinline__ void t4_item(const long long* __restrict__ begin, con
     else t4_decode<L>(begin, per, w.d.snps, g, i, j, k0, l0);
 }
 
-// 16-byte chunk of the epilogue transpose buffer holding (cases w0, w1,
-// controls w0, w1) of row (kk, xyz) for the column group ll; conflict-free for
-// the row-wise writes (fixed ll) and the combination-wise reads (fixed xyz).
-__device__ __forceinline__ int t4_chunk(int kk, int ll, int xyz) { return (kk * 8 + ll) * 8 + (xyz ^ ll); }
+// 8-byte slot of the epilogue transpose buffer holding (cases w0 | w1 << 16,
+// controls w0 | w1 << 16) of row (kk, xyz) for the column ll of a group;
+// conflict-free for the row-wise writes (fixed ll) and the combination-wise
+// reads (fixed xyz): each half-warp covers the 32 banks once.
+__device__ __forceinline__ int t4_slot(int kk, int ll, int xyz) { return kk * 64 + (ll ^ (kk & 1)) * 8 + (xyz ^ ll); }
 
 // The cores of one combination that depend on both k and l: triples (i,k,l)
 // and (j,k,l) (cases, controls) and pair (k,l), loaded from global memory at
@@ -382,7 +388,8 @@ __global__ void __launch_bounds__(kT4Threads, 1)
     constexpr int L = PACK ? kT4L : kT4L / 2;                     // l per item
     constexpr int NR = 2 * L;                                       // N of one accumulator region
     constexpr uint32_t kTx = NR * kT3KB + kT4SK + 2 * 2 * kT3KB;  // bytes the TMA brings per stage
-    constexpr int NCC = L / 16;                                     // column groups of 8 l per epilogue warp
+    constexpr int NG = L / 8;                                       // column groups of 8 l per item
+    constexpr int H = kT4EpiWarps / 4;                              // epilogue warps per lane quarter
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -547,15 +554,15 @@ __global__ void __launch_bounds__(kT4Threads, 1)
         }
     } else {
         // ---------------------------------------------------------------- epilogue
-        const int e = warp - (2 + kT4BuildWarps);  // 0..7
+        const int e = warp - (2 + kT4BuildWarps);  // 0 .. kT4EpiWarps - 1
         const int q = warp & 3;                     // tensor-memory lane quarter this warp may access
-        const int hh = e >> 2;                      // column groups 2 cc + hh: l offsets 16 cc + 8 hh + [0, 8)
+        const int hh = e >> 2;                      // column groups hh, hh + H, ...: l offsets 8 gi + [0, 8)
         uint32_t* ebuf = ebuf_all + e * (kT4Ebuf / 4);
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
         const uint32_t wmask = PACK ? (1u << pack) - 1u : 0xffffffffu;
         const int kkw = lane >> 3, xyz = lane & 7;  // this thread's accumulator row (4 q + kkw, xyz)
         const int kkc = lane >> 3, llc = lane & 7;  // this lane's combination in a column group
-        const int et = tid - 32 * (2 + kT4BuildWarps);  // 0..255
+        const int et = tid - 32 * (2 + kT4BuildWarps);  // 0 .. 32 kT4EpiWarps - 1
         T4Item* items = reinterpret_cast<T4Item*>(ebuf_all + kT4EpiWarps * (kT4Ebuf / 4));  // two buffers
         long long item = 0;
         if (g0 + blockIdx.x < g1)
@@ -566,7 +573,7 @@ __global__ void __launch_bounds__(kT4Threads, 1)
             const int buf = (int)(item & 1);
             const int k = k0 + (LAYER ? w.dist_step : 1) * (4 * q + kkc);
             // this thread's copies of the item's sources have landed; the named
-            // barrier (the 256 epilogue threads) makes everyone's visible and
+            // barrier (the epilogue threads) makes everyone's visible and
             // frees the other buffer (every thread is done with the previous item)
             asm volatile("cp.async.wait_group 0;" ::: "memory");
             asm volatile("bar.sync 1, %0;" ::"n"(32 * kT4EpiWarps) : "memory");
@@ -580,13 +587,14 @@ __global__ void __launch_bounds__(kT4Threads, 1)
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
-            for (int cc = 0; cc < NCC; ++cc) {
-                const int l = l0 + 16 * cc + 8 * hh + llc;  // the two warps of a quarter interleave
+            for (int gi = hh; gi < NG; gi += H) {
+                const int l = l0 + 8 * gi + llc;  // the warps of a quarter interleave
                 const bool valid = k < n && l < n && l > k;
+                const bool last = gi + H >= NG;  // this warp's last column group of the item
                 // a column group without a valid combination in this warp is skipped
                 // (its accumulators are never read); the region is still released
                 if (!__any_sync(0xffffffffu, valid)) {
-                    if (cc == NCC - 1) {
+                    if (last) {
                         asm volatile("tcgen05.fence::before_thread_sync;");
                         __syncwarp();
                         if (lane == 0)
@@ -598,12 +606,12 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                 T4KL kl{};
                 if (valid && !dump) kl = t4_load_kl(pairs, triples, i, j, k, l, n);
                 {
-                    const uint32_t col = (uint32_t)(kT4N * buf + 32 * cc + 16 * hh);
+                    const uint32_t col = (uint32_t)(kT4N * buf + 16 * gi);
                     uint32_t v[16], vt[16];
                     t4_ld16(lane_base + col, v);
                     if (!PACK) t4_ld16(lane_base + col + NR, vt);  // control counts of the same rows / columns
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    if (cc == NCC - 1) {  // last read of this item's accumulators: the region is free
+                    if (last) {  // this warp's last read of the item's accumulators
                         asm volatile("tcgen05.fence::before_thread_sync;");
                         __syncwarp();
                         if (lane == 0)
@@ -614,23 +622,23 @@ __global__ void __launch_bounds__(kT4Threads, 1)
                     for (int ll = 0; ll < 8; ++ll) {
                         const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * ll]));
                         const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * ll + 1]));
-                        uint4 c4;
+                        uint2 c2;
                         if (PACK) {
-                            c4 = make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                            c2 = make_uint2((u0 & wmask) | (u1 & wmask) << 16, (u0 >> pack) | (u1 >> pack) << 16);
                         } else {
-                            c4 = make_uint4(u0, u1, __float2uint_rn(__uint_as_float(vt[2 * ll])),
-                                            __float2uint_rn(__uint_as_float(vt[2 * ll + 1])));
+                            c2 = make_uint2(u0 | u1 << 16, __float2uint_rn(__uint_as_float(vt[2 * ll])) |
+                                                               __float2uint_rn(__uint_as_float(vt[2 * ll + 1])) << 16);
                         }
-                        *reinterpret_cast<uint4*>(ebuf + 4 * t4_chunk(kkw, ll, xyz)) = c4;
+                        *reinterpret_cast<uint2*>(ebuf + 2 * t4_slot(kkw, ll, xyz)) = c2;
                     }
                 }
                 __syncwarp();
                 uint32_t cp[2][8];
 #pragma unroll
                 for (int r = 0; r < 8; ++r) {
-                    const uint4 c4 = *reinterpret_cast<const uint4*>(ebuf + 4 * t4_chunk(kkc, llc, r));
-                    cp[0][r] = c4.x | (c4.y << 16);
-                    cp[1][r] = c4.z | (c4.w << 16);
+                    const uint2 c2 = *reinterpret_cast<const uint2*>(ebuf + 2 * t4_slot(kkc, llc, r));
+                    cp[0][r] = c2.x;
+                    cp[1][r] = c2.y;
                 }
                 __syncwarp();
                 t4_eval<DIGEST>(w, sink, thr_q, dump, single, pairs, triples, it, cp, kl, i, j, 4 * q + kkc, l0,
