@@ -69,7 +69,7 @@ constexpr int kT3SI = 1024;                      // i rows of a stage (2 x 128 B
                                                  // rows' chunk c sit in different banks)
 constexpr int kT3EpiWarps = 8, kT3BuildWarps = 4;
 constexpr int kT3Threads = 32 * (2 + kT3BuildWarps + kT3EpiWarps);  // 448
-constexpr int kT3Ebuf = 4096;                    // per epilogue warp: 8 j x 8 l x 4 (x,y) x 16 B
+constexpr int kT3Ebuf = 2048;                    // per epilogue warp: 256 transpose slots of 8 B
 constexpr int kT3Stash = 32 * (kT3L / 2) * 4;    // per epilogue warp: 32 rows x 48 words (16-bit case pairs)
 constexpr size_t kT3Smem = 1024 + (size_t)kT3Stages * (kT3SB + kT3SJ + kT3SI) +
                            (size_t)kT3EpiWarps * (kT3Ebuf + kT3Stash);
@@ -141,12 +141,13 @@ __device__ __forceinline__ int t3x_j(int j0, long long p0, long long p_end, cons
     return p < p_end ? __ldg(jlist + p) : n;
 }
 
-// 16-byte chunk of the epilogue transpose buffer holding the 4 counts
-// (cases z0, z1, controls z0, z1) of row (jl, xy) and column group k; the XOR
-// makes both the row-wise writes and the combination-wise reads free of bank
-// conflicts (8 distinct chunk positions per quarter-warp).
-__device__ __forceinline__ int t3_chunk(int jl, int k, int xy) {
-    return (((jl * 8 + k) * 4) + xy) ^ (((k >> 1) & 3) | ((jl & 1) << 2));
+// 8-byte slot of the order-3 epilogue transpose buffer holding the counts
+// (cases z0 | z1 << 16, controls z0 | z1 << 16) of row (jl, xy) and column
+// group k; the XOR makes both the row-wise writes (lanes (jl, xy), fixed k)
+// and the combination-wise reads (lanes (jl, k / 2), fixed xy) cover the 32
+// banks once per half-warp.
+__device__ __forceinline__ int t3_slot(int jl, int k, int xy) {
+    return ((jl * 8 + k) * 4 + xy) ^ ((jl & 3) | (((jl ^ (k >> 1)) & 3) << 2));
 }
 
 // Float view of the packed 16-bit pair cores [class][x][y].
@@ -215,11 +216,11 @@ __device__ __forceinline__ void t3_eval(const ScanWork& w, const CandSink& sink,
     float core[2][8];
 #pragma unroll
     for (int x4 = 0; x4 < 4; ++x4) {
-        const uint4 c4 = *reinterpret_cast<const uint4*>(ebuf + 4 * t3_chunk(jl, k, x4));
-        core[0][2 * x4] = u2f(c4.x);
-        core[0][2 * x4 + 1] = u2f(c4.y);
-        core[1][2 * x4] = u2f(c4.z);
-        core[1][2 * x4 + 1] = u2f(c4.w);
+        const uint2 c2 = *reinterpret_cast<const uint2*>(ebuf + 2 * t3_slot(jl, k, x4));
+        core[0][2 * x4] = u2f(c2.x & 0xffffu);
+        core[0][2 * x4 + 1] = u2f(c2.x >> 16);
+        core[1][2 * x4] = u2f(c2.y & 0xffffu);
+        core[1][2 * x4 + 1] = u2f(c2.y >> 16);
     }
     uint4 pil = make_uint4(0, 0, 0, 0), pjl = pil, sl4 = pil;
     if (valid) {
@@ -595,12 +596,9 @@ __global__ void __launch_bounds__(kT3Threads, 1)
                     }
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
-                        uint4 c4;
-                        c4.x = su[k] & 0xffffu;
-                        c4.y = su[k] >> 16;
-                        c4.z = f2u(__uint_as_float(vt[2 * k]));
-                        c4.w = f2u(__uint_as_float(vt[2 * k + 1]));
-                        *reinterpret_cast<uint4*>(ebuf + 4 * t3_chunk(jl, k, xy)) = c4;
+                        const uint32_t t0 = f2u(__uint_as_float(vt[2 * k]));
+                        const uint32_t t1 = f2u(__uint_as_float(vt[2 * k + 1]));
+                        *reinterpret_cast<uint2*>(ebuf + 2 * t3_slot(jl, k, xy)) = make_uint2(su[k], t0 | t1 << 16);
                     }
                 }
                 __syncwarp();
@@ -952,8 +950,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPThreads, 1)
                     for (int k = 0; k < 8; ++k) {
                         const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * k]));
                         const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * k + 1]));
-                        *reinterpret_cast<uint4*>(ebuf + 4 * t3_chunk(jl, k, xy)) =
-                            make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                        *reinterpret_cast<uint2*>(ebuf + 2 * t3_slot(jl, k, xy)) =
+                            make_uint2((u0 & wmask) | (u1 & wmask) << 16, (u0 >> pack) | (u1 >> pack) << 16);
                     }
                 }
                 __syncwarp();
@@ -1022,11 +1020,12 @@ __device__ __forceinline__ void t2_decode(const long long* __restrict__ item_beg
     j0 = kT2L * b;
 }
 
-// 16-byte chunk of the order-2 transpose buffer holding (cases y0, y1, controls
-// y0, y1) of row (ii, x) and column group k; conflict-free for the row-wise
-// writes (fixed k) and the pair-wise reads (fixed x, k = 4 kh + kk).
-__device__ __forceinline__ int t2_chunk(int ii, int k, int x) {
-    return (((ii * 8 + k) * 2 + x) ^ ((ii & 3) << 1) ^ ((k >> 2) & 1));
+// 8-byte slot of the order-2 transpose buffer holding (cases y0 | y1 << 16,
+// controls y0 | y1 << 16) of row (ii, x) and column group k; each half-warp
+// covers the 32 banks once for the row-wise writes (lanes (ii, x), fixed k)
+// and the pair-wise reads (lanes (ii, kh), fixed x, k = 4 kh + kk).
+__device__ __forceinline__ int t2_slot(int ii, int k, int x) {
+    return ((((ii >> 3) * 4 + (k & 3)) * 2 + (k >> 2)) * 16) + (((ii & 7) << 1) | (x ^ (k >> 2)));
 }
 
 // Distribution layers of order-2 scans: the owned prefixes are the SNPs
@@ -1069,11 +1068,11 @@ __device__ __forceinline__ void t2_eval(const ScanWork& w, const CandSink& sink,
     float t[2][9];
 #pragma unroll
     for (int x = 0; x < 2; ++x) {
-        const uint4 c4 = *reinterpret_cast<const uint4*>(ebuf + 4 * t2_chunk(ii, k, x));
-        t[0][x * 3 + 0] = u2f(c4.x);
-        t[0][x * 3 + 1] = u2f(c4.y);
-        t[1][x * 3 + 0] = u2f(c4.z);
-        t[1][x * 3 + 1] = u2f(c4.w);
+        const uint2 c2 = *reinterpret_cast<const uint2*>(ebuf + 2 * t2_slot(ii, k, x));
+        t[0][x * 3 + 0] = u2f(c2.x & 0xffffu);
+        t[0][x * 3 + 1] = u2f(c2.x >> 16);
+        t[1][x * 3 + 0] = u2f(c2.y & 0xffffu);
+        t[1][x * 3 + 1] = u2f(c2.y >> 16);
     }
     // single cores of j = jg + k, loaded by lane k of the warp for the column group
     uint4 sj4;
@@ -1362,16 +1361,16 @@ __global__ void __launch_bounds__(kT2Threads, 1)
                     }
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
-                        uint4 c4;
+                        uint2 c2;
                         if (pack) {
                             const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * k]));
                             const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * k + 1]));
-                            c4 = make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                            c2 = make_uint2((u0 & wmask) | (u1 & wmask) << 16, (u0 >> pack) | (u1 >> pack) << 16);
                         } else {
-                            c4 = make_uint4(f2u(__uint_as_float(v[2 * k])), f2u(__uint_as_float(v[2 * k + 1])),
-                                            f2u(__uint_as_float(vt[2 * k])), f2u(__uint_as_float(vt[2 * k + 1])));
+                            c2 = make_uint2(f2u(__uint_as_float(v[2 * k])) | f2u(__uint_as_float(v[2 * k + 1])) << 16,
+                                            f2u(__uint_as_float(vt[2 * k])) | f2u(__uint_as_float(vt[2 * k + 1])) << 16);
                         }
-                        *reinterpret_cast<uint4*>(ebuf + 4 * t2_chunk(ii, k, x)) = c4;
+                        *reinterpret_cast<uint2*>(ebuf + 2 * t2_slot(ii, k, x)) = c2;
                     }
                 }
                 __syncwarp();
@@ -1645,16 +1644,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kT2Threads, 1)
                     }
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
-                        uint4 c4;
+                        uint2 c2;
                         if (pack) {
                             const uint32_t u0 = __float2uint_rn(__uint_as_float(v[2 * k]));
                             const uint32_t u1 = __float2uint_rn(__uint_as_float(v[2 * k + 1]));
-                            c4 = make_uint4(u0 & wmask, u1 & wmask, u0 >> pack, u1 >> pack);
+                            c2 = make_uint2((u0 & wmask) | (u1 & wmask) << 16, (u0 >> pack) | (u1 >> pack) << 16);
                         } else {
-                            c4 = make_uint4(f2u(__uint_as_float(v[2 * k])), f2u(__uint_as_float(v[2 * k + 1])),
-                                            f2u(__uint_as_float(vt[2 * k])), f2u(__uint_as_float(vt[2 * k + 1])));
+                            c2 = make_uint2(f2u(__uint_as_float(v[2 * k])) | f2u(__uint_as_float(v[2 * k + 1])) << 16,
+                                            f2u(__uint_as_float(vt[2 * k])) | f2u(__uint_as_float(vt[2 * k + 1])) << 16);
                         }
-                        *reinterpret_cast<uint4*>(ebuf + 4 * t2_chunk(ii, k, x)) = c4;
+                        *reinterpret_cast<uint2*>(ebuf + 2 * t2_slot(ii, k, x)) = c2;
                     }
                 }
                 __syncwarp();
