@@ -9,6 +9,12 @@
 
   - ``libref_base.so``: ``src/base/{gt_combine,gt_popcnt,mi_compute}.cpp``,
     no ``ALIGN`` (the portable scalar build);
+  - ``libref_base_seg.so``: the same with ``-DSEGMENT_SIZE=1474560``
+    (``src/CMakeLists.txt:260-262``): ``ThreadedSearch`` runs its segmented
+    search (``ThreadedSearch.h:65-69,79-140``);
+  - ``libref_bench.so``: ``oracle/ref/bench_driver.cpp`` over the two
+    sequential benchmark programs (``benchmarks/*_sequential_search.cpp``,
+    their depth-first ``stack_search``) with the scalar kernels;
   - ``libref_avx512.so``: ``src/avx512bw/{gt_combine,gt_popcnt_avx512bw_lu,
     mi_compute_512}.cpp`` with ``-DALIGN=64 -march=native -ffast-math -lmvec``
     (the reference's default build on an AVX-512BW CPU without VPOPCNTDQ,
@@ -86,6 +92,19 @@ def build_ref(force: bool = False) -> dict:
     if force or _stale(out, [driver, shim, digest_h] + base_srcs):
         _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread"] + inc + [driver] + base_srcs + ["-o", out])
     built["base"] = out
+    out = os.path.join(REF_OUT, "libref_base_seg.so")
+    if force or _stale(out, [driver, shim, digest_h] + base_srcs):
+        _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread", "-DSEGMENT_SIZE=1474560"] + inc +
+             [driver] + base_srcs + ["-o", out])
+    built["base_seg"] = out
+    bench_driver = os.path.join(HERE, "ref", "bench_driver.cpp")
+    bench_srcs = [os.path.join(REF_ROOT, "benchmarks", f)
+                  for f in ("nonsegmented_sequential_search.cpp", "segmented_sequential_search.cpp", "utils.h")]
+    out = os.path.join(REF_OUT, "libref_bench.so")
+    if force or _stale(out, [bench_driver, shim] + bench_srcs + base_srcs):
+        _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread"] + inc +
+             ["-I", os.path.join(REF_ROOT, "benchmarks"), bench_driver] + base_srcs + ["-o", out])
+    built["bench"] = out
     if _has_avx512bw():
         d = os.path.join(REF_ROOT, "src", "avx512bw")
         srcs = [os.path.join(d, f) for f in ("gt_combine.cpp", "gt_popcnt_avx512bw_lu.cpp", "mi_compute_512.cpp")]

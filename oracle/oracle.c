@@ -475,3 +475,139 @@ long orc_table_digest(const uint64_t *data, size_t snps, size_t cases_words, siz
     *digest = sum;
     return (long)combos;
 }
+
+/* ------------------------------------------------------------------------ */
+/* The depth-first traversal of the reference's sequential benchmark programs
+ * (stack_search in benchmarks/nonsegmented_sequential_search.cpp:31-104 and
+ * benchmarks/segmented_sequential_search.cpp:31-117): for each first SNP i
+ * ascending, the pairs (i, j) go onto a stack with j ascending; a popped
+ * combination shorter than the order gets its genotype table (combine of its
+ * parent's table with its last SNP) and pushes its children (last SNP + 1 ..
+ * n - 1, ascending); a popped combination of full order is counted
+ * (combine_and_popcnt of its parent's table with its last SNP).  So the
+ * combinations are visited first SNP ascending, the rest in descending
+ * lexicographic order.  The segmented program collects `block` tables before
+ * computing their MI and feeding the MaxArray in visiting order (block = 1 is
+ * the non-segmented program; the benchmarks use 1 474 560 / 3^order).
+ * mi_mode as in orc_search.  Returns the number of results written. */
+typedef struct {
+    int size;
+    int32_t pos[ORC_MAX_ORDER];
+} orc_node;
+
+long orc_search_dfs(const uint64_t *data, size_t snps, size_t n_cases, size_t n_ctrls, size_t cw, size_t tw,
+                    int order, size_t block, unsigned outputs, int mi_mode, int32_t *out_combos, float *out_vals,
+                    double *out_vals64, uint64_t *combos_done)
+{
+    if (order < 2 || order > ORC_MAX_ORDER || block < 1 || snps < 2) return -1;
+    const size_t per_snp = 3 * (cw + tw);
+    size_t cells = 1;
+    for (int i = 0; i < order; ++i) cells *= 3;
+    /* genotype table of the combination of size s on the current path: rows 3^s */
+    uint64_t *gc[ORC_MAX_ORDER + 1] = {0}, *gt[ORC_MAX_ORDER + 1] = {0};
+    size_t rows = 3;
+    for (int s = 2; s < order; ++s) {
+        rows *= 3;
+        gc[s] = (uint64_t *)malloc(rows * cw * sizeof(uint64_t) + 8);
+        gt[s] = (uint64_t *)malloc(rows * tw * sizeof(uint64_t) + 8);
+    }
+    /* at most (order - 1) levels of at most snps children each are stacked at once */
+    const size_t stack_cap = snps * (size_t)order;
+    orc_node *stack = (orc_node *)malloc(stack_cap * sizeof(orc_node));
+    uint32_t *bc = (uint32_t *)malloc(block * cells * sizeof(uint32_t));
+    uint32_t *bt = (uint32_t *)malloc(block * cells * sizeof(uint32_t));
+    orc_result *br = (orc_result *)calloc(block, sizeof(orc_result));
+    orc_maxarray max = {(orc_result *)calloc(outputs ? outputs : 1, sizeof(orc_result)), outputs, 0, 0};
+    size_t top = 0, filled = 0;
+    uint64_t combos = 0;
+    long rc = 0;
+    for (int i = 0; i < (int)snps && rc == 0; ++i) {
+        for (int j = i + 1; j < (int)snps; ++j) {
+            orc_node nd;
+            memset(&nd, 0, sizeof(nd));
+            nd.size = 2;
+            nd.pos[0] = i;
+            nd.pos[1] = j;
+            stack[top++] = nd;
+        }
+        while (top > 0) {
+            const orc_node nd = stack[--top];
+            const int s = nd.size, last = nd.pos[s - 1];
+            /* the parent's table: SNP pos[0] itself for a pair, else the path's table of size s - 1 */
+            const uint64_t *pc = s == 2 ? data + (size_t)nd.pos[0] * per_snp : gc[s - 1];
+            const uint64_t *pt = s == 2 ? pc + 3 * cw : gt[s - 1];
+            size_t prow = 1;
+            for (int q = 1; q < s; ++q) prow *= 3;
+            const uint64_t *lc = data + (size_t)last * per_snp, *lt = lc + 3 * cw;
+            if (s == order) {
+                orc_popcnt(pc, prow, lc, cw, bc + filled * cells, cells);
+                orc_popcnt(pt, prow, lt, tw, bt + filled * cells, cells);
+                memset(&br[filled], 0, sizeof(orc_result));
+                for (int q = 0; q < order; ++q) br[filled].c[q] = nd.pos[q];
+                if (++filled == block) {
+                    for (size_t b = 0; b < filled; ++b) {
+                        const uint32_t *tc = bc + b * cells, *tt = bt + b * cells;
+                        if (mi_mode == 0) {
+                            br[b].val = orc_mi_f32(tc, tt, cells, (uint32_t)n_cases, (uint32_t)n_ctrls);
+                            br[b].val64 = br[b].val;
+                        } else {
+                            br[b].val64 = orc_mi_f64(tc, tt, cells, (uint32_t)n_cases, (uint32_t)n_ctrls);
+                            br[b].val = (float)br[b].val64;
+                        }
+                        orc_max_add(&max, &br[b], mi_mode == 1);
+                    }
+                    combos += filled;
+                    filled = 0;
+                }
+            } else {
+                orc_combine(pc, prow, lc, cw, gc[s]);
+                orc_combine(pt, prow, lt, tw, gt[s]);
+                if (top + snps > stack_cap) {
+                    rc = -2;
+                    break;
+                }
+                for (int l = last + 1; l < (int)snps; ++l) {
+                    orc_node ch = nd;
+                    ch.size = s + 1;
+                    ch.pos[s] = l;
+                    stack[top++] = ch;
+                }
+            }
+        }
+    }
+    for (size_t b = 0; b < filled; ++b) { /* the last, partial block */
+        const uint32_t *tc = bc + b * cells, *tt = bt + b * cells;
+        if (mi_mode == 0) {
+            br[b].val = orc_mi_f32(tc, tt, cells, (uint32_t)n_cases, (uint32_t)n_ctrls);
+            br[b].val64 = br[b].val;
+        } else {
+            br[b].val64 = orc_mi_f64(tc, tt, cells, (uint32_t)n_cases, (uint32_t)n_ctrls);
+            br[b].val = (float)br[b].val64;
+        }
+        orc_max_add(&max, &br[b], mi_mode == 1);
+    }
+    combos += filled;
+    for (int s = 2; s < order; ++s) { free(gc[s]); free(gt[s]); }
+    free(stack);
+    free(bc);
+    free(bt);
+    free(br);
+    if (rc) {
+        free(max.a);
+        return rc;
+    }
+    pthread_mutex_lock(&g_sort_lock);
+    g_cmp_order = order;
+    g_cmp_by64 = mi_mode == 1;
+    qsort(max.a, max.size, sizeof(orc_result), orc_cmp_desc);
+    pthread_mutex_unlock(&g_sort_lock);
+    const size_t nout = max.size < outputs ? max.size : outputs;
+    for (size_t i = 0; i < nout; ++i) {
+        for (int j = 0; j < order; ++j) out_combos[i * order + j] = max.a[i].c[j];
+        out_vals[i] = max.a[i].val;
+        if (out_vals64) out_vals64[i] = max.a[i].val64;
+    }
+    free(max.a);
+    if (combos_done) *combos_done = combos;
+    return (long)nout;
+}

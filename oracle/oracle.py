@@ -50,6 +50,9 @@ class Oracle:
         L.orc_table_digest.argtypes = [_u64p, C.c_size_t, C.c_size_t, C.c_size_t, C.c_int, C.c_int, C.c_int,
                                        C.c_int, C.c_int, C.POINTER(C.c_uint64)]
         L.orc_table_digest.restype = C.c_long
+        L.orc_search_dfs.argtypes = [_u64p, C.c_size_t, C.c_size_t, C.c_size_t, C.c_size_t, C.c_size_t, C.c_int,
+                                     C.c_size_t, C.c_uint, C.c_int, _i32p, _f32p, _f64p, C.POINTER(C.c_uint64)]
+        L.orc_search_dfs.restype = C.c_long
         self.L = L
 
     # -- data model ---------------------------------------------------------
@@ -120,6 +123,20 @@ class Oracle:
             raise ValueError("oracle search: invalid arguments")
         return combos[: r * order].reshape(r, order), v32[:r], v64[:r], int(done.value)
 
+
+    def search_dfs(self, data, snps, n_cases, n_ctrls, cases_words, ctrls_words, order, outputs, block=1,
+                   mi_mode=1):
+        """The benchmark programs' depth-first traversal (block tables per MI batch; 1 = non-segmented).
+        Returns (combos[n, order] int32, vals float32, vals64 float64, combos evaluated)."""
+        combos = np.zeros(max(outputs, 1) * order, np.int32)
+        v32 = np.zeros(max(outputs, 1), np.float32)
+        v64 = np.zeros(max(outputs, 1), np.float64)
+        done = C.c_uint64(0)
+        r = self.L.orc_search_dfs(np.ascontiguousarray(data, np.uint64), snps, n_cases, n_ctrls, cases_words,
+                                  ctrls_words, order, block, outputs, mi_mode, combos, v32, v64, C.byref(done))
+        if r < 0:
+            raise ValueError("oracle depth-first search: invalid arguments")
+        return combos[: r * order].reshape(r, order), v32[:r], v64[:r], int(done.value)
 
     def table_digest(self, data, snps, cases_words, ctrls_words, order, threads=1, dist=None):
         """Digest (oracle/ref/tabledigest.h) of every table of a scan: (digest, combinations)."""
@@ -232,3 +249,29 @@ class RefDataset:
         mi = np.zeros(q, np.float32)
         self.ref.L.ref_tables(self.h, order, combos, q, cc, tt, mi)
         return cc, tt, mi
+
+
+class ReferenceBench:
+    """The reference's sequential benchmark programs' depth-first traversal
+    (oracle/ref/bench_driver.cpp, built from their sources by oracle/build.py)."""
+
+    def __init__(self):
+        built = _build.build_ref()
+        if "bench" not in built:
+            raise FileNotFoundError("reference benchmark build not available")
+        L = C.CDLL(built["bench"])
+        L.ref_stack_search.argtypes = [_u64p, C.c_size_t, C.c_size_t, C.c_size_t, C.c_size_t, C.c_size_t, C.c_int,
+                                       C.c_int, C.c_uint, _i32p, _f32p]
+        L.ref_stack_search.restype = C.c_long
+        self.L = L
+
+    def stack_search(self, data, snps, cases, ctrls, cw, tw, order, outputs, segmented):
+        """stack_search of the segmented or non-segmented program: (combos[n, order], vals float32),
+        by descending value."""
+        combos = np.zeros(max(outputs, 1) * order, np.int32)
+        vals = np.zeros(max(outputs, 1), np.float32)
+        r = self.L.ref_stack_search(np.ascontiguousarray(data, np.uint64), snps, cases, ctrls, cw, tw, order,
+                                    int(bool(segmented)), outputs, combos, vals)
+        if r < 0:
+            raise RuntimeError("reference stack_search failed")
+        return combos[: r * order].reshape(r, order), vals[:r]

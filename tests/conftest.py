@@ -30,3 +30,9 @@ def golden_testdata():
 def golden_synth():
     import numpy as np
     return dict(np.load(os.path.join(GOLDEN, "reference_synth.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_traversals():
+    import numpy as np
+    return dict(np.load(os.path.join(GOLDEN, "reference_traversals.npz")))

@@ -706,3 +706,27 @@ def test_order2_40000x16000_top1000(oracle):
                   [x.combination for x in a])
     assert np.allclose(av, ex, rtol=1e-9, atol=0)
     assert_sorted_desc(av)
+
+
+# ------------------------------------------------ segmented evaluation and depth-first traversals
+@pytest.mark.parametrize("name", ["o2", "o3", "o4", "ties"])
+def test_search_vs_reference_traversals(gs, oracle, golden_traversals, name):
+    """The GPU list against the reference's segmented ThreadedSearch and its two depth-first
+    benchmark programs (benchmarks/*_sequential_search.cpp): the same combinations up to ties
+    at the cut-off; with the cut-off inside a group of equal values the GPU keeps what
+    ThreadedSearch keeps (its visiting order), while the depth-first programs keep another
+    member of the group."""
+    from fiuncho_gb300 import Dataset, Distribution
+    g = golden_traversals
+    ds = Dataset.from_genotypes(g[name + "_geno"], g[name + "_is_case"])
+    order, outputs = (int(x) for x in g[name + "_meta"])
+    res, v64 = gs.run(ds, order, Distribution(ds.snps, order - 1), outputs, with_fp64=True)
+    got = _check_topn(oracle, ds, order, outputs, res, v64)
+    ex = lambda cs: exact_mi(oracle, ds.data, ds.cases_words, ds.ctrls_words, ds.cases, ds.ctrls, order, cs)
+    for tag in ("seg", "dfs", "dfsseg"):
+        rc = g[name + "_%s_combos" % tag]
+        rv = g[name + "_%s_vals" % tag].astype(np.float64)
+        assert_topn_equivalent(got, rc, ex, 2 * float(np.max(np.abs(rv - ex(rc)))) + 1e-12)
+    if name == "ties":
+        assert as_set(got) == as_set(g["ties_seg_combos"])
+        assert as_set(got) != as_set(g["ties_dfs_combos"])

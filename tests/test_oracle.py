@@ -264,3 +264,55 @@ def test_scale_fixture_layout():
         assert_ascending_unique(c)
         assert_sorted_desc(v)
         assert len(str(g[name + "_sha256"])) == 64
+
+
+# ------------------------------------------------ segmented evaluation and depth-first traversals
+TRAVERSAL_CASES = ["o2", "o3", "o4", "ties"]
+
+
+def _traversal_case(g, name):
+    from fiuncho_gb300.dataset import Dataset
+    ds = Dataset.from_genotypes(g[name + "_geno"], g[name + "_is_case"])
+    order, outputs = (int(x) for x in g[name + "_meta"])
+    return ds, order, outputs
+
+
+def _by_value_then_combo(combos, vals):
+    """A list ordered by descending value, ties by ascending combination (order-free comparison)."""
+    return sorted(zip((-float(v) for v in vals), map(tuple, np.asarray(combos).tolist())))
+
+
+@pytest.mark.parametrize("name", TRAVERSAL_CASES)
+def test_depth_first_traversal_matches_reference(oracle, golden_traversals, name):
+    """The oracle's depth-first traversal (stack_search of the benchmark programs, segmented
+    and not) returns the reference programs' MaxArray content, ties at the cut-off included."""
+    g = golden_traversals
+    ds, order, outputs = _traversal_case(g, name)
+    args = (ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words, order, outputs)
+    for tag, block in (("dfs", 1), ("dfsseg", 1474560 // 3 ** order)):
+        c, v, _, n = oracle.search_dfs(*args, block=block, mi_mode=0)
+        assert n == math.comb(ds.snps, order)
+        assert _by_value_then_combo(c, v) == _by_value_then_combo(g[name + "_%s_combos" % tag],
+                                                                   g[name + "_%s_vals" % tag])
+
+
+@pytest.mark.parametrize("name", TRAVERSAL_CASES)
+def test_segmented_threaded_search_matches_oracle(oracle, golden_traversals, name):
+    """ThreadedSearch built with SEGMENT_SIZE (MI in blocks, MaxArray fed in the same order)
+    returns exactly the non-segmented list, which the oracle restates."""
+    g = golden_traversals
+    ds, order, outputs = _traversal_case(g, name)
+    c, v, _, _ = oracle.search(ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words, order,
+                               outputs, mi_mode=0)
+    assert _by_value_then_combo(c, v) == _by_value_then_combo(g[name + "_seg_combos"], g[name + "_seg_vals"])
+
+
+def test_traversal_order_decides_ties(golden_traversals):
+    """With duplicated SNP columns the cut-off falls inside a group of equal MI values: the
+    depth-first programs keep a different tied combination than ThreadedSearch, with the
+    same value list."""
+    g = golden_traversals
+    a = set(map(tuple, g["ties_dfs_combos"].tolist()))
+    b = set(map(tuple, g["ties_seg_combos"].tolist()))
+    assert a != b and len(a ^ b) == 2
+    assert np.array_equal(np.sort(g["ties_dfs_vals"]), np.sort(g["ties_seg_vals"]))
