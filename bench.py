@@ -438,8 +438,10 @@ def run_batch_and_serve(args, gs, ctx):
 
     The served stream draws full-size scans (no truncation) from the same 64
     at Poisson(`--serve-rate`) for `--serve-seconds` against a 120 GB device
-    budget; at the end of the arrival window the backlog is recorded and the
-    server is destroyed (scans still running are cancelled)."""
+    budget, admitted and run in `--serve-policy` order (shortest-first by
+    default: the offered load is far above the device's throughput); at the
+    end of the arrival window the backlog is recorded and the server is
+    destroyed (scans still running are cancelled)."""
     import ctypes as C
     import random
 
@@ -517,7 +519,8 @@ def run_batch_and_serve(args, gs, ctx):
         if tnow >= duration:
             break
         arrivals.append((tnow, rng.randrange(len(data))))
-    srv = Server(ctx.device, budget_bytes=120 * 1000 ** 3)
+    policy = Server.SHORTEST_FIRST if args.serve_policy == "shortest" else Server.FIFO
+    srv = Server(ctx.device, budget_bytes=120 * 1000 ** 3, policy=policy)
     lat, done_idx, pending = [], [], []
     try:
         t0 = time.perf_counter()
@@ -568,6 +571,8 @@ def run_batch_and_serve(args, gs, ctx):
     out["served"] = {
         "workload": "Poisson arrivals of full-size scans drawn uniformly from the 64 above (configuration 5), "
                     "120 GB device budget",
+        "policy": "shortest-first (least combinations x samples taken first)" if policy == Server.SHORTEST_FIRST
+                  else "fifo (submission order)",
         "offered_scans_per_s": rate, "duration_s": duration, "requests": len(arrivals),
         "offered_combos_samples_per_s": offered_work / duration,
         "completed": int(st["completed"]), "completed_scans_per_s": st["completed"] / window,
@@ -599,6 +604,8 @@ def main():
     ap.add_argument("--profile-layer", default="", metavar="STEP,OFFSET",
                     help="profiling case: search Distribution(snps, order-1, STEP, OFFSET) twice and exit")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="served stream: Poisson arrivals per second")
+    ap.add_argument("--serve-policy", default="shortest", choices=["shortest", "fifo"],
+                    help="served stream: order in which queued scans are admitted and run")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="served stream: arrival window (60 s, the served configuration's loop)")
     ap.add_argument("--batch-cap", type=float, default=2e12,

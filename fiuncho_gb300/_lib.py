@@ -98,6 +98,7 @@ _SIGS = {
     "fiu_mi_compute_noalloc": (C.c_int, [_vp, _vp, C.c_size_t, C.c_size_t, C.c_uint, C.c_uint, _vp, _vp]),
     "fiu_search_batch": (C.c_int, [_vp, C.POINTER(Scan_t), C.c_uint, C.c_int]),
     "fiu_server_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_vp)]),
+    "fiu_server_set_policy": (C.c_int, [_vp, C.c_int]),
     "fiu_server_submit": (C.c_int, [_vp, C.POINTER(Dataset_t), C.c_uint, C.c_uint, C.POINTER(C.c_uint64)]),
     "fiu_server_submit_shard": (C.c_int, [_vp, C.POINTER(Dataset_t), C.c_uint, C.c_uint, C.c_uint, C.c_uint,
                                           C.POINTER(C.c_uint64)]),

@@ -60,6 +60,7 @@ struct ServeScan {
     unsigned shard = 0, n_shards = 1;  // shard of the scan's work units (fiu_server_submit_shard)
     long long m_end = 0;               // end of the shard's prefix ordinals (round scans)
     size_t bytes = 0;
+    double work = 0;  // combinations x samples of the scan (its shard): the shortest-first key
     char* buf = nullptr;
     size_t off_scored = 0, off_comb = 0, off_val = 0, off_val64 = 0;
     int status = FIU_OK;
@@ -91,6 +92,7 @@ size_t footprint(const ServeScan& s) {
 struct fiu_server {
     fiu_ctx* ctx = nullptr;
     uint64_t budget = 0;
+    int policy = FIU_SERVE_FIFO;  // order in which queued scans are admitted and solo lanes pick (under mu)
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<ServeScan*> queue;
@@ -355,8 +357,18 @@ int run_round(fiu_server* sv) {
     return FIU_OK;
 }
 
-// A solo lane: takes scans that run alone from the shared FIFO and runs each
-// on the lane's own stream.
+// Position of the scan a queue hands out next: its head (FIFO) or, under
+// FIU_SERVE_SHORTEST_FIRST, the scan of least work (the earliest of equals).
+size_t next_of(const fiu_server* sv, const std::deque<ServeScan*>& q) {
+    size_t best = 0;
+    if (sv->policy == FIU_SERVE_SHORTEST_FIRST)
+        for (size_t i = 1; i < q.size(); ++i)
+            if (q[i]->work < q[best]->work) best = i;
+    return best;
+}
+
+// A solo lane: takes scans that run alone from the shared queue (in the
+// server's policy order) and runs each on the lane's own stream.
 void solo_main(fiu_server* sv, int lane) {
     fiu_ctx* ctx = sv->solo_ctx[lane];
     Scope scope(ctx);
@@ -366,8 +378,9 @@ void solo_main(fiu_server* sv, int lane) {
             std::unique_lock<std::mutex> g(sv->mu);
             sv->cv_solo.wait(g, [&] { return sv->stop || !sv->solo_queue.empty(); });
             if (sv->stop) return;
-            s = sv->solo_queue.front();
-            sv->solo_queue.pop_front();
+            const size_t at = next_of(sv, sv->solo_queue);
+            s = sv->solo_queue[at];
+            sv->solo_queue.erase(sv->solo_queue.begin() + (long)at);
             start_run(sv, s);
         }
         fiu_distribution dist{(int)s->host.snps, (int)s->order - 1, 1, 0};
@@ -384,19 +397,20 @@ void solo_main(fiu_server* sv, int lane) {
 void worker_main(fiu_server* sv) {
     Scope scope(sv->ctx);
     for (;;) {
-        // admit while the head of the queue fits the budget
+        // admit while the next scan of the queue (policy order) fits the budget
         for (;;) {
             ServeScan* s = nullptr;
             {
                 std::unique_lock<std::mutex> g(sv->mu);
                 if (sv->stop) return;
                 if (sv->queue.empty() || sv->free_slots.empty()) break;
-                ServeScan* h = sv->queue.front();
+                const size_t at = next_of(sv, sv->queue);
+                ServeScan* h = sv->queue[at];
                 // every admitted scan holds its footprint until it finishes, whether it runs
                 // in the rounds or waits for / runs on a solo lane; a scan larger than the
                 // budget left runs only when nothing else holds device memory
                 if (sv->bytes_in_use + h->bytes > sv->budget && sv->bytes_in_use > 0) break;
-                sv->queue.pop_front();
+                sv->queue.erase(sv->queue.begin() + (long)at);
                 sv->bytes_in_use += h->bytes;
                 sv->peak_bytes = std::max(sv->peak_bytes, sv->bytes_in_use);
                 s = h;
@@ -471,6 +485,13 @@ int fiu_server_create(int device, uint64_t budget_bytes, fiu_server** out) {
     return FIU_OK;
 }
 
+int fiu_server_set_policy(fiu_server* sv, int policy) {
+    if (!sv || (policy != FIU_SERVE_FIFO && policy != FIU_SERVE_SHORTEST_FIRST)) return FIU_ERR_INVALID;
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->policy = policy;
+    return FIU_OK;
+}
+
 int fiu_server_submit(fiu_server* sv, const fiu_dataset* d, unsigned order, unsigned outputs, uint64_t* ticket) {
     return fiu_server_submit_shard(sv, d, order, outputs, 0, 1, ticket);
 }
@@ -490,6 +511,7 @@ int fiu_server_submit_shard(fiu_server* sv, const fiu_dataset* d, unsigned order
     s->order = order;
     s->outputs = outputs;
     s->bytes = footprint(*s);
+    s->work = (double)binom((long long)d->snps, (int)order) / n_shards * (double)(d->cases + d->ctrls);
     s->submitted = Clock::now();
     std::lock_guard<std::mutex> g(sv->mu);
     if (s->bytes > sv->budget) {

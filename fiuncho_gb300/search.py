@@ -355,13 +355,20 @@ class Server:
     any time; they are admitted against a device-memory budget and run with
     continuous batching.  ``result`` returns (results, fp64 values, latency ms)."""
 
-    def __init__(self, device: int = 0, budget_bytes: int = 0):
+    FIFO, SHORTEST_FIRST = 0, 1  # admission / solo-lane order (fiu_server_set_policy)
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0, policy: int = 0):
         self.lib = _lib.load()
         h = C.c_void_p()
         rc = self.lib.fiu_server_create(int(device), int(budget_bytes), C.byref(h))
         if rc:
             raise FiunchoError(rc, "cannot create a server on CUDA device %d" % device)
         self.h = h
+        if policy:
+            rc = self.lib.fiu_server_set_policy(self.h, int(policy))
+            if rc:
+                self.lib.fiu_server_destroy(self.h)
+                raise FiunchoError(rc, "unknown serving policy %d" % policy)
         self._orders = {}
         self._keep = {}
 

@@ -239,6 +239,16 @@ typedef struct {
  * admitted scans leave, whichever lane then runs it; scans larger than the
  * whole budget are rejected at submit. */
 int fiu_server_create(int device, uint64_t budget_bytes, fiu_server **out);
+/* Order in which queued scans are admitted and the solo lanes take them:
+ * FIU_SERVE_FIFO (the default: submission order) or FIU_SERVE_SHORTEST_FIRST
+ * (least combinations x samples first, submission order among equals).  Under
+ * an offered load above the device's throughput shortest-first completes the
+ * small scans with short latency while the largest wait; FIFO bounds every
+ * scan's wait by the work submitted before it.  Applies to scans not yet
+ * taken. */
+#define FIU_SERVE_FIFO 0
+#define FIU_SERVE_SHORTEST_FIRST 1
+int fiu_server_set_policy(fiu_server *srv, int policy);
 /* Queues a scan of the whole data set (Distribution(snps, order-1, 1, 0)). */
 int fiu_server_submit(fiu_server *srv, const fiu_dataset *dataset, unsigned order, unsigned outputs,
                       uint64_t *ticket);

@@ -176,3 +176,38 @@ def test_server_destroy_cancels_running_scans():
     t0 = time.perf_counter()
     srv.close()
     assert time.perf_counter() - t0 < 0.6
+
+
+def test_server_shortest_first():
+    """FIU_SERVE_SHORTEST_FIRST: with both solo lanes busy on two long scans, queued scans are
+    taken least work first (the smallest finishes before the largest starts), and every
+    result is the scan's result alone."""
+    from fiuncho_gb300 import Distribution, GpuSearch, Server
+    gs = GpuSearch(0)
+    long_ds = [_ds(40 + i, 2000, 4000, 4000) for i in range(2)]
+    small = [(50, 3000, 1000, 1000), (51, 2000, 1000, 1000), (52, 1000, 1000, 1000), (53, 400, 1000, 1000)]
+    small_ds = [_ds(*m) for m in small]
+    ref_long = [gs.run(ds, 3, Distribution(ds.snps, 2), 20, with_fp64=True) for ds in long_ds]
+    ref_small = [gs.run(ds, 2, Distribution(ds.snps, 1), 20, with_fp64=True) for ds in small_ds]
+    with pytest.raises(Exception):
+        Server(0, policy=7)
+    srv = Server(0, policy=Server.SHORTEST_FIRST)
+    try:
+        tl = [srv.submit(ds, 3, 20) for ds in long_ds]
+        time.sleep(0.03)  # both lanes take a long scan
+        ts, t0 = [], []
+        for ds in small_ds:  # largest first
+            t0.append(time.perf_counter())
+            ts.append(srv.submit(ds, 2, 20))
+        done = []
+        for t, s0, r in zip(ts, t0, ref_small):
+            res, v64, lat = srv.result(t)
+            _same((res, v64, lat), r)
+            done.append(s0 + lat / 1e3)
+        for t, r in zip(tl, ref_long):
+            _same(srv.result(t), r)
+        assert done[3] < done[0], done
+        st = srv.stats()
+        assert st["completed"] == 6 and st["failed"] == 0
+    finally:
+        srv.close()
