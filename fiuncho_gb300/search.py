@@ -367,7 +367,7 @@ class Server:
         if policy:
             rc = self.lib.fiu_server_set_policy(self.h, int(policy))
             if rc:
-                self.lib.fiu_server_destroy(self.h)
+                self.close()  # destroys the server once and drops the handle
                 raise FiunchoError(rc, "unknown serving policy %d" % policy)
         self._orders = {}
         self._keep = {}

@@ -99,3 +99,30 @@ def test_pack_partial_word_right_aligned(oracle):
         is_case[rng.permutation(n_case + n_ctrl)[:n_case]] = 1
         cw, tw = words_for(n_case) + 1, max(words_for(n_ctrl), 1)
         assert np.array_equal(pack_rows(geno, is_case, cw, tw), oracle.pack(geno, is_case, cw, tw))
+
+
+def test_server_rejected_policy_destroys_once(monkeypatch):
+    """A refused serving policy destroys the new server exactly once (no second destroy
+    when the Python object is collected)."""
+    import gc
+
+    from fiuncho_gb300 import _lib, search
+
+    calls = []
+
+    class FakeLib:
+        def fiu_server_create(self, dev, budget, ph):
+            ph._obj.value = 1234
+            return 0
+
+        def fiu_server_set_policy(self, h, policy):
+            return 1
+
+        def fiu_server_destroy(self, h):
+            calls.append(h)
+
+    monkeypatch.setattr(_lib, "load", lambda: FakeLib())
+    with pytest.raises(search.FiunchoError):
+        search.Server(0, policy=7)
+    gc.collect()
+    assert len(calls) == 1
