@@ -316,3 +316,19 @@ def test_traversal_order_decides_ties(golden_traversals):
     b = set(map(tuple, g["ties_seg_combos"].tolist()))
     assert a != b and len(a ^ b) == 2
     assert np.array_equal(np.sort(g["ties_dfs_vals"]), np.sort(g["ties_seg_vals"]))
+
+
+@pytest.mark.parametrize("order", [2, 3, 4])
+def test_segmented_blocks_do_not_change_the_list(oracle, order):
+    """MI in blocks of any size feeds the MaxArray in the same visiting order, so the
+    segmented traversal returns the non-segmented list exactly (values and ties)."""
+    from fiuncho_gb300 import Dataset, synth
+    spec = synth.ScanSpec(26 if order < 4 else 18, 211, 190, order, 17, seed=31 + order)
+    g, c, _ = synth.simulate(spec)
+    g[5] = g[2]  # a duplicated column: ties in the list
+    ds = Dataset.from_genotypes(g, c)
+    args = (ds.data, ds.snps, ds.cases, ds.ctrls, ds.cases_words, ds.ctrls_words, order, spec.outputs)
+    base = oracle.search_dfs(*args, block=1, mi_mode=0)
+    for block in (2, 7, 1000, 10 ** 6):
+        got = oracle.search_dfs(*args, block=block, mi_mode=0)
+        assert np.array_equal(got[0], base[0]) and np.array_equal(got[1], base[1]) and got[3] == base[3]
