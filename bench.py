@@ -346,7 +346,10 @@ def run_gpu(args, spec):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * my_time / args.steps, "step_ms": [round(x, 3) for x in step_ms],
         "higher_is_better": True, "scaling": "strong",  # the one scan's work units split over the ranks
-        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "e4m3", "data": "synthetic",
+        "arithmetic": "one-hot data: e4m3 0/1 operands on the tensor cores with FP32 accumulation (exact integer "
+                      "counts below 2^24), derived cells in int32, MI keys in int64 fixed point, the kept candidates "
+                      "re-scored in FP64; other data: uint64 AND + POPC",
         "config": {"workload": args.workload, "snps": spec.snps, "cases": spec.cases, "ctrls": spec.ctrls,
                    "order": spec.order, "outputs": spec.outputs, "combinations": total_combos,
                    "parallelism": "work-unit shards over %d rank(s)" % ws,
